@@ -1,0 +1,256 @@
+/*
+ * illume-gb300: C-ABI of the GB300 wavefront path tracer.
+ *
+ * Drop-in boundary for the reference renderer's render path (matthewshang/illume):
+ *   HostScene(rapidjson::Document&)            src/scene/scene.h:11-28, src/scene/scene.cpp:11-99
+ *   SceneRef(HostScene&)                       src/scene/sceneref.h:11-35 (host -> device copy)
+ *   Renderer(json, HostScene&, spp, max_depth) src/renderer.h:8-25, src/renderer.cu:39-59
+ *   Renderer::render_to_bitmap(Bitmap*)        src/renderer.cu:498-597
+ *   Renderer::get_width / get_height           src/renderer.cu:599-607
+ *   bitmap_new / bitmap_free / bitmap_save_to_png   src/bitmap.h:26-30
+ *   CLI  illume <save> <scene> <spp> <maxdepth>     src/main.cu:14-43
+ *
+ * Conventions: every function that can fail returns an int status (ILLUME_OK = 0,
+ * negative on error) and never exits or prints on the render path; the message of the
+ * last failure on the calling thread is returned by illume_last_error(). Handles are
+ * opaque. A context owns one CUDA stream on one device; it may be used from one host
+ * thread at a time, and different contexts may be used concurrently. The library owns
+ * device memory; callers own every host buffer they pass.
+ */
+#ifndef ILLUME_H
+#define ILLUME_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ILLUME_ABI_VERSION 1
+
+enum illume_status {
+  ILLUME_OK = 0,
+  ILLUME_ERR_INVALID = -1,     /* bad argument or handle */
+  ILLUME_ERR_CUDA = -2,        /* CUDA runtime error (message has the CUDA string) */
+  ILLUME_ERR_OOM = -3,         /* device or host allocation failed */
+  ILLUME_ERR_IO = -4,          /* file could not be read or written */
+  ILLUME_ERR_PARSE = -5,       /* malformed JSON or OBJ */
+  ILLUME_ERR_BUDGET = -6,      /* request exceeds the context's HBM budget */
+  ILLUME_ERR_TIMEOUT = -7,     /* a bounded device wait ran out */
+  ILLUME_ERR_CANCELLED = -8,   /* job cancelled */
+  ILLUME_ERR_UNSUPPORTED = -9, /* feature not available in this build */
+  ILLUME_ERR_NOT_READY = -10   /* job still running (illume_job_poll) */
+};
+
+/* ---- enumerations shared with the JSON scene format ---- */
+enum illume_material_type { /* src/material.h:12-20 */
+  ILLUME_MAT_EMISSIVE = 0, ILLUME_MAT_LAMBERT = 1, ILLUME_MAT_REFLECTIVE = 2, ILLUME_MAT_REFRACTIVE = 3,
+  ILLUME_MAT_ROUGHREFLECTIVE = 4, ILLUME_MAT_ROUGHREFRACTIVE = 5, ILLUME_MAT_CONDUCTOR = 6,
+  ILLUME_MAT_ROUGHCONDUCTOR = 7, ILLUME_MAT_PLASTIC = 8
+};
+enum illume_texture_type { ILLUME_TEX_CONSTANT = 0, ILLUME_TEX_CHECKERBOARD = 1, ILLUME_TEX_BITMAP = 2 }; /* src/texture.h:8-11 */
+enum illume_distribution { ILLUME_DIST_BECKMANN = 0, ILLUME_DIST_GGX = 1 };
+enum illume_tonemapper { ILLUME_TONE_LINEAR = 0, ILLUME_TONE_REINHARD = 1, ILLUME_TONE_FILMIC = 2, ILLUME_TONE_UNCHARTED = 3 }; /* src/tonemapper.h:10-13 */
+enum illume_intersector { ILLUME_ISECT_MT = 0, ILLUME_ISECT_WATERTIGHT = 1 };
+enum illume_bvh_kind { ILLUME_BVH_BINARY = 0, ILLUME_BVH_WIDE8 = 1 };
+enum illume_accum_mode { ILLUME_ACCUM_FP32 = 0, ILLUME_ACCUM_KAHAN = 1, ILLUME_ACCUM_FP64 = 2 };
+
+/* ---- reference output types: same layout as src/bitmap.h:6-20 ---- */
+typedef struct { size_t red, green, blue; } illume_pixel;
+typedef struct { illume_pixel* pixels; size_t width, height; } illume_bitmap;
+
+typedef struct illume_context illume_context;
+typedef struct illume_scene illume_scene;
+typedef struct illume_renderer illume_renderer;
+
+/* Flat, host-side description of a scene: what HostScene holds after parsing
+ * (src/scene/scene.h:20-27), as plain arrays. Matrices are 3x4 row-major (the rows of
+ * the reference's Matrix4 without the constant last row). Unused pointers may be NULL
+ * when the matching count is zero. Per-mesh arrays index into the pooled arrays. */
+typedef struct {
+  /* meshes (src/primitives/mesh.h:18-33) */
+  int32_t num_meshes;
+  const int32_t* mesh_vertex_offset;  /* first vertex of each mesh in positions */
+  const int32_t* mesh_num_vertices;
+  const int32_t* mesh_tri_offset;     /* first triangle of each mesh in tris */
+  const int32_t* mesh_num_tris;
+  const int32_t* mesh_has_normals;    /* 0 = face normals (the JSON default) */
+  const int32_t* mesh_has_texcoords;
+  const int32_t* mesh_bvh_leaf_size;  /* bvh_items_per_node (JSON default 4) */
+  const float* positions;             /* 3 per vertex */
+  const float* normals;               /* 3 per vertex (read for meshes with normals) */
+  const float* texcoords;             /* 2 per vertex (read for meshes with texcoords) */
+  const int32_t* tris;                /* 3 per triangle, vertex indices local to the mesh */
+  /* instances (src/primitives/mesh_instance.h:13-20) */
+  int32_t num_instances;
+  const int32_t* inst_mesh;
+  const int32_t* inst_material;
+  const float* inst_mat;              /* 12 per instance: object -> world */
+  const float* inst_inv;              /* 12 per instance: world -> object */
+  const float* inst_trans_inv;        /* 12 per instance: normal transform (transpose of inv) */
+  /* spheres (src/primitives/sphere.h:11-17) */
+  int32_t num_spheres;
+  const float* sphere_center_radius;  /* 4 per sphere */
+  const int32_t* sphere_material;
+  /* materials (src/material.h:22-33) */
+  int32_t num_materials;
+  const int32_t* mat_type;            /* illume_material_type */
+  const int32_t* mat_albedo_tex;
+  const int32_t* mat_roughness_tex;
+  const int32_t* mat_medium;          /* -1 = air */
+  const int32_t* mat_distribution;    /* illume_distribution */
+  const float* mat_ior;
+  const float* mat_diffuse_fresnel;   /* plastic: Fresnel::diffuse_fresnel(1/ior, 1e6) */
+  const float* mat_eta;               /* 3 per material */
+  const float* mat_k;                 /* 3 per material */
+  /* mediums (src/medium.h:8-14) */
+  int32_t num_mediums;
+  const float* med_absorption;        /* 3 per medium, already 1 - JSON value */
+  const float* med_scattering;
+  const float* med_g;
+  const int32_t* med_active;
+  /* textures (src/texture.h:13-48) */
+  int32_t num_textures;
+  const int32_t* tex_type;            /* illume_texture_type */
+  const float* tex_color;             /* 3 per texture: constant colour / checker on colour */
+  const float* tex_off;               /* 3 per texture: checker off colour */
+  const float* tex_scale;             /* 2 per texture */
+  const int32_t* tex_width;
+  const int32_t* tex_height;
+  const int32_t* tex_hdr;             /* 1 = float texels, bilinear; 0 = 8-bit texels, point */
+  const int64_t* tex_texel_offset;    /* first float of each bitmap in texels */
+  const float* texels;                /* RGBA, 4 floats per texel (8-bit texels as 0..255) */
+  int32_t env_tex;                    /* environment texture, -1 = black */
+  /* camera (src/camera.h:9-17) */
+  float camera_transform[12];
+  float camera_fov, camera_dof, camera_aperture;
+  /* render_settings (src/renderer.cu:42-58) */
+  int32_t width, height;
+  float ray_bias;
+  int32_t tonemapper;                 /* illume_tonemapper */
+} illume_scene_desc;
+
+/* Parameters of one render (Renderer's settings plus the GB300 extensions). */
+typedef struct {
+  int32_t width, height;      /* image size (scene default from render_settings) */
+  int32_t spp;                /* samples per pixel */
+  int32_t max_depth;          /* closest-hit queries per path */
+  int32_t sample_begin;       /* first sample index (progressive / sharded renders) */
+  float ray_bias;
+  int32_t tonemapper;         /* illume_tonemapper */
+  uint32_t seed, job;         /* Philox key */
+  int32_t accum_mode;         /* illume_accum_mode */
+  int32_t intersector;        /* illume_intersector */
+  int32_t bvh_kind;           /* illume_bvh_kind */
+  int32_t exact_hg;           /* 0 = reference Henyey-Greenstein sampler, 1 = exact */
+  int32_t samples_per_pass;   /* samples of every pixel kept in flight per wavefront pass (0 = auto) */
+  int32_t reserved[6];
+} illume_render_params;
+
+typedef struct {
+  int64_t rays;               /* closest-hit queries, counted as src/renderer.cu:554 counts them */
+  int64_t paths;
+  double render_ms;           /* device time of the bounce loop (CUDA events) */
+  double total_ms;            /* wall time of the call, uploads and downloads included */
+  int64_t kernel_launches;    /* launches of this library's kernels during the call */
+  int64_t h2d_bytes, d2h_bytes;
+} illume_render_stats;
+
+/* Hit record of the closest-hit test hook. */
+typedef struct {
+  float t;                    /* FLT_MAX on a miss */
+  float u, v;                 /* barycentric weights of vertices 1 and 2 (mesh hits) */
+  int32_t inst;               /* instance index, -1 if none */
+  int32_t prim;               /* triangle index within the instance's mesh, -1 if none */
+  int32_t sphere;             /* sphere index, -1 if none */
+  int32_t pad[2];
+} illume_hit;
+
+/* ---- errors and version ---- */
+const char* illume_last_error(void);
+int illume_abi_version(void);
+
+/* ---- context ---- */
+int illume_context_create(int device, size_t hbm_budget_bytes, illume_context** out);
+int illume_context_destroy(illume_context* ctx);
+/* the context's CUDA stream (a cudaStream_t) */
+void* illume_context_stream(illume_context* ctx);
+
+/* ---- scenes: HostScene + SceneRef ---- */
+/* Parse a scene file in the reference JSON format; relative "file" paths resolve
+ * against base_dir (NULL = the current directory, as the reference does). */
+int illume_scene_load_json(illume_context* ctx, const char* path, const char* base_dir, illume_scene** out);
+int illume_scene_load_json_string(illume_context* ctx, const char* json, const char* base_dir, illume_scene** out);
+int illume_scene_create(illume_context* ctx, const illume_scene_desc* desc, illume_scene** out);
+/* Fill *out with pointers into the scene's host copy (valid while the scene lives). */
+int illume_scene_describe(const illume_scene* scene, illume_scene_desc* out);
+/* Device bytes held by the scene (geometry, BVHs, textures). */
+int illume_scene_device_bytes(const illume_scene* scene, size_t* out);
+int illume_scene_destroy(illume_scene* scene);
+
+/* ---- renderer ---- */
+/* Defaults of the reference: the scene's render_settings, seed 0, linear tonemap unless
+ * the scene names another, FP32 accumulation, Beckmann as parsed. */
+int illume_render_params_default(const illume_scene* scene, int spp, int max_depth, illume_render_params* out);
+int illume_renderer_create(illume_context* ctx, illume_scene* scene, const illume_render_params* params,
+                           illume_renderer** out);
+int illume_renderer_destroy(illume_renderer* r);
+int illume_renderer_get_width(const illume_renderer* r);
+int illume_renderer_get_height(const illume_renderer* r);
+/* Renderer::render_to_bitmap: full render and tonemap into a caller-allocated bitmap of
+ * the renderer's size. */
+int illume_render_to_bitmap(illume_renderer* r, illume_bitmap* bitmap, illume_render_stats* stats);
+/* Render into host buffers (each nullable): mean linear radiance (W*H*3 floats), the
+ * per-pixel sum and sum of squares of per-sample radiance (W*H*3 doubles each) and the
+ * tonemapped RGB8 image (W*H*3 bytes). */
+int illume_render(illume_renderer* r, float* out_mean, double* out_sum, double* out_sumsq, uint8_t* out_rgb8,
+                  illume_render_stats* stats);
+/* Device-resident variant: runs the bounce loop only, leaving the accumulators on the
+ * device (inputs already resident). Accumulates on top of earlier calls when
+ * accumulate != 0. */
+int illume_render_device(illume_renderer* r, int accumulate, illume_render_stats* stats);
+/* Copies the device accumulators (sum, sumsq as in illume_render) to host buffers. */
+int illume_renderer_read(illume_renderer* r, float* out_mean, double* out_sum, double* out_sumsq, uint8_t* out_rgb8);
+
+/* ---- bitmap (src/bitmap.h:26-30) ---- */
+illume_bitmap* illume_bitmap_new(size_t width, size_t height);
+void illume_bitmap_free(illume_bitmap* bitmap);
+int illume_bitmap_save_png(const illume_bitmap* bitmap, const char* path);
+int illume_bitmap_save_ppm(const illume_bitmap* bitmap, const char* path);
+int illume_save_pfm(const float* rgb, int width, int height, const char* path);
+
+/* ---- test hooks ---- */
+/* Closest hit of n rays (8 floats each: ox, oy, oz, unused, dx, dy, dz, unused; the
+ * direction is used as given) against a scene, on the device; host buffers. */
+int illume_trace_closest(illume_context* ctx, illume_scene* scene, const float* rays, int n, int intersector,
+                         int bvh_kind, illume_hit* hits);
+/* Same with device pointers, on the context's stream, no synchronisation. */
+int illume_trace_closest_device(illume_context* ctx, illume_scene* scene, const float* d_rays, int n,
+                                int intersector, int bvh_kind, illume_hit* d_hits);
+/* BSDF sample / eval / pdf on the device for n tuples (host buffers). Each input tuple
+ * is 16 floats: wi (3, pointing away from the surface), n (3), u1, u2, u3, roughness,
+ * ior, eta.xyz, k.x, (unused); outputs are 16 floats: new_dir (3), weight (3), D, pdf_m,
+ * G, F, eval (f * cos), pdf_dir, status (0 killed, 1 reflect, 2 transmit), 3 unused.
+ * For conductors k.yz are taken equal to k.x. */
+int illume_bsdf_batch(illume_context* ctx, int material_type, int distribution, const float* inputs, int n,
+                      float* outputs);
+
+/* ---- batched and served rendering ---- */
+typedef struct illume_server illume_server;
+typedef int64_t illume_job_id;
+int illume_server_create(illume_context* ctx, size_t hbm_budget_bytes, int max_jobs_in_flight, illume_server** out);
+int illume_server_destroy(illume_server* s);
+/* Admit a job when its footprint fits the budget (ILLUME_ERR_BUDGET if it never can). */
+int illume_job_submit(illume_server* s, illume_scene* scene, const illume_render_params* params, illume_job_id* out);
+/* Advance the server by one scheduling round (one wavefront pass over all running jobs). */
+int illume_server_step(illume_server* s, int* jobs_running);
+/* ILLUME_OK when done (results copied to the nullable buffers), ILLUME_ERR_NOT_READY otherwise. */
+int illume_job_poll(illume_server* s, illume_job_id id, float* out_mean, uint8_t* out_rgb8, illume_render_stats* stats);
+int illume_job_cancel(illume_server* s, illume_job_id id);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ILLUME_H */

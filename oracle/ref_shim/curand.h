@@ -1,0 +1,3 @@
+// Host stand-in header for building the reference renderer on the CPU (test infrastructure).
+#pragma once
+#include "illume_ref_shim.h"
