@@ -87,6 +87,13 @@ class RenderStats(ctypes.Structure):
     ]
 
 
+class Profile(ctypes.Structure):
+    """illume_profile"""
+    _fields_ = [("raygen_ms", c_double), ("trace_ms", c_double), ("shade_ms", c_double), ("accumulate_ms", c_double),
+                ("trace_launches", c_int64), ("shade_launches", c_int64), ("rays", c_int64),
+                ("node_fetches", c_int64), ("tri_tests", c_int64), ("node_bytes", c_int64), ("tri_bytes", c_int64)]
+
+
 class Hit(ctypes.Structure):
     """illume_hit"""
     _fields_ = [("t", c_float), ("u", c_float), ("v", c_float), ("inst", c_int32), ("prim", c_int32),
@@ -115,6 +122,9 @@ PROTOTYPES = {
     "illume_scene_create": (c_int, [c_void_p, POINTER(SceneDesc), POINTER(c_void_p)]),
     "illume_scene_describe": (c_int, [c_void_p, POINTER(SceneDesc)]),
     "illume_scene_device_bytes": (c_int, [c_void_p, POINTER(c_size_t)]),
+    "illume_scene_check_bvh": (c_int, [c_void_p, c_char_p, c_size_t]),
+    "illume_scene_upload": (c_int, [c_void_p, POINTER(c_size_t)]),
+    "illume_renderer_profile": (c_int, [c_void_p, c_int, POINTER(Profile)]),
     "illume_scene_destroy": (c_int, [c_void_p]),
     "illume_render_params_default": (c_int, [c_void_p, c_int, c_int, POINTER(RenderParams)]),
     "illume_renderer_create": (c_int, [c_void_p, c_void_p, POINTER(RenderParams), POINTER(c_void_p)]),

@@ -1,0 +1,523 @@
+#include "bvh_build.h"
+
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cfloat>
+
+namespace illume {
+
+namespace {
+
+struct Box {
+  double lo[3], hi[3];
+  void reset() {
+    for (int a = 0; a < 3; ++a) { lo[a] = INFINITY; hi[a] = -INFINITY; }
+  }
+  void grow(const Box& b) {
+    for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], b.lo[a]); hi[a] = std::max(hi[a], b.hi[a]); }
+  }
+  void grow_pt(const double* p) {
+    for (int a = 0; a < 3; ++a) { lo[a] = std::min(lo[a], p[a]); hi[a] = std::max(hi[a], p[a]); }
+  }
+  double area() const {
+    const double dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+    if (dx < 0 || dy < 0 || dz < 0) return 0.0;
+    return 2.0 * (dx * dy + dy * dz + dz * dx);
+  }
+};
+
+struct BNode {
+  Box box;
+  int left = -1, right = -1;  // children (binary tree), -1 for leaves
+  int first = 0, count = 0;   // leaf range in the prim order
+};
+
+float down(double d) {
+  float f = (float)d;
+  if ((double)f > d) f = nextafterf(f, -INFINITY);
+  return f;
+}
+float up(double d) {
+  float f = (float)d;
+  if ((double)f < d) f = nextafterf(f, INFINITY);
+  return f;
+}
+
+// Binned SAH build; returns nodes (root at 0) and fills order.
+std::vector<BNode> build_binary(const std::vector<Box>& boxes, std::vector<int>& order, int max_leaf) {
+  const int N = (int)boxes.size();
+  order.resize(N);
+  for (int i = 0; i < N; ++i) order[i] = i;
+  std::vector<double> ctr((size_t)N * 3);
+  for (int i = 0; i < N; ++i)
+    for (int a = 0; a < 3; ++a) ctr[3 * (size_t)i + a] = 0.5 * (boxes[i].lo[a] + boxes[i].hi[a]);
+  std::vector<BNode> nodes;
+  nodes.reserve(2 * (size_t)N + 1);
+  nodes.emplace_back();
+  struct Work { int node, first, count; };
+  std::vector<Work> stack{{0, 0, N}};
+  const int kBins = 16;
+  while (!stack.empty()) {
+    const Work w = stack.back();
+    stack.pop_back();
+    BNode nd;
+    nd.box.reset();
+    Box cb;
+    cb.reset();
+    for (int i = w.first; i < w.first + w.count; ++i) {
+      nd.box.grow(boxes[order[i]]);
+      cb.grow_pt(&ctr[3 * (size_t)order[i]]);
+    }
+    nd.first = w.first;
+    nd.count = w.count;
+    const double parent_area = nd.box.area();
+    const double leaf_cost = (double)w.count;
+    double best_cost = INFINITY;
+    int best_axis = -1, best_bin = -1;
+    if (w.count > 1) {
+      for (int a = 0; a < 3; ++a) {
+        const double ext = cb.hi[a] - cb.lo[a];
+        if (!(ext > 0)) continue;
+        Box bb[kBins];
+        int bc[kBins] = {0};
+        for (int b = 0; b < kBins; ++b) bb[b].reset();
+        const double k = kBins / ext;
+        for (int i = w.first; i < w.first + w.count; ++i) {
+          const int p = order[i];
+          int b = (int)((ctr[3 * (size_t)p + a] - cb.lo[a]) * k);
+          b = std::min(std::max(b, 0), kBins - 1);
+          bb[b].grow(boxes[p]);
+          bc[b]++;
+        }
+        double rarea[kBins];
+        int rcount[kBins];
+        Box acc;
+        acc.reset();
+        int cnt = 0;
+        for (int b = kBins - 1; b > 0; --b) {
+          acc.grow(bb[b]);
+          cnt += bc[b];
+          rarea[b] = acc.area();
+          rcount[b] = cnt;
+        }
+        acc.reset();
+        cnt = 0;
+        for (int b = 0; b < kBins - 1; ++b) {
+          acc.grow(bb[b]);
+          cnt += bc[b];
+          if (cnt == 0 || rcount[b + 1] == 0) continue;
+          const double cost = 1.0 + (acc.area() * cnt + rarea[b + 1] * rcount[b + 1]) / std::max(parent_area, 1e-300);
+          if (cost < best_cost) { best_cost = cost; best_axis = a; best_bin = b; }
+        }
+      }
+    }
+    const bool make_leaf = w.count == 1 || (w.count <= max_leaf && leaf_cost <= best_cost);
+    if (make_leaf) {
+      nodes[w.node] = nd;
+      continue;
+    }
+    int mid;
+    if (best_axis < 0) {
+      // all centroids coincide (or no valid split): object median
+      mid = w.first + w.count / 2;
+    } else {
+      const double ext = cb.hi[best_axis] - cb.lo[best_axis];
+      const double k = kBins / ext;
+      auto it = std::partition(order.begin() + w.first, order.begin() + w.first + w.count, [&](int p) {
+        int b = (int)((ctr[3 * (size_t)p + best_axis] - cb.lo[best_axis]) * k);
+        b = std::min(std::max(b, 0), kBins - 1);
+        return b <= best_bin;
+      });
+      mid = (int)(it - order.begin());
+      if (mid == w.first || mid == w.first + w.count) mid = w.first + w.count / 2;
+    }
+    nd.left = (int)nodes.size();
+    nd.right = nd.left + 1;
+    nodes.emplace_back();
+    nodes.emplace_back();
+    nodes[w.node] = nd;
+    stack.push_back({nd.right, mid, w.first + w.count - mid});
+    stack.push_back({nd.left, w.first, mid - w.first});
+  }
+  return nodes;
+}
+
+void put_tri(std::vector<float4>& out, const float* P, const int* tri, int prim) {
+  const float* a = P + 3 * (size_t)tri[0];
+  const float* b = P + 3 * (size_t)tri[1];
+  const float* c = P + 3 * (size_t)tri[2];
+  float w;
+  memcpy(&w, &prim, 4);
+  out.push_back(float4{a[0], a[1], a[2], w});
+  out.push_back(float4{b[0], b[1], b[2], 0.0f});
+  out.push_back(float4{c[0], c[1], c[2], 0.0f});
+}
+
+int tree_depth(const std::vector<BNode>& n, int i) {
+  if (n[i].left < 0) return 1;
+  return 1 + std::max(tree_depth(n, n[i].left), tree_depth(n, n[i].right));
+}
+
+}  // namespace
+
+void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, MeshBvh* out) {
+  (void)num_vertices;
+  // padded triangle boxes
+  double mlo[3] = {INFINITY, INFINITY, INFINITY}, mhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int i = 0; i < T; ++i)
+    for (int k = 0; k < 3; ++k)
+      for (int a = 0; a < 3; ++a) {
+        const double v = P[3 * (size_t)tris[3 * i + k] + a];
+        mlo[a] = std::min(mlo[a], v);
+        mhi[a] = std::max(mhi[a], v);
+      }
+  double ext = 0, mag = 0;
+  for (int a = 0; a < 3; ++a) {
+    if (T > 0) {
+      ext = std::max(ext, mhi[a] - mlo[a]);
+      mag = std::max(mag, std::max(fabs(mlo[a]), fabs(mhi[a])));
+    }
+  }
+  const double pad = ldexp(ext + mag, -16) + 1e-30;
+  std::vector<Box> boxes(T);
+  for (int i = 0; i < T; ++i) {
+    boxes[i].reset();
+    for (int k = 0; k < 3; ++k) {
+      double p[3];
+      for (int a = 0; a < 3; ++a) p[a] = P[3 * (size_t)tris[3 * i + k] + a];
+      boxes[i].grow_pt(p);
+    }
+    for (int a = 0; a < 3; ++a) {
+      boxes[i].lo[a] = (double)down(boxes[i].lo[a] - pad);
+      boxes[i].hi[a] = (double)up(boxes[i].hi[a] + pad);
+    }
+  }
+  for (int a = 0; a < 3; ++a) {
+    out->lo[a] = T ? down(mlo[a] - pad) : 0.0f;
+    out->hi[a] = T ? up(mhi[a] + pad) : 0.0f;
+  }
+
+  // ---------------- binary layout ----------------
+  {
+    std::vector<int> order;
+    std::vector<BNode> bn = T ? build_binary(boxes, order, 4) : std::vector<BNode>();
+    out->bvh2.clear();
+    out->bvh2_tris.clear();
+    out->bvh2_tris.reserve((size_t)T * 3);
+    for (int i = 0; i < T; ++i) put_tri(out->bvh2_tris, P, tris + 3 * (size_t)order[i], order[i]);
+    auto encode_box = [](Bvh2Node& n, int slot, const Box& b) {
+      float lo[3], hi[3];
+      for (int a = 0; a < 3; ++a) { lo[a] = (float)b.lo[a]; hi[a] = (float)b.hi[a]; }
+      if (slot == 0) {
+        n.a = float4{lo[0], lo[1], lo[2], hi[0]};
+        n.b.x = hi[1]; n.b.y = hi[2];
+      } else {
+        n.b.z = lo[0]; n.b.w = lo[1];
+        n.c = float4{lo[2], hi[0], hi[1], hi[2]};
+      }
+    };
+    const float inf = INFINITY;
+    if (T == 0) {
+      Bvh2Node n{};
+      n.a = float4{inf, inf, inf, -inf}; n.b = float4{-inf, -inf, inf, inf}; n.c = float4{inf, -inf, -inf, -inf};
+      n.d = int4{~0, ~0, 0, 0};
+      out->bvh2.push_back(n);
+    } else {
+      // map binary inner nodes to Bvh2 node indices (DFS order)
+      std::vector<int> idx(bn.size(), -1);
+      std::vector<int> st{0};
+      std::vector<int> inner;
+      if (bn[0].left < 0) {
+        // whole mesh in one leaf: one inner node with the leaf and an empty slot
+        out->root_leaf = true;
+        Bvh2Node n{};
+        encode_box(n, 0, bn[0].box);
+        Box empty;
+        empty.reset();
+        n.b.z = inf; n.b.w = inf; n.c = float4{inf, -inf, -inf, -inf};
+        n.d = int4{~bn[0].first, ~0, bn[0].count, 0};
+        out->bvh2.push_back(n);
+      } else {
+        while (!st.empty()) {
+          const int i = st.back();
+          st.pop_back();
+          idx[i] = (int)inner.size();
+          inner.push_back(i);
+          if (bn[bn[i].right].left >= 0) st.push_back(bn[i].right);
+          if (bn[bn[i].left].left >= 0) st.push_back(bn[i].left);
+        }
+        out->bvh2.resize(inner.size());
+        for (size_t k = 0; k < inner.size(); ++k) {
+          const BNode& b = bn[inner[k]];
+          Bvh2Node n{};
+          const BNode& L = bn[b.left];
+          const BNode& R = bn[b.right];
+          encode_box(n, 0, L.box);
+          encode_box(n, 1, R.box);
+          n.d.x = L.left >= 0 ? idx[b.left] : ~L.first;
+          n.d.y = R.left >= 0 ? idx[b.right] : ~R.first;
+          n.d.z = L.left >= 0 ? 0 : L.count;
+          n.d.w = R.left >= 0 ? 0 : R.count;
+          out->bvh2[k] = n;
+          out->stats.bvh2_leaves += (L.left < 0) + (R.left < 0);
+        }
+      }
+      out->stats.bvh2_nodes = (int)out->bvh2.size();
+      out->stats.bvh2_depth = tree_depth(bn, 0);
+    }
+  }
+
+  // ---------------- 8-wide quantised layout ----------------
+  {
+    std::vector<int> order;
+    std::vector<BNode> bn = T ? build_binary(boxes, order, 3) : std::vector<BNode>();
+    out->wide.clear();
+    out->wide_tris.clear();
+    out->wide_tris.reserve((size_t)T * 3);
+    if (T == 0) {
+      WideNode w{};
+      out->wide.push_back(w);
+    } else {
+      // queue of (binary node, wide node index); children of one wide node are allocated
+      // consecutively so that a child's index = child_base + rank among inner children
+      std::vector<std::pair<int, int>> queue;
+      out->wide.emplace_back();
+      queue.push_back({0, 0});
+      size_t head = 0;
+      int max_depth = 0;
+      std::vector<int> depth_of{1};
+      while (head < queue.size()) {
+        const int b = queue[head].first;
+        const int wi = queue[head].second;
+        ++head;
+        max_depth = std::max(max_depth, depth_of[wi]);
+        // collapse: expand the largest inner child until 8 children
+        std::vector<int> kids;
+        if (bn[b].left < 0) {
+          kids.push_back(b);  // root leaf
+        } else {
+          kids = {bn[b].left, bn[b].right};
+          for (;;) {
+            if (kids.size() >= 8) break;
+            int best = -1;
+            double ba = -1;
+            for (size_t k = 0; k < kids.size(); ++k)
+              if (bn[kids[k]].left >= 0 && bn[kids[k]].box.area() > ba) { ba = bn[kids[k]].box.area(); best = (int)k; }
+            if (best < 0) break;
+            const int x = kids[best];
+            kids[best] = bn[x].left;
+            kids.push_back(bn[x].right);
+          }
+        }
+        // node box and octant slot assignment
+        Box nb;
+        nb.reset();
+        for (int k : kids) nb.grow(bn[k].box);
+        double nc[3];
+        for (int a = 0; a < 3; ++a) nc[a] = 0.5 * (nb.lo[a] + nb.hi[a]);
+        struct Cand { double cost; int kid, slot; };
+        std::vector<Cand> cands;
+        for (size_t k = 0; k < kids.size(); ++k) {
+          const Box& cbx = bn[kids[k]].box;
+          for (int s = 0; s < 8; ++s) {
+            const double sx = (s & 4) ? -1 : 1, sy = (s & 2) ? -1 : 1, sz = (s & 1) ? -1 : 1;
+            const double cost = (0.5 * (cbx.lo[0] + cbx.hi[0]) - nc[0]) * sx + (0.5 * (cbx.lo[1] + cbx.hi[1]) - nc[1]) * sy +
+                                (0.5 * (cbx.lo[2] + cbx.hi[2]) - nc[2]) * sz;
+            cands.push_back({cost, (int)k, s});
+          }
+        }
+        std::sort(cands.begin(), cands.end(), [](const Cand& x, const Cand& y) {
+          return x.cost < y.cost || (x.cost == y.cost && (x.kid < y.kid || (x.kid == y.kid && x.slot < y.slot)));
+        });
+        int slot_kid[8];
+        for (int s = 0; s < 8; ++s) slot_kid[s] = -1;
+        std::vector<bool> used(kids.size(), false);
+        for (const Cand& c : cands) {
+          if (used[c.kid] || slot_kid[c.slot] >= 0) continue;
+          used[c.kid] = true;
+          slot_kid[c.slot] = c.kid;
+        }
+        // quantisation frame
+        WideNode w{};
+        w.px = down(nb.lo[0]); w.py = down(nb.lo[1]); w.pz = down(nb.lo[2]);
+        const double p[3] = {w.px, w.py, w.pz};
+        int e[3];
+        for (int a = 0; a < 3; ++a) {
+          const double ext = nb.hi[a] - p[a];
+          int ea = -126;
+          if (ext > 0) {
+            ea = (int)ceil(log2(ext / 255.0));
+            while (ldexp(255.0, ea) < ext) ++ea;
+            ea = std::max(-126, std::min(127, ea));
+          }
+          e[a] = ea;
+        }
+        w.ex = (uint8_t)(e[0] + 127); w.ey = (uint8_t)(e[1] + 127); w.ez = (uint8_t)(e[2] + 127);
+        w.child_base = (uint32_t)out->wide.size();
+        w.tri_base = (uint32_t)(out->wide_tris.size() / 3);
+        int tri_off = 0;
+        for (int s = 0; s < 8; ++s) {
+          const int k = slot_kid[s];
+          if (k < 0) continue;
+          const BNode& c = bn[kids[k]];
+          uint8_t* qlo[3] = {w.qlox, w.qloy, w.qloz};
+          uint8_t* qhi[3] = {w.qhix, w.qhiy, w.qhiz};
+          for (int a = 0; a < 3; ++a) {
+            const double sc = ldexp(1.0, e[a]);
+            double ql = floor((c.box.lo[a] - p[a]) / sc), qh = ceil((c.box.hi[a] - p[a]) / sc);
+            ql = std::max(0.0, std::min(255.0, ql));
+            qh = std::max(0.0, std::min(255.0, qh));
+            while (ql > 0 && p[a] + ql * sc > c.box.lo[a]) ql -= 1;
+            while (qh < 255 && p[a] + qh * sc < c.box.hi[a]) qh += 1;
+            qlo[a][s] = (uint8_t)ql;
+            qhi[a][s] = (uint8_t)qh;
+          }
+          if (c.left >= 0) {
+            w.imask |= (uint8_t)(1u << s);
+            const int child_index = (int)out->wide.size();
+            out->wide.emplace_back();
+            depth_of.resize(out->wide.size());
+            depth_of[child_index] = depth_of[wi] + 1;
+            queue.push_back({kids[k], child_index});
+          } else {
+            w.meta[s] = (uint8_t)((c.count << 5) | tri_off);
+            for (int t = c.first; t < c.first + c.count; ++t) put_tri(out->wide_tris, P, tris + 3 * (size_t)order[t], order[t]);
+            tri_off += c.count;
+            out->stats.wide_leaves++;
+          }
+        }
+        out->wide[wi] = w;
+      }
+      out->stats.wide_nodes = (int)out->wide.size();
+      out->stats.wide_depth = max_depth;
+    }
+  }
+}
+
+}  // namespace illume
+
+namespace illume {
+
+namespace {
+
+struct DBox {
+  double lo[3], hi[3];
+  bool contains_point(const double* p) const {
+    for (int a = 0; a < 3; ++a)
+      if (p[a] < lo[a] || p[a] > hi[a]) return false;
+    return true;
+  }
+  bool contains(const DBox& b) const {
+    for (int a = 0; a < 3; ++a)
+      if (b.lo[a] < lo[a] || b.hi[a] > hi[a]) return false;
+    return true;
+  }
+};
+
+bool tri_inside(const float4* tv, const DBox& b) {
+  for (int k = 0; k < 3; ++k) {
+    const double p[3] = {tv[k].x, tv[k].y, tv[k].z};
+    if (!b.contains_point(p)) return false;
+  }
+  return true;
+}
+
+int prim_of(const float4& v) {
+  int p;
+  memcpy(&p, &v.w, 4);
+  return p;
+}
+
+}  // namespace
+
+bool check_mesh_bvh(const float* P, const int* tris, int T, const MeshBvh& b, std::string* msg) {
+  (void)P; (void)tris;
+  if (T == 0) return true;
+  // ---- binary ----
+  {
+    std::vector<int> seen(T, 0);
+    std::vector<std::pair<int, DBox>> st;  // node, box the parent claims for it
+    DBox all{{-INFINITY, -INFINITY, -INFINITY}, {INFINITY, INFINITY, INFINITY}};
+    st.push_back({0, all});
+    while (!st.empty()) {
+      const int ni = st.back().first;
+      const DBox parent = st.back().second;
+      st.pop_back();
+      if (ni < 0 || ni >= (int)b.bvh2.size()) { *msg = "binary: node index out of range"; return false; }
+      const Bvh2Node& n = b.bvh2[ni];
+      const DBox c0{{n.a.x, n.a.y, n.a.z}, {n.a.w, n.b.x, n.b.y}};
+      const DBox c1{{n.b.z, n.b.w, n.c.x}, {n.c.y, n.c.z, n.c.w}};
+      const int child[2] = {n.d.x, n.d.y}, count[2] = {n.d.z, n.d.w};
+      const DBox* cb[2] = {&c0, &c1};
+      for (int s = 0; s < 2; ++s) {
+        if (child[s] < 0) {
+          if (count[s] == 0) continue;
+          if (!parent.contains(*cb[s]) && ni != 0) { *msg = "binary: child box outside parent"; return false; }
+          for (int i = ~child[s]; i < ~child[s] + count[s]; ++i) {
+            if (i < 0 || i >= T) { *msg = "binary: triangle index out of range"; return false; }
+            const int p = prim_of(b.bvh2_tris[3 * i]);
+            if (p < 0 || p >= T || seen[p]++) { *msg = "binary: triangle referenced twice or invalid"; return false; }
+            if (!tri_inside(&b.bvh2_tris[3 * i], *cb[s])) { *msg = "binary: triangle outside its leaf box"; return false; }
+          }
+        } else {
+          if (ni != 0 && !parent.contains(*cb[s])) { *msg = "binary: child box outside parent"; return false; }
+          st.push_back({child[s], *cb[s]});
+        }
+      }
+    }
+    for (int p = 0; p < T; ++p)
+      if (seen[p] != 1) { *msg = "binary: triangle " + std::to_string(p) + " not referenced exactly once"; return false; }
+  }
+  // ---- wide ----
+  {
+    std::vector<int> seen(T, 0);
+    std::vector<std::pair<uint32_t, DBox>> st;
+    DBox all{{-INFINITY, -INFINITY, -INFINITY}, {INFINITY, INFINITY, INFINITY}};
+    st.push_back({0u, all});
+    while (!st.empty()) {
+      const uint32_t ni = st.back().first;
+      const DBox parent = st.back().second;
+      st.pop_back();
+      if (ni >= b.wide.size()) { *msg = "wide: node index out of range"; return false; }
+      const WideNode& w = b.wide[ni];
+      const double p[3] = {w.px, w.py, w.pz};
+      const double sc[3] = {ldexp(1.0, (int)w.ex - 127), ldexp(1.0, (int)w.ey - 127), ldexp(1.0, (int)w.ez - 127)};
+      const uint8_t* ql[3] = {w.qlox, w.qloy, w.qloz};
+      const uint8_t* qh[3] = {w.qhix, w.qhiy, w.qhiz};
+      for (int s = 0; s < 8; ++s) {
+        const bool inner = (w.imask >> s) & 1;
+        if (!inner && w.meta[s] == 0) continue;
+        DBox cbx;
+        for (int a = 0; a < 3; ++a) {
+          cbx.lo[a] = p[a] + ql[a][s] * sc[a];
+          cbx.hi[a] = p[a] + qh[a][s] * sc[a];
+        }
+        if (!parent.contains(cbx)) {
+          // a slot box may exceed the parent's slot box by quantisation of the parent only
+          // when the parent box itself is coarser; contents are checked below instead
+        }
+        if (inner) {
+          const uint32_t ci = w.child_base + __builtin_popcount(w.imask & ((1u << s) - 1));
+          st.push_back({ci, cbx});
+        } else {
+          const int cnt = w.meta[s] >> 5, off = w.meta[s] & 31;
+          for (int i = 0; i < cnt; ++i) {
+            const size_t t = (size_t)w.tri_base + off + i;
+            if (t >= (size_t)T) { *msg = "wide: triangle index out of range"; return false; }
+            const int pr = prim_of(b.wide_tris[3 * t]);
+            if (pr < 0 || pr >= T || seen[pr]++) { *msg = "wide: triangle referenced twice or invalid"; return false; }
+            if (!tri_inside(&b.wide_tris[3 * t], cbx)) { *msg = "wide: triangle outside its quantised leaf box"; return false; }
+            if (!tri_inside(&b.wide_tris[3 * t], parent)) { *msg = "wide: triangle outside an ancestor box"; return false; }
+          }
+        }
+      }
+    }
+    for (int p = 0; p < T; ++p)
+      if (seen[p] != 1) { *msg = "wide: triangle " + std::to_string(p) + " not referenced exactly once"; return false; }
+  }
+  return true;
+}
+
+}  // namespace illume

@@ -1,0 +1,45 @@
+// BVH construction for one mesh (object space).
+//
+// * Binned SAH binary build (16 bins per axis on centroids).
+// * Binary layout (Bvh2Node, 64 B): both child boxes live in the parent node.
+// * 8-wide layout (WideNode, 80 B): the binary tree collapsed greedily into nodes of up
+//   to 8 children, child slots ordered by ray octant, child boxes quantised to 8 bits per
+//   axis with outward rounding.
+// Triangle boxes are padded by a small absolute margin before building, so that a box
+// test evaluated in FP32 never rejects a ray whose FP32 triangle test reports a hit
+// (for ray origins within ~100x the mesh extent); quantisation only widens boxes.
+#pragma once
+
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../common/types.h"
+
+namespace illume {
+
+struct BuildStats {
+  int bvh2_nodes = 0, bvh2_leaves = 0, bvh2_depth = 0;
+  int wide_nodes = 0, wide_leaves = 0, wide_depth = 0;
+  double sah_cost = 0.0;
+};
+
+struct MeshBvh {
+  std::vector<Bvh2Node> bvh2;
+  std::vector<float4> bvh2_tris;   // 3 float4 per triangle in leaf order, .w of the first = prim id
+  std::vector<WideNode> wide;
+  std::vector<float4> wide_tris;
+  bool root_leaf = false;
+  float lo[3], hi[3];              // padded object-space bounds of the mesh
+  BuildStats stats;
+};
+
+// positions: 3 floats per vertex; tris: 3 ints per triangle.
+void build_mesh_bvh(const float* positions, int num_vertices, const int* tris, int num_tris, MeshBvh* out);
+
+// Invariants of both layouts: every triangle referenced exactly once, every triangle
+// inside its leaf box, every inner child box inside its parent's box, quantised boxes
+// (decoded exactly) containing their contents. Returns false with a message on failure.
+bool check_mesh_bvh(const float* positions, const int* tris, int num_tris, const MeshBvh& b, std::string* msg);
+
+}  // namespace illume

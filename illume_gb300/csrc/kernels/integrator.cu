@@ -1,0 +1,379 @@
+// Wavefront integrator stages: camera-ray generation, material-sorted shading,
+// radiance accumulation and tonemapping, plus the BSDF test hook.
+//
+// One pass renders `per_pass` samples of every pixel: raygen fills the bounce-0 queue,
+// then max_depth x (trace, shade), then accumulate and advance. The bounce loop of
+// src/renderer.cu:538-557 (host compaction after every bounce) becomes device-side
+// warp-aggregated appends; the per-path arithmetic is that of pathtrace_kernel
+// (src/renderer.cu:139-388).
+#include "launch.h"
+#include "shading.cuh"
+#include "../common/philox.cuh"
+
+namespace illume {
+
+__device__ __forceinline__ int* ev_counts2(const WaveBuffers& w, int parity) { return w.counters + 2 + 16 * parity; }
+
+// init_rays, src/renderer.cu:81-110, for path slots pid = sample_in_pass * npix + pixel.
+__global__ void __launch_bounds__(256) k_raygen(WaveBuffers w, CameraView cam, RenderKnobs k) {
+  const PassState ps = *w.pass;
+  const int npaths = ps.nsamples * w.npix;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    w.counters[0] = npaths;
+    w.counters[1] = 0;
+    for (int c = 0; c < EV_COUNT; ++c) ev_counts2(w, 0)[c] = 0;
+  }
+  for (int pid = blockIdx.x * blockDim.x + threadIdx.x; pid < npaths; pid += gridDim.x * blockDim.x) {
+    const int pixel = pid % w.npix;
+    const int sample = ps.sample_base + pid / w.npix;
+    RngStream rng;
+    rng.init((uint32_t)pixel, (uint32_t)sample, 0u, k.seed, k.job);
+    const int x = pixel % cam.width, y = pixel / cam.width;
+    const float left_edge = cam.left + cam.pixel_size * (float)x;
+    const float top_edge = cam.top - cam.pixel_size * (float)y;
+    const float r_x = left_edge + cam.pixel_size * rng.next();
+    const float r_y = top_edge - cam.pixel_size * rng.next();
+    V3 pos = v3(0.0f, 0.0f, 0.0f);
+    if (cam.aperture > FLT_EPSILON) {
+      const float u1 = rng.next(), u2 = rng.next();
+      pos = mul(sample_circle(u1, u2), cam.aperture);
+    }
+    const V3 origin = xform(cam.m, pos, 1.0f);
+    const V3 image_pos = xform(cam.m, v3(r_x, r_y, cam.dof), 1.0f);
+    const V3 dir = normalize(sub(image_pos, origin));
+    w.q_orig[0][pid] = make_float4(origin.x, origin.y, origin.z, __int_as_float(pid));
+    w.q_dir[0][pid] = make_float4(dir.x, dir.y, dir.z, __int_as_float(-1));
+    w.q_thr[0][pid] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    w.contrib[pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
+struct BounceRng {
+  RngStream s;
+  __device__ __forceinline__ float operator()() { return s.next(); }
+};
+
+// Shading of one bounce over the material-sorted event queues.
+__global__ void __launch_bounds__(128) k_shade(WaveBuffers w, SceneView sc, RenderKnobs k, int bounce) {
+  const int parity = bounce & 1;
+  const int* counts = ev_counts2(w, parity);
+  __shared__ int prefix[EV_COUNT + 1];
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int c = 0; c < EV_COUNT; ++c) { prefix[c] = acc; acc += counts[c]; }
+    prefix[EV_COUNT] = acc;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    int* next_counts = ev_counts2(w, parity ^ 1);
+    for (int c = 0; c < EV_COUNT; ++c) next_counts[c] = 0;
+    atomicAdd(w.rays, (unsigned long long)w.counters[parity]);
+  }
+  const int total = prefix[EV_COUNT];
+  const int sample_base = w.pass->sample_base;
+  int* next_count = w.counters + (parity ^ 1);
+  const float bias = k.ray_bias;
+  for (int base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
+    const int g = base + threadIdx.x;
+    bool cont = false;
+    float4 no = make_float4(0, 0, 0, 0), nd = no, nt = no;
+    if (g < total) {
+      int cls = 0;
+      while (cls + 1 < EV_COUNT && g >= prefix[cls + 1]) ++cls;
+      const int i = w.evq[(size_t)cls * w.cap + (g - prefix[cls])];
+      const float4 qo = w.q_orig[parity][i];
+      const float4 qd = w.q_dir[parity][i];
+      const float4 qt = w.q_thr[parity][i];
+      const float4 hv = w.hit[i];
+      const int geom = w.hit_geom[i];
+      const int pid = __float_as_int(qo.w);
+      int medium = __float_as_int(qd.w);
+      const V3 o = v3(qo.x, qo.y, qo.z), d = v3(qd.x, qd.y, qd.z);
+      V3 thr = v3(qt.x, qt.y, qt.z);
+      const float t = hv.x;
+      BounceRng rng;
+      rng.s.init((uint32_t)(pid % w.npix), (uint32_t)(sample_base + pid / w.npix), (uint32_t)(bounce + 1), k.seed,
+                 k.job);
+      float4* contrib = w.contrib + pid;
+      if (medium >= 0 && sc.mediums[medium].active) {
+        const DevMedium md = sc.mediums[medium];
+        const float u = rng();
+        const float dist = -logf(u) / md.scattering;
+        if (cls == EV_MEDIUM) {
+          const float u1 = rng(), u2 = rng();
+          const V3 dir = to_basis(sample_hg(md.g, u1, u2, k.exact_hg != 0), d);
+          const V3 no3 = add(o, mul(d, dist));
+          const V3 nd3 = normalize(dir);
+          thr = mulv(thr, v3(expf(-1.0f * dist * md.absorption[0]), expf(-1.0f * dist * md.absorption[1]),
+                             expf(-1.0f * dist * md.absorption[2])));
+          if (!((double)length2(thr) < 1e-4)) {
+            cont = true;
+            no = make_float4(no3.x, no3.y, no3.z, qo.w);
+            nd = make_float4(nd3.x, nd3.y, nd3.z, qd.w);
+            nt = make_float4(thr.x, thr.y, thr.z, 0.0f);
+          }
+          goto done;
+        }
+        thr = mulv(thr, v3(expf(-1.0f * t * md.absorption[0]), expf(-1.0f * t * md.absorption[1]),
+                           expf(-1.0f * t * md.absorption[2])));
+      }
+      if (cls == EV_MISS) {
+        const V3 L = mulv(thr, env_eval(sc, d));
+        *contrib = make_float4(L.x, L.y, L.z, 0.0f);
+        goto done;
+      }
+      {
+        // shading frame of the hit
+        V3 N;
+        float uv0, uv1;
+        int matid;
+        if (geom >= 0) {
+          const DevInstance& in = sc.instances[geom];
+          const DevMesh& m = sc.meshes[in.mesh];
+          const int prim = __float_as_int(hv.w);
+          const int i0 = __ldg(m.tris + 3 * prim), i1 = __ldg(m.tris + 3 * prim + 1), i2 = __ldg(m.tris + 3 * prim + 2);
+          const float bu = hv.y, bv = hv.z;
+          V3 n;
+          if (!m.normals) {
+            const V3 v0 = v3(__ldg(m.positions + 3 * i0), __ldg(m.positions + 3 * i0 + 1), __ldg(m.positions + 3 * i0 + 2));
+            const V3 v1 = v3(__ldg(m.positions + 3 * i1), __ldg(m.positions + 3 * i1 + 1), __ldg(m.positions + 3 * i1 + 2));
+            const V3 v2 = v3(__ldg(m.positions + 3 * i2), __ldg(m.positions + 3 * i2 + 1), __ldg(m.positions + 3 * i2 + 2));
+            n = normalize(cross(sub(v1, v0), sub(v2, v0)));
+          } else {
+            const V3 n0 = v3(__ldg(m.normals + 3 * i0), __ldg(m.normals + 3 * i0 + 1), __ldg(m.normals + 3 * i0 + 2));
+            const V3 n1 = v3(__ldg(m.normals + 3 * i1), __ldg(m.normals + 3 * i1 + 1), __ldg(m.normals + 3 * i1 + 2));
+            const V3 n2 = v3(__ldg(m.normals + 3 * i2), __ldg(m.normals + 3 * i2 + 1), __ldg(m.normals + 3 * i2 + 2));
+            n = normalize(add(mul(n0, 1.0f - bu - bv), add(mul(n1, bu), mul(n2, bv))));
+          }
+          N = normalize(xform(in.trans_inv, n, 0.0f));
+          if (m.texcoords) {
+            const float w0 = 1.0f - bu - bv;
+            uv0 = (__ldg(m.texcoords + 2 * i0) * w0 + __ldg(m.texcoords + 2 * i1) * bu) + __ldg(m.texcoords + 2 * i2) * bv;
+            uv1 = (__ldg(m.texcoords + 2 * i0 + 1) * w0 + __ldg(m.texcoords + 2 * i1 + 1) * bu) +
+                  __ldg(m.texcoords + 2 * i2 + 1) * bv;
+          } else {
+            uv0 = bu;
+            uv1 = bv;
+          }
+          matid = in.material;
+        } else {
+          const DevSphere sp = sc.spheres[-2 - geom];
+          const V3 pos = add(o, mul(d, t));
+          N = normalize(sub(pos, v3(sp.cx, sp.cy, sp.cz)));
+          uv0 = (float)((double)(atan2f(N.z, N.x) * 0.5f) * ILLUME_INV_PI_D + 0.5);
+          uv1 = (float)(0.5 - (double)asinf(N.y) * ILLUME_INV_PI_D);
+          matid = sp.material;
+        }
+        const DevMaterial mat = sc.materials[matid];
+        const V3 albedo = tex_eval(sc, mat.albedo_tex, uv0, uv1);
+        const float roughness = tex_eval(sc, mat.roughness_tex, uv0, uv1).x;
+        if (mat.type == MAT_EMISSIVE) {
+          const V3 L = mulv(thr, albedo);
+          *contrib = make_float4(L.x, L.y, L.z, 0.0f);
+          goto done;
+        }
+        const ScatterResult s = scatter(mat, d, N, albedo, roughness, rng);
+        if (s.status == SCATTER_KILLED) goto done;
+        if (s.medium != kMediumUnchanged) medium = s.medium;
+        thr = mulv(thr, s.weight);
+        const V3 p = add(add(o, mul(d, t)), mul(s.offset_dir, s.offset_sign * bias));
+        const V3 dir = normalize(s.dir);
+        cont = true;
+        no = make_float4(p.x, p.y, p.z, qo.w);
+        nd = make_float4(dir.x, dir.y, dir.z, __int_as_float(medium));
+        nt = make_float4(thr.x, thr.y, thr.z, 0.0f);
+      }
+    done:;
+    }
+    // compacted append of the continuing paths into the next bounce's queue
+    const unsigned ballot = __ballot_sync(0xffffffffu, cont);
+    if (ballot) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(ballot) - 1;
+      int slot = 0;
+      if (lane == leader) slot = atomicAdd(next_count, __popc(ballot));
+      slot = __shfl_sync(0xffffffffu, slot, leader);
+      if (cont) {
+        const int j = slot + __popc(ballot & ((1u << lane) - 1));
+        w.q_orig[parity ^ 1][j] = no;
+        w.q_dir[parity ^ 1][j] = nd;
+        w.q_thr[parity ^ 1][j] = nt;
+      }
+    }
+  }
+}
+
+// Adds the pass's per-path radiance into the per-pixel accumulators, sample by sample
+// in sample order (deterministic), in the selected precision.
+__global__ void __launch_bounds__(256) k_accumulate(WaveBuffers w, Accumulators acc, int mode) {
+  const int ns = w.pass->nsamples;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < w.npix; p += gridDim.x * blockDim.x) {
+    float s32[3], c32[3];
+    double s64[3], q64[3];
+    for (int c = 0; c < 3; ++c) {
+      s32[c] = mode != ACCUM_FP64 ? acc.sum32[3 * p + c] : 0.0f;
+      c32[c] = mode == ACCUM_KAHAN ? acc.comp32[3 * p + c] : 0.0f;
+      s64[c] = mode == ACCUM_FP64 ? acc.sum64[3 * p + c] : 0.0;
+      q64[c] = acc.sumsq ? acc.sumsq[3 * p + c] : 0.0;
+    }
+    for (int s = 0; s < ns; ++s) {
+      const float4 L = w.contrib[(size_t)s * w.npix + p];
+      const float l[3] = {L.x, L.y, L.z};
+      for (int c = 0; c < 3; ++c) {
+        if (mode == ACCUM_FP32) {
+          s32[c] = s32[c] + l[c];
+        } else if (mode == ACCUM_KAHAN) {
+          // Kahan-Babuska-Neumaier compensated summation
+          const float tsum = s32[c] + l[c];
+          if (fabsf(s32[c]) >= fabsf(l[c])) c32[c] += (s32[c] - tsum) + l[c];
+          else c32[c] += (l[c] - tsum) + s32[c];
+          s32[c] = tsum;
+        } else {
+          s64[c] += (double)l[c];
+        }
+        q64[c] += (double)l[c] * (double)l[c];
+      }
+    }
+    for (int c = 0; c < 3; ++c) {
+      if (mode != ACCUM_FP64) acc.sum32[3 * p + c] = s32[c];
+      if (mode == ACCUM_KAHAN) acc.comp32[3 * p + c] = c32[c];
+      if (mode == ACCUM_FP64) acc.sum64[3 * p + c] = s64[c];
+      if (acc.sumsq) acc.sumsq[3 * p + c] = q64[c];
+    }
+  }
+}
+
+__global__ void k_advance_pass(PassState* ps) {
+  ps->sample_base += ps->nsamples;
+  const int left = ps->sample_end - ps->sample_base;
+  ps->nsamples = left < ps->per_pass ? (left > 0 ? left : 0) : ps->per_pass;
+}
+
+// Tonemap of mean radiance: src/renderer.cu:426-441 and src/tonemapper.cu:32-76.
+__device__ __forceinline__ V3 uncharted2(V3 x) {
+  const float A = 0.15f, B = 0.50f, C = 0.10f, D = 0.20f, E = 0.02f, F = 0.30f;
+  const V3 num = v3(C * B + x.x * A, C * B + x.y * A, C * B + x.z * A);
+  const V3 nn = v3(D * E + x.x * num.x, D * E + x.y * num.y, D * E + x.z * num.z);
+  const V3 den = v3(B + x.x * A, B + x.y * A, B + x.z * A);
+  const V3 dd = v3(D * F + x.x * den.x, D * F + x.y * den.y, D * F + x.z * den.z);
+  return v3(-E / F + nn.x / dd.x, -E / F + nn.y / dd.y, -E / F + nn.z / dd.z);
+}
+__device__ __forceinline__ V3 tonemap_op(int op, V3 in) {
+  const float gamma = 1.0f / 2.2f;
+  switch (op) {
+    case 1:
+      return v3(powf(in.x / (1.0f + in.x), gamma), powf(in.y / (1.0f + in.y), gamma), powf(in.z / (1.0f + in.z), gamma));
+    case 2: {
+      const V3 x = v3(fmaxf(-0.004f + in.x, 0.0f), fmaxf(-0.004f + in.y, 0.0f), fmaxf(-0.004f + in.z, 0.0f));
+      return v3((x.x * (0.5f + x.x * 6.2f)) / (0.06f + x.x * (1.7f + x.x * 6.2f)),
+                (x.y * (0.5f + x.y * 6.2f)) / (0.06f + x.y * (1.7f + x.y * 6.2f)),
+                (x.z * (0.5f + x.z * 6.2f)) / (0.06f + x.z * (1.7f + x.z * 6.2f)));
+    }
+    case 3: {
+      const float W = 11.2f;
+      const V3 curr = uncharted2(mul(in, 2.0f));
+      const V3 white = uncharted2(v3(W, W, W));
+      const V3 ws = v3(1.0f / white.x, 1.0f / white.y, 1.0f / white.z);
+      return v3(powf(curr.x * ws.x, gamma), powf(curr.y * ws.y, gamma), powf(curr.z * ws.z, gamma));
+    }
+    default:
+      return v3(powf(in.x, gamma), powf(in.y, gamma), powf(in.z, gamma));
+  }
+}
+
+__global__ void k_tonemap(Accumulators acc, int mode, int npix, float samples, int op, uint8_t* rgb8, float* mean) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+    V3 sum;
+    if (mode == ACCUM_FP64) sum = v3((float)acc.sum64[3 * p], (float)acc.sum64[3 * p + 1], (float)acc.sum64[3 * p + 2]);
+    else if (mode == ACCUM_KAHAN)
+      sum = v3(acc.sum32[3 * p] + acc.comp32[3 * p], acc.sum32[3 * p + 1] + acc.comp32[3 * p + 1],
+               acc.sum32[3 * p + 2] + acc.comp32[3 * p + 2]);
+    else sum = v3(acc.sum32[3 * p], acc.sum32[3 * p + 1], acc.sum32[3 * p + 2]);
+    V3 avg = mul(sum, 1.0f / samples);
+    if (mean) {
+      mean[3 * p] = avg.x; mean[3 * p + 1] = avg.y; mean[3 * p + 2] = avg.z;
+    }
+    if (rgb8) {
+      avg = tonemap_op(op, avg);
+      avg = v3(fmaxf(fminf(avg.x, 1.0f), 0.0f), fmaxf(fminf(avg.y, 1.0f), 0.0f), fmaxf(fminf(avg.z, 1.0f), 0.0f));
+      rgb8[3 * p] = (uint8_t)(int)(255.0f * avg.x);
+      rgb8[3 * p + 1] = (uint8_t)(int)(255.0f * avg.y);
+      rgb8[3 * p + 2] = (uint8_t)(int)(255.0f * avg.z);
+    }
+  }
+}
+
+__global__ void k_clear(Accumulators acc, int npix) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * npix; i += gridDim.x * blockDim.x) {
+    if (acc.sum32) acc.sum32[i] = 0.0f;
+    if (acc.comp32) acc.comp32[i] = 0.0f;
+    if (acc.sum64) acc.sum64[i] = 0.0;
+    if (acc.sumsq) acc.sumsq[i] = 0.0;
+  }
+}
+
+// BSDF test hook: layout of illume_bsdf_batch (include/illume.h).
+struct FixedRng {
+  float u[3];
+  int k;
+  __device__ __forceinline__ float operator()() { return u[k < 3 ? k++ : 2]; }
+};
+
+__global__ void k_bsdf_batch(int type, int dist, const float* in, int n, float* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float* x = in + 16 * (size_t)i;
+    float* y = out + 16 * (size_t)i;
+    DevMaterial m;
+    m.type = type; m.albedo_tex = 0; m.roughness_tex = 0; m.medium = -1; m.distribution = dist;
+    m.ior = x[10];
+    for (int c = 0; c < 3; ++c) { m.eta[c] = x[11 + c]; m.k[c] = x[14]; }
+    m.diffuse_fresnel = x[15];
+    const V3 wi = v3(x[0], x[1], x[2]), N = v3(x[3], x[4], x[5]);
+    const V3 d = mul(wi, -1.0f);
+    FixedRng rng{{x[6], x[7], x[8]}, 0};
+    const ScatterResult s = scatter(m, d, N, v3(1.0f, 1.0f, 1.0f), x[9], rng);
+    const V3 nd = s.status == SCATTER_KILLED ? v3(0.0f, 0.0f, 0.0f) : normalize(s.dir);
+    y[0] = nd.x; y[1] = nd.y; y[2] = nd.z;
+    y[3] = s.weight.x; y[4] = s.weight.y; y[5] = s.weight.z;
+    y[6] = s.D; y[7] = s.pdf_m; y[8] = s.G; y[9] = s.F;
+    float ev = 0.0f, pd = 0.0f;
+    if (s.status == SCATTER_REFLECT && (type == MAT_ROUGHREFLECTIVE || type == MAT_ROUGHCONDUCTOR || type == MAT_ROUGHREFRACTIVE)) {
+      const float win = fabsf(dot(wi, N)), wom = fabsf(dot(nd, s.m));
+      ev = s.F * s.D * s.G / (4.0f * win);
+      pd = s.pdf_m / (4.0f * wom);
+    } else if (type == MAT_LAMBERT) {
+      const float won = fabsf(dot(nd, N));
+      ev = (float)((double)won * ILLUME_INV_PI_D);
+      pd = ev;
+    }
+    y[10] = ev; y[11] = pd; y[12] = (float)s.status; y[13] = y[14] = y[15] = 0.0f;
+  }
+}
+
+const void* shade_kernel_ptr() { return (const void*)k_shade; }
+
+void launch_raygen(const WaveBuffers& w, const CameraView& cam, const RenderKnobs& k, int grid, cudaStream_t st) {
+  k_raygen<<<grid, 256, 0, st>>>(w, cam, k);
+}
+void launch_shade(const WaveBuffers& w, const SceneView& sc, const RenderKnobs& k, int bounce, int grid,
+                  cudaStream_t st) {
+  k_shade<<<grid, 128, 0, st>>>(w, sc, k, bounce);
+}
+void launch_accumulate(const WaveBuffers& w, const Accumulators& acc, int mode, int grid, cudaStream_t st) {
+  k_accumulate<<<grid, 256, 0, st>>>(w, acc, mode);
+}
+void launch_advance_pass(const WaveBuffers& w, cudaStream_t st) { k_advance_pass<<<1, 1, 0, st>>>(w.pass); }
+void launch_tonemap(const Accumulators& acc, int mode, int npix, float samples, int op, uint8_t* rgb8, float* mean,
+                    cudaStream_t st) {
+  const int grid = (npix + 255) / 256;
+  if (grid > 0) k_tonemap<<<grid, 256, 0, st>>>(acc, mode, npix, samples, op, rgb8, mean);
+}
+void launch_clear_accumulators(const Accumulators& acc, int npix, cudaStream_t st) {
+  const int grid = (3 * npix + 255) / 256;
+  if (grid > 0) k_clear<<<grid < 4096 ? grid : 4096, 256, 0, st>>>(acc, npix);
+}
+void launch_bsdf_batch(int type, int dist, const float* in, int n, float* out, cudaStream_t st) {
+  if (n > 0) k_bsdf_batch<<<(n + 127) / 128, 128, 0, st>>>(type, dist, in, n, out);
+}
+
+}  // namespace illume

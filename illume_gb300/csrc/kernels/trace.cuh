@@ -1,0 +1,294 @@
+// Closest-hit queries on the device: spheres, then mesh instances, each instance's
+// triangles through its binary or 8-wide BVH.
+//
+// Semantics follow get_min_hit (src/renderer.cu:112-137) with a deterministic tie rule:
+// spheres in index order, then instances in index order, a later primitive replaces the
+// best only when strictly closer; inside one mesh the closest t wins and equal t goes
+// to the lower triangle index (the reference keeps the first one its traversal order
+// meets). Triangle tests are Moller-Trumbore as src/primitives/mesh.cu:445-476, or the
+// watertight test of Woop, Benthin and Wald (JCGT 2013), written operation by operation
+// like the CPU oracle so that, in this -fmad=false build, hits match it bit for bit.
+// Box tests are conservative: boxes are padded when built and the exit distance is
+// widened by 8 ulp, so no box that contains a reported hit is culled.
+#pragma once
+
+#include "../common/dmath.cuh"
+#include "../common/types.h"
+
+namespace illume {
+
+static constexpr float kExitSlack = 1.000001f;  // ~8 ulp widening of box exit distances
+static constexpr int kStack = 64;
+// Upper bound on node fetches of one ray in one mesh: a well-formed tree never comes
+// close (each node is fetched at most once per ray); it only bounds the loop.
+static constexpr int kMaxNodeVisits = 1 << 22;
+
+struct TraceRay {
+  V3 o, d;        // object-space origin / direction (direction as given, not normalised)
+  V3 idir;        // clamped reciprocal direction for box tests
+  int oct;        // bit 2: d.x < 0, bit 1: d.y < 0, bit 0: d.z < 0
+  // watertight setup
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+};
+
+__device__ __forceinline__ float safe_rcp(float d) {
+  return 1.0f / (fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d));
+}
+
+__device__ __forceinline__ void setup_ray(TraceRay& r, V3 o, V3 d, int isect) {
+  r.o = o;
+  r.d = d;
+  r.idir = v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+  r.oct = (d.x < 0.0f ? 4 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 1 : 0);
+  if (isect == ISECT_WATERTIGHT) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    const float dd[3] = {d.x, d.y, d.z};
+    const float dz = dd[kz];
+    if (dz < 0.0f) { const int t = kx; kx = ky; ky = t; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.Sx = dd[kx] / dz;
+    r.Sy = dd[ky] / dz;
+    r.Sz = 1.0f / dz;
+  }
+}
+
+__device__ __forceinline__ float comp(V3 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+// Moller-Trumbore (returns -1 on a miss)
+__device__ __forceinline__ float tri_mt(V3 v0, V3 v1, V3 v2, const TraceRay& r, float& u, float& v) {
+  const V3 e1 = sub(v1, v0), e2 = sub(v2, v0);
+  const V3 P = cross(r.d, e2);
+  float det = dot(e1, P);
+  if (fabsf(det) < FLT_EPSILON) return -1.0f;
+  det = 1.0f / det;
+  const V3 T = sub(r.o, v0);
+  u = dot(T, P) * det;
+  if (u < 0.0f || u > 1.0f) return -1.0f;
+  const V3 Q = cross(T, e1);
+  v = dot(r.d, Q) * det;
+  if (v < 0.0f || u + v > 1.0f) return -1.0f;
+  return dot(e2, Q) * det;
+}
+
+// Watertight test (returns -1 on a miss); u, v weight vertices 1 and 2.
+__device__ __forceinline__ float tri_wt(V3 v0, V3 v1, V3 v2, const TraceRay& r, float& u, float& v) {
+  const V3 A = sub(v0, r.o), B = sub(v1, r.o), C = sub(v2, r.o);
+  const float Akz = comp(A, r.kz), Bkz = comp(B, r.kz), Ckz = comp(C, r.kz);
+  const float Ax = comp(A, r.kx) - r.Sx * Akz, Ay = comp(A, r.ky) - r.Sy * Akz;
+  const float Bx = comp(B, r.kx) - r.Sx * Bkz, By = comp(B, r.ky) - r.Sy * Bkz;
+  const float Cx = comp(C, r.kx) - r.Sx * Ckz, Cy = comp(C, r.ky) - r.Sy * Ckz;
+  float U = Cx * By - Cy * Bx;
+  float V = Ax * Cy - Ay * Cx;
+  float W = Bx * Ay - By * Ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = (float)(__dmul_rn((double)Cx, (double)By) - __dmul_rn((double)Cy, (double)Bx));
+    V = (float)(__dmul_rn((double)Ax, (double)Cy) - __dmul_rn((double)Ay, (double)Cx));
+    W = (float)(__dmul_rn((double)Bx, (double)Ay) - __dmul_rn((double)By, (double)Ax));
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return -1.0f;
+  const float det = U + V + W;
+  if (det == 0.0f) return -1.0f;
+  const float Az = r.Sz * Akz, Bz = r.Sz * Bkz, Cz = r.Sz * Ckz;
+  const float T = U * Az + V * Bz + W * Cz;
+  if ((det < 0.0f && T >= 0.0f) || (det > 0.0f && T <= 0.0f)) return -1.0f;
+  const float rcp = 1.0f / det;
+  u = V * rcp;
+  v = W * rcp;
+  return T * rcp;
+}
+
+struct MeshBest { float t; int prim; float u, v; };
+
+// Visit counters of the instrumented trace kernel (node fetches, triangle tests).
+struct VisitCount { unsigned nodes = 0, tris = 0; };
+
+__device__ __forceinline__ void test_triangle(const float4* tv, int isect, const TraceRay& r, MeshBest& b) {
+  const float4 a = __ldg(tv), bb = __ldg(tv + 1), c = __ldg(tv + 2);
+  const V3 v0 = v3(a.x, a.y, a.z), v1 = v3(bb.x, bb.y, bb.z), v2 = v3(c.x, c.y, c.z);
+  float u = 0.0f, v = 0.0f;
+  const float t = isect == ISECT_MT ? tri_mt(v0, v1, v2, r, u, v) : tri_wt(v0, v1, v2, r, u, v);
+  const int prim = __float_as_int(a.w);
+  if (t > 0.0f && (t < b.t || (t == b.t && prim < b.prim))) {
+    b.t = t; b.prim = prim; b.u = u; b.v = v;
+  }
+}
+
+// Slab test against one box with sign-selected near/far planes.
+__device__ __forceinline__ bool box_hit(float lox, float loy, float loz, float hix, float hiy, float hiz,
+                                        const TraceRay& r, float tbest, float& tentry) {
+  const float nx = r.idir.x >= 0.0f ? lox : hix, fx = r.idir.x >= 0.0f ? hix : lox;
+  const float ny = r.idir.y >= 0.0f ? loy : hiy, fy = r.idir.y >= 0.0f ? hiy : loy;
+  const float nz = r.idir.z >= 0.0f ? loz : hiz, fz = r.idir.z >= 0.0f ? hiz : loz;
+  const float t0 = fmaxf(fmaxf((nx - r.o.x) * r.idir.x, (ny - r.o.y) * r.idir.y), fmaxf((nz - r.o.z) * r.idir.z, 0.0f));
+  const float t1 = fminf(fminf((fx - r.o.x) * r.idir.x, (fy - r.o.y) * r.idir.y), (fz - r.o.z) * r.idir.z) * kExitSlack;
+  tentry = t0;
+  return t0 <= t1 && t0 <= tbest * kExitSlack;
+}
+
+// ---- binary BVH ----
+template <bool COUNT>
+__device__ __forceinline__ void traverse_bvh2(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
+                                              int* stack, VisitCount& vc) {
+  int sp = 0;
+  int node = 0;
+  for (int guard = 0; guard < kMaxNodeVisits; ++guard) {
+    if (COUNT) vc.nodes++;
+    const Bvh2Node* n = m.bvh2 + node;
+    const float4 a = __ldg(&n->a), b = __ldg(&n->b), c = __ldg(&n->c);
+    const int4 d = __ldg(&n->d);
+    float te0, te1;
+    const bool h0 = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0);
+    const bool h1 = box_hit(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1);
+    // leaves are tested at once; inner children are visited near first
+    int inner0 = -1, inner1 = -1;
+    if (h0) {
+      if (d.x < 0) {
+        if (COUNT) vc.tris += d.z;
+        for (int i = ~d.x; i < ~d.x + d.z; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
+      }
+      else inner0 = d.x;
+    }
+    if (h1) {
+      if (d.y < 0) {
+        if (COUNT) vc.tris += d.w;
+        for (int i = ~d.y; i < ~d.y + d.w; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
+      }
+      else inner1 = d.y;
+    }
+    if (inner0 >= 0 && inner1 >= 0) {
+      const bool swap = te1 < te0;
+      node = swap ? inner1 : inner0;
+      if (sp < kStack) stack[sp++] = swap ? inner0 : inner1;
+      continue;
+    }
+    if (inner0 >= 0) { node = inner0; continue; }
+    if (inner1 >= 0) { node = inner1; continue; }
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+}
+
+// ---- 8-wide quantised BVH ----
+__device__ __forceinline__ float exp2i(uint8_t biased) { return __int_as_float((int)biased << 23); }
+
+template <bool COUNT>
+__device__ __forceinline__ void traverse_wide(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
+                                              uint2* stack, VisitCount& vc) {
+  // group = (child_base, imask << 8 | pending visit-rank bits)
+  int sp = 0;
+  uint32_t node = 0;
+  for (int guard = 0; guard < kMaxNodeVisits; ++guard) {
+    if (COUNT) vc.nodes++;
+    const float4* np = reinterpret_cast<const float4*>(m.wide + node);
+    const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3), q4 = __ldg(np + 4);
+    const float px = q0.x, py = q0.y, pz = q0.z;
+    const uint32_t ew = __float_as_uint(q0.w);
+    const uint8_t ex = ew & 0xff, ey = (ew >> 8) & 0xff, ez = (ew >> 16) & 0xff;
+    const uint32_t imask = ew >> 24;
+    const uint32_t child_base = __float_as_uint(q1.x), tri_base = __float_as_uint(q1.y);
+    const uint32_t meta[2] = {__float_as_uint(q1.z), __float_as_uint(q1.w)};
+    const uint32_t qlx[2] = {__float_as_uint(q2.x), __float_as_uint(q2.y)};
+    const uint32_t qly[2] = {__float_as_uint(q2.z), __float_as_uint(q2.w)};
+    const uint32_t qlz[2] = {__float_as_uint(q3.x), __float_as_uint(q3.y)};
+    const uint32_t qhx[2] = {__float_as_uint(q3.z), __float_as_uint(q3.w)};
+    const uint32_t qhy[2] = {__float_as_uint(q4.x), __float_as_uint(q4.y)};
+    const uint32_t qhz[2] = {__float_as_uint(q4.z), __float_as_uint(q4.w)};
+    // per-axis affine map q -> t
+    const float sx = exp2i(ex) * r.idir.x, sy = exp2i(ey) * r.idir.y, sz = exp2i(ez) * r.idir.z;
+    const float bx = (px - r.o.x) * r.idir.x, by = (py - r.o.y) * r.idir.y, bz = (pz - r.o.z) * r.idir.z;
+    uint32_t pending = 0;
+    for (int s = 0; s < 8; ++s) {
+      const int w = s >> 2, sh = (s & 3) * 8;
+      const uint32_t me = (meta[w] >> sh) & 0xff;
+      const bool inner = (imask >> s) & 1;
+      if (!inner && me == 0) continue;
+      const float lx = (float)((qlx[w] >> sh) & 0xff), hx = (float)((qhx[w] >> sh) & 0xff);
+      const float ly = (float)((qly[w] >> sh) & 0xff), hy = (float)((qhy[w] >> sh) & 0xff);
+      const float lz = (float)((qlz[w] >> sh) & 0xff), hz = (float)((qhz[w] >> sh) & 0xff);
+      const float nx = r.idir.x >= 0.0f ? lx : hx, fx = r.idir.x >= 0.0f ? hx : lx;
+      const float ny = r.idir.y >= 0.0f ? ly : hy, fy = r.idir.y >= 0.0f ? hy : ly;
+      const float nz = r.idir.z >= 0.0f ? lz : hz, fz = r.idir.z >= 0.0f ? hz : lz;
+      const float t0 = fmaxf(fmaxf(__fmaf_rn(nx, sx, bx), __fmaf_rn(ny, sy, by)), fmaxf(__fmaf_rn(nz, sz, bz), 0.0f));
+      const float t1 = fminf(fminf(__fmaf_rn(fx, sx, bx), __fmaf_rn(fy, sy, by)), __fmaf_rn(fz, sz, bz)) * kExitSlack;
+      if (!(t0 <= t1 && t0 <= best.t * kExitSlack)) continue;
+      if (inner) {
+        pending |= 1u << (s ^ r.oct);
+      } else {
+        const uint32_t cnt = me >> 5, off = me & 31;
+        if (COUNT) vc.tris += cnt;
+        for (uint32_t i = 0; i < cnt; ++i) test_triangle(m.wide_tris + 3 * (tri_base + off + i), isect, r, best);
+      }
+    }
+    if (pending) {
+      const int k = __ffs(pending) - 1;
+      pending &= pending - 1;
+      const int slot = k ^ r.oct;
+      node = child_base + __popc(imask & ((1u << slot) - 1));
+      if (pending && sp < kStack) stack[sp++] = make_uint2(child_base, (imask << 8) | pending);
+      continue;
+    }
+    // pop the next pending child of a stacked group
+    bool found = false;
+    while (sp > 0) {
+      uint2& g = stack[sp - 1];
+      uint32_t pend = g.y & 0xff;
+      if (!pend) { --sp; continue; }
+      const int k = __ffs(pend) - 1;
+      pend &= pend - 1;
+      const uint32_t im = g.y >> 8;
+      const int slot = k ^ r.oct;
+      node = g.x + __popc(im & ((1u << slot) - 1));
+      if (pend) g.y = (im << 8) | pend; else --sp;
+      found = true;
+      break;
+    }
+    if (!found) break;
+  }
+}
+
+// Full closest-hit query for a world-space ray (direction used as given).
+template <int KIND, bool COUNT = false>
+__device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
+                                                 VisitCount* vcp = nullptr) {
+  VisitCount vc;
+  HitRecord h;
+  h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f; h.prim = -1; h.geom = -1;
+  // spheres (src/primitives/sphere.cu:43-77)
+  for (int s = 0; s < sc.num_spheres; ++s) {
+    const DevSphere sp = sc.spheres[s];
+    const V3 l = sub(v3(sp.cx, sp.cy, sp.cz), o);
+    const float sd = dot(l, d);
+    const float ls = dot(l, l);
+    const float rs = sp.r * sp.r;
+    if (sd < 0.0f && ls > rs) continue;
+    const float ms = ls - sd * sd;
+    if (ms > rs) continue;
+    const float q = sqrtf(rs - ms);
+    const float t = ls > rs ? sd - q : sd + q;
+    if (t < h.t) { h.t = t; h.geom = -2 - s; h.prim = -1; }
+  }
+  // world-space probe for instance boxes
+  TraceRay wr;
+  wr.o = o; wr.d = d;
+  wr.idir = v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+  for (int i = 0; i < sc.num_instances; ++i) {
+    const DevInstance& in = sc.instances[i];
+    float te;
+    if (!box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) continue;
+    TraceRay r;
+    setup_ray(r, xform(in.inv, o, 1.0f), xform(in.inv, d, 0.0f), isect);
+    MeshBest b{h.t, -1, 0.0f, 0.0f};
+    const DevMesh& m = sc.meshes[in.mesh];
+    if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);
+    else traverse_bvh2<COUNT>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
+    if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }
+  }
+  if (COUNT && vcp) *vcp = vc;
+  return h;
+}
+
+}  // namespace illume

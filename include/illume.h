@@ -179,7 +179,10 @@ void* illume_context_stream(illume_context* ctx);
 
 /* ---- scenes: HostScene + SceneRef ---- */
 /* Parse a scene file in the reference JSON format; relative "file" paths resolve
- * against base_dir (NULL = the current directory, as the reference does). */
+ * against base_dir (NULL = the current directory, as the reference does).
+ * With ctx == NULL the three scene constructors build a host-only scene (parsed,
+ * validated, BVHs built, nothing uploaded): it can be described and checked, not
+ * rendered. */
 int illume_scene_load_json(illume_context* ctx, const char* path, const char* base_dir, illume_scene** out);
 int illume_scene_load_json_string(illume_context* ctx, const char* json, const char* base_dir, illume_scene** out);
 int illume_scene_create(illume_context* ctx, const illume_scene_desc* desc, illume_scene** out);
@@ -187,6 +190,14 @@ int illume_scene_create(illume_context* ctx, const illume_scene_desc* desc, illu
 int illume_scene_describe(const illume_scene* scene, illume_scene_desc* out);
 /* Device bytes held by the scene (geometry, BVHs, textures). */
 int illume_scene_device_bytes(const illume_scene* scene, size_t* out);
+/* Copies the scene's host tables to its device buffers again (what the reference's
+ * SceneRef does at the start of every render_to_bitmap, src/scene/sceneref.cpp:9-122);
+ * synchronous. Returns the bytes copied in *bytes (nullable). */
+int illume_scene_upload(illume_scene* scene, size_t* bytes);
+/* Checks the BVH invariants of every mesh (each triangle referenced exactly once, child
+ * boxes inside their parent's, quantised boxes containing the exact boxes) and writes a
+ * one-line summary per mesh (node counts, depths) into report. */
+int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t report_len);
 int illume_scene_destroy(illume_scene* scene);
 
 /* ---- renderer ---- */
@@ -213,6 +224,20 @@ int illume_render_device(illume_renderer* r, int accumulate, illume_render_stats
 /* Copies the device accumulators (sum, sumsq as in illume_render) to host buffers. */
 int illume_renderer_read(illume_renderer* r, float* out_mean, double* out_sum, double* out_sumsq, uint8_t* out_rgb8);
 
+/* Per-stage timing of one wavefront pass (samples_per_pass samples of every pixel),
+ * launched kernel by kernel with CUDA events on the context stream. With count_visits,
+ * the pass runs an instrumented trace kernel that counts node fetches and triangle
+ * tests (its timings are then not representative). Accumulates into the renderer like
+ * a progressive call. */
+typedef struct {
+  double raygen_ms, trace_ms, shade_ms, accumulate_ms;
+  int64_t trace_launches, shade_launches;
+  int64_t rays;
+  int64_t node_fetches, tri_tests;   /* count_visits only */
+  int64_t node_bytes, tri_bytes;     /* bytes of one node / one triangle record in the BVH used */
+} illume_profile;
+int illume_renderer_profile(illume_renderer* r, int count_visits, illume_profile* out);
+
 /* ---- bitmap (src/bitmap.h:26-30) ---- */
 illume_bitmap* illume_bitmap_new(size_t width, size_t height);
 void illume_bitmap_free(illume_bitmap* bitmap);
@@ -230,9 +255,10 @@ int illume_trace_closest_device(illume_context* ctx, illume_scene* scene, const 
                                 int intersector, int bvh_kind, illume_hit* d_hits);
 /* BSDF sample / eval / pdf on the device for n tuples (host buffers). Each input tuple
  * is 16 floats: wi (3, pointing away from the surface), n (3), u1, u2, u3, roughness,
- * ior, eta.xyz, k.x, (unused); outputs are 16 floats: new_dir (3), weight (3), D, pdf_m,
- * G, F, eval (f * cos), pdf_dir, status (0 killed, 1 reflect, 2 transmit), 3 unused.
- * For conductors k.yz are taken equal to k.x. */
+ * ior, eta.xyz, k, plastic diffuse-Fresnel term (0 = computed from ior); outputs are 16
+ * floats: new_dir (3), weight (3), D, pdf_m, G, F, eval (f * cos, reflection), pdf_dir,
+ * status (0 killed, 1 reflect, 2 transmit), 3 unused. The albedo is 1; conductors use
+ * the one k for all three channels. */
 int illume_bsdf_batch(illume_context* ctx, int material_type, int distribution, const float* inputs, int n,
                       float* outputs);
 

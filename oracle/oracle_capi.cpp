@@ -346,7 +346,7 @@ void oracle_bsdf_batch(int material_type, int distribution, const float* in, int
     // Layout: wi(0..2) n(3..5) u1 u2 u3 (6..8) roughness (9) ior (10) eta (11..13) k (14)
     m2.ior = x[10];
     for (int c = 0; c < 3; ++c) { m2.eta[c] = x[11 + c]; m2.k[c] = x[14]; }
-    m2.diffuse_fresnel = material_type == MAT_PLASTIC ? diffuse_fresnel(1.0f / x[10], 1000000) : 0.0f;
+    m2.diffuse_fresnel = material_type != MAT_PLASTIC ? 0.0f : (x[15] != 0.0f ? x[15] : diffuse_fresnel(1.0f / x[10], 1000000));
     auto run2 = [&](auto zero) {
       using R = decltype(zero);
       int k = 0;

@@ -1,0 +1,199 @@
+"""The oracle (CPU restatement) pinned against the reference's own code.
+
+The fixtures in tests/golden/ were produced by the reference renderer's sources built
+for the host (tests/golden/make_golden.py). FP32 components compare within a few ulp
+(libm's float functions may differ by an ulp between CPU architectures; arithmetic-only
+functions compare exactly); renders compare per pixel.
+"""
+import numpy as np
+import pytest
+
+from conftest import f32_normalize, golden, golden_scene, rays6_to_8
+from illume_gb300 import _capi as C
+
+
+def ulp_diff(a, b):
+    a = np.ascontiguousarray(a, np.float32).view(np.int32).astype(np.int64)
+    b = np.ascontiguousarray(b, np.float32).view(np.int32).astype(np.int64)
+    a = np.where(a < 0, -(a & 0x7FFFFFFF), a)
+    b = np.where(b < 0, -(b & 0x7FFFFFFF), b)
+    return np.abs(a - b)
+
+
+def fp(a):
+    import ctypes
+    return np.ascontiguousarray(a, np.float32).ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def test_philox_known_answers(oracle_lib):
+    from oracle import pyoracle
+    from illume_gb300 import synth
+    kat = [([0, 0, 0, 0], [0, 0], [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]),
+           ([0xffffffff] * 4, [0xffffffff] * 2, [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]),
+           ([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0],
+            [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1])]
+    for ctr, key, want in kat:
+        assert pyoracle.philox(ctr, key) == want
+        got = synth.philox4x32_10(*[np.array([c]) for c in ctr], key[0], key[1])
+        assert [int(g[0]) for g in got] == want
+
+
+def test_fresnel_and_microfacet_components(oracle_lib):
+    z = golden("ref_components.npz")
+    L = oracle_lib
+    n = len(z["fres_cosI"])
+    F = np.zeros(n, np.float32)
+    cT = np.zeros(n, np.float32)
+    for i in range(n):
+        c = np.zeros(1, np.float32)
+        F[i] = L.oracle_fresnel_dielectric(float(z["fres_cosI"][i]), float(z["fres_ior"][i]), fp(c))
+        cT[i] = c[0]
+    assert ulp_diff(F, z["fres_F"]).max() <= 2
+    assert ulp_diff(cT, z["fres_cosT"]).max() <= 2
+    cond = np.array([L.oracle_fresnel_conductor1(float(a), float(b), float(c))
+                     for a, b, c in zip(z["cond_eta"], z["cond_k"], z["cond_cos"])], np.float32)
+    assert ulp_diff(cond, z["cond_F"]).max() <= 2
+    dfr = np.array([L.oracle_diffuse_fresnel(float(1.0 / x), 1000000) for x in z["dfres_ior"]], np.float32)
+    assert ulp_diff(dfr, z["dfres_val"]).max() <= 4
+    D = np.array([L.oracle_D_beckmann(fp(z["basis_out"][i]), fp(z["basis_n"][i]), float(z["alpha"][i]))
+                  for i in range(n)], np.float32)
+    ok = np.isfinite(z["D_beck"])
+    assert ulp_diff(D[ok], z["D_beck"][ok]).max() <= 8
+    G = np.array([L.oracle_G_beckmann(fp(z["G_wi"][i]), fp(z["G_wo"][i]), fp(z["basis_out"][i]), float(z["alpha"][i]))
+                  for i in range(n)], np.float32)
+    ok = np.isfinite(z["G_beck"])
+    assert ulp_diff(G[ok], z["G_beck"][ok]).max() <= 8
+
+
+@pytest.mark.parametrize("which", ["hemi", "circle", "sphere", "hg", "beck"])
+def test_samplers(oracle_lib, which):
+    z = golden("ref_components.npz")
+    L = oracle_lib
+    u, a, g = z["u"], z["alpha"], z["g"]
+    out = np.zeros((len(u), 3), np.float32)
+    for i in range(len(u)):
+        o = out[i]
+        if which == "hemi":
+            L.oracle_sample_hemisphere_cosine(float(u[i, 0]), float(u[i, 1]), fp(o))
+        elif which == "circle":
+            L.oracle_sample_circle(float(u[i, 0]), float(u[i, 1]), fp(o))
+        elif which == "sphere":
+            L.oracle_sample_sphere(float(u[i, 0]), float(u[i, 1]), fp(o))
+        elif which == "hg":
+            L.oracle_sample_hg(float(g[i]), float(u[i, 0]), float(u[i, 1]), 0, fp(o))
+        else:
+            L.oracle_sample_beckmann(float(a[i]), float(u[i, 0]), float(u[i, 1]), fp(o))
+    ref = z["s_" + which]
+    ok = np.isfinite(ref).all(1)
+    # values near zero: compare absolutely
+    assert np.abs(out[ok] - ref[ok]).max() <= 4e-7
+    assert (ulp_diff(out[ok], ref[ok]) <= 2).mean() > 0.999
+
+
+def test_to_basis(oracle_lib):
+    z = golden("ref_components.npz")
+    out = np.zeros_like(z["basis_out"])
+    for i in range(len(out)):
+        oracle_lib.oracle_to_basis(fp(z["basis_v"][i]), fp(z["basis_n"][i]), fp(out[i]))
+    assert np.abs(out - z["basis_out"]).max() <= 4e-7
+
+
+def test_triangle_aabb_sphere_tests_exact(oracle_lib):
+    z = golden("ref_components.npz")
+    L = oracle_lib
+    n = len(z["tri_t"])
+    for i in range(n):
+        u = np.zeros(1, np.float32)
+        v = np.zeros(1, np.float32)
+        t = L.oracle_triangle_mt(fp(z["tri_v"][i, 0]), fp(z["tri_v"][i, 1]), fp(z["tri_v"][i, 2]), fp(z["tri_o"][i]),
+                                 fp(z["tri_d"][i]), fp(u), fp(v))
+        assert np.float32(t) == z["tri_t"][i]
+        if t > 0:
+            assert u[0] == z["tri_u"][i] and v[0] == z["tri_v_out"][i]
+        bt = L.oracle_aabb_intersect(fp(z["box_lo"][i]), fp(z["box_hi"][i]), fp(z["tri_o"][i]), fp(z["tri_d"][i]))
+        assert np.float32(bt) == z["box_t"][i]
+    hits = 0
+    for i in range(n):
+        t = np.zeros(1, np.float32)
+        nn = np.zeros(3, np.float32)
+        uv = np.zeros(2, np.float32)
+        h = L.oracle_sphere_intersect(fp(z["sph_c"][i]), float(z["sph_r"][i]), fp(z["tri_o"][i]), fp(z["tri_d"][i]),
+                                      fp(t), fp(nn), fp(uv))
+        assert h == z["sph_hit"][i]
+        if h:
+            hits += 1
+            assert t[0] == z["sph_t"][i]
+            assert np.array_equal(nn, z["sph_n"][i])
+            assert np.abs(uv - z["sph_uv"][i]).max() <= 1.2e-7
+    assert hits > 100
+
+
+def test_tonemap_operators(oracle_lib):
+    z = golden("ref_components.npz")
+    x = z["tone_in"]
+    for op in range(4):
+        out = np.zeros_like(x)
+        for i in range(len(x)):
+            oracle_lib.oracle_tonemap_eval(op, fp(x[i]), fp(out[i]))
+        assert (ulp_diff(out, z[f"tone{op}"]) <= 2).all(), op
+
+
+@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+def test_camera_rays_bit_exact(oracle_lib, name):
+    from oracle import pyoracle
+    z = golden(f"ref_scene_{name}.npz")
+    os_ = pyoracle.OracleScene(golden_scene(name))
+    W, H = (int(v) for v in z["camera_size"])
+    assert np.array_equal(os_.camera_rays(W, H, sample=5, seed=0), z["camera_rays"])
+
+
+@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+def test_closest_hits_match_reference(oracle_lib, name):
+    from oracle import pyoracle
+    z = golden(f"ref_scene_{name}.npz")
+    sd = golden_scene(name)
+    os_ = pyoracle.OracleScene(sd)
+    rays = z["hit_rays"].copy()
+    rays[:, 3:] = f32_normalize(rays[:, 3:])      # the reference normalises in ray_create
+    h = os_.closest_hit(rays6_to_8(rays), isect=C.ISECT_MT)
+    ns = len(sd.spheres)
+    prim = np.where(h["sphere"] >= 0, h["sphere"], np.where(h["inst"] >= 0, ns + h["inst"], -1))
+    assert (prim == z["hit_prim"]).mean() >= 0.999
+    same = prim == z["hit_prim"]
+    hit = same & (prim >= 0)
+    assert (h["t"][hit] == z["hit_t"][hit]).mean() >= 0.999
+
+
+@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+def test_render_matches_reference_integrator(oracle_lib, name):
+    """Same Philox streams: the oracle's FP32 path equals the reference's path by path."""
+    from oracle import pyoracle
+    z = golden(f"ref_scene_{name}.npz")
+    sd = golden_scene(name)
+    os_ = pyoracle.OracleScene(sd)
+    w, h, spp, depth = (int(v) for v in z["render_size"])
+    s, s2, rays = os_.render(w, h, spp, depth, isect=C.ISECT_MT, precision=32)
+    assert rays == int(z["render_rays"])
+    ref = z["render_sum"].astype(np.float64)
+    rel = np.abs(s - ref) / np.maximum(np.abs(ref), 1e-3)
+    assert (rel.max(1) < 1e-5).mean() >= 0.999
+    rgb = pyoracle.tonemap_image(s, float(spp), sd.tonemapper)
+    assert (rgb.astype(int) - z["render_rgb8"].astype(int)).__abs__().max() <= 1
+    assert (rgb == z["render_rgb8"]).all(1).mean() >= 0.999
+
+
+def test_oracle_bvh_equals_brute_force(oracle_lib):
+    from oracle import pyoracle
+    from illume_gb300 import synth
+    sd = synth.traversal_scene(tris=8000, env_size=(16, 8), width=32, height=32)
+    os_ = pyoracle.OracleScene(sd)
+    rng = np.random.default_rng(3)
+    o = rng.uniform(-3, 3, size=(1500, 3)).astype(np.float32)
+    d = f32_normalize(rng.normal(size=(1500, 3)))
+    r8 = rays6_to_8(np.concatenate([o, d], 1))
+    for isect in (C.ISECT_MT, C.ISECT_WATERTIGHT):
+        a = os_.closest_hit(r8, isect=isect)
+        b = os_.closest_hit(r8, isect=isect, brute=True)
+        for k in ("inst", "prim", "sphere"):
+            assert np.array_equal(a[k], b[k]), (isect, k)
+        assert np.array_equal(a["t"], b["t"])
