@@ -136,6 +136,7 @@ PROTOTYPES = {
                               POINTER(RenderStats)]),
     "illume_render_device": (c_int, [c_void_p, c_int, POINTER(RenderStats)]),
     "illume_renderer_read": (c_int, [c_void_p, _pf, POINTER(c_double), POINTER(c_double), POINTER(c_uint8)]),
+    "illume_render_noalloc": (c_int, [c_void_p, c_void_p, POINTER(RenderParams), c_void_p]),
     "illume_bitmap_new": (POINTER(Bitmap), [c_size_t, c_size_t]),
     "illume_bitmap_free": (None, [POINTER(Bitmap)]),
     "illume_bitmap_save_png": (c_int, [POINTER(Bitmap), c_char_p]),

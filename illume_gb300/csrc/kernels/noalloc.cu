@@ -1,0 +1,155 @@
+// illume_render_noalloc: the wavefront render for callers that cannot allocate device
+// memory at render time.
+//
+// Who needs it: hosts that hand all device memory to their own pool at start-up (a
+// later cudaMalloc then fails), and latency-bound frame loops in which a cudaMalloc or
+// cudaFree would stall the frame (cudaFree synchronises the device). Such callers
+// create the context and upload the scene once at set-up, then render every frame
+// through this entry point, which allocates nothing.
+//
+// How: the queues and counters the wavefront kernels need live in one file-scope
+// __device__ array of kNoAllocScratchBytes (about 12 MB). Every GPU that loads this
+// library reserves that array until the process exits. Host code cannot use the
+// array's name as a device address, so the first call on each device, with that device
+// current, asks the runtime for the array's address (cudaGetSymbolAddress) and caches
+// it; make that first call before any stream capture. The kernels are the same ones
+// illume_render_device launches, pointed at slices of the array, one sample of every
+// pixel per pass, FP32 accumulation straight into the caller's output buffer.
+//
+// Every call shares the one array, which keeps the previous call's contents: each call
+// clears the counters it needs and the caller's output before rendering. Calls whose
+// work overlaps on the GPU (for example on two streams, or from two contexts on one
+// device) race on the array: the caller must order them.
+#include <algorithm>
+#include <mutex>
+#include <string>
+
+#include "launch.h"
+#include "../host/handles.h"
+
+namespace illume {
+
+static constexpr size_t kNoAllocMaxPaths = ILLUME_NOALLOC_MAX_PIXELS;
+static constexpr size_t kNoAllocPerPath = 6 * sizeof(float4) + sizeof(float4) + sizeof(int) + EV_COUNT * sizeof(int) +
+                                          sizeof(float4);
+static constexpr size_t kNoAllocScratchBytes = kNoAllocMaxPaths * kNoAllocPerPath + 4096;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[256];
+
+// Clears what must start at zero (counters, ray and visit totals, the output sums) and
+// sets the pass state for the first sample.
+__global__ void k_noalloc_begin(int* counters, unsigned long long* rays, unsigned long long* visits, PassState* ps,
+                                float* sum, int npix, int sample_begin, int spp) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 64) counters[i] = 0;
+  if (i == 0) {
+    *rays = 0;
+    visits[0] = visits[1] = 0;
+    ps->sample_base = sample_begin;
+    ps->per_pass = 1;
+    ps->sample_end = sample_begin + spp;
+    ps->nsamples = spp > 0 ? 1 : 0;
+  }
+  for (int k = i; k < 3 * npix; k += gridDim.x * blockDim.x) sum[k] = 0.0f;
+}
+
+static unsigned char* carve(unsigned char*& p, size_t bytes) {
+  unsigned char* r = p;
+  p += (bytes + 255) & ~(size_t)255;
+  return r;
+}
+
+}  // namespace illume
+
+using namespace illume;
+
+extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, const illume_render_params* params,
+                                     float* d_sum) {
+  if (!ctx || !scene || !params || !d_sum) { set_error("null argument"); return ILLUME_ERR_INVALID; }
+  if (scene->s.ctx != &ctx->c) { set_error("scene was not uploaded with this context"); return ILLUME_ERR_INVALID; }
+  const illume_render_params& p = *params;
+  const long long npix = (long long)p.width * p.height;
+  if (p.width <= 0 || p.height <= 0 || npix > (long long)kNoAllocMaxPaths) {
+    set_error("illume_render_noalloc: image of " + std::to_string(npix) + " pixels exceeds the fixed scratch limit of " +
+              std::to_string(kNoAllocMaxPaths) + " pixels (use illume_render_device)");
+    return ILLUME_ERR_INVALID;
+  }
+  if (p.spp < 0 || p.max_depth < 0) { set_error("negative spp or depth"); return ILLUME_ERR_INVALID; }
+  if (p.accum_mode != ILLUME_ACCUM_FP32) { set_error("illume_render_noalloc accumulates in FP32 only"); return ILLUME_ERR_INVALID; }
+  if (p.intersector != ILLUME_ISECT_MT && p.intersector != ILLUME_ISECT_WATERTIGHT) { set_error("unknown intersector"); return ILLUME_ERR_INVALID; }
+  if (p.bvh_kind != ILLUME_BVH_BINARY && p.bvh_kind != ILLUME_BVH_WIDE8) { set_error("unknown BVH kind"); return ILLUME_ERR_INVALID; }
+  const int dev = ctx->c.device;
+  if (dev < 0 || dev >= 256) { set_error("device index out of range"); return ILLUME_ERR_INVALID; }
+  ILLUME_CUDA_TRY(cudaSetDevice(dev));
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* ptr = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess || !ptr) {
+        set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        return ILLUME_ERR_CUDA;
+      }
+      g_noalloc_ptr[dev] = ptr;
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  const int cap = (int)npix;
+  unsigned char* cur = static_cast<unsigned char*>(base);
+  WaveBuffers w{};
+  for (int k = 0; k < 2; ++k) {
+    w.q_orig[k] = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
+    w.q_dir[k] = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
+    w.q_thr[k] = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
+  }
+  w.hit = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
+  w.hit_geom = reinterpret_cast<int*>(carve(cur, sizeof(int) * cap));
+  w.evq = reinterpret_cast<int*>(carve(cur, sizeof(int) * (size_t)cap * EV_COUNT));
+  w.contrib = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
+  w.counters = reinterpret_cast<int*>(carve(cur, sizeof(int) * 64));
+  w.rays = reinterpret_cast<unsigned long long*>(carve(cur, 8));
+  w.visits = reinterpret_cast<unsigned long long*>(carve(cur, 16));
+  w.pass = reinterpret_cast<PassState*>(carve(cur, sizeof(PassState)));
+  if ((size_t)(cur - static_cast<unsigned char*>(base)) > kNoAllocScratchBytes) {
+    set_error("scratch layout exceeds the fixed array");
+    return ILLUME_ERR_INVALID;
+  }
+  w.cap = cap;
+  w.npix = cap;
+  w.width = p.width;
+  w.height = p.height;
+  Accumulators acc{};
+  acc.sum32 = d_sum;
+  RenderKnobs k{};
+  k.seed = p.seed;
+  k.job = p.job;
+  k.max_depth = p.max_depth;
+  k.ray_bias = p.ray_bias;
+  k.isect = p.intersector;
+  k.exact_hg = p.exact_hg;
+  k.bvh_kind = p.bvh_kind;
+  k.accum_mode = ILLUME_ACCUM_FP32;
+  const CameraView cam = make_camera(scene->s.host, p.width, p.height);
+  cudaStream_t st = ctx->c.stream;
+  const int sms = ctx->c.sm_count > 0 ? ctx->c.sm_count : 1;
+  const int grid_trace = kernel_grid_blocks(trace_kernel_ptr(p.bvh_kind), 128, dev);
+  const int grid_shade = kernel_grid_blocks(shade_kernel_ptr(), 128, dev);
+  const int grid_small = std::max(1, std::min((cap + 255) / 256, sms * 8));
+  k_noalloc_begin<<<grid_small, 256, 0, st>>>(w.counters, w.rays, w.visits, w.pass, d_sum, cap, p.sample_begin, p.spp);
+  for (int s = 0; s < p.spp; ++s) {
+    launch_raygen(w, cam, k, grid_small, st);
+    for (int b = 0; b < p.max_depth; ++b) {
+      launch_trace(w, scene->s.view, k, b, grid_trace, st);
+      launch_shade(w, scene->s.view, k, b, grid_shade, st);
+    }
+    launch_accumulate(w, acc, ILLUME_ACCUM_FP32, grid_small, st);
+    launch_advance_pass(w, st);
+  }
+  ILLUME_CUDA_TRY(cudaGetLastError());
+  ctx->c.launches += 1 + (long long)p.spp * (3 + 2 * p.max_depth);
+  return ILLUME_OK;
+}

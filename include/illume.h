@@ -238,6 +238,20 @@ typedef struct {
 } illume_profile;
 int illume_renderer_profile(illume_renderer* r, int count_visits, illume_profile* out);
 
+/* Render without allocating (no counterpart in the reference). For callers that cannot
+ * allocate device memory at render time: hosts whose own pool owns all device memory,
+ * and frame loops that must not stall on cudaMalloc/cudaFree. The wavefront queues live
+ * in a fixed array inside the library (about 12 MB, reserved on every GPU that loads the
+ * library until exit), which limits images to ILLUME_NOALLOC_MAX_PIXELS pixels; larger
+ * images are rejected with ILLUME_ERR_INVALID. Renders params->spp samples (one per
+ * pass, FP32 accumulation in sample order, accum_mode must be ILLUME_ACCUM_FP32) and
+ * writes the per-pixel sum of radiance (3 floats per pixel) to the caller's device
+ * buffer d_sum. Asynchronous on the context's stream. The first call on a device looks
+ * up the array's device address; make it before any stream capture. All calls share the
+ * array: calls whose GPU work overlaps race, so order them on one stream. */
+#define ILLUME_NOALLOC_MAX_PIXELS 65536
+int illume_render_noalloc(illume_context* ctx, illume_scene* scene, const illume_render_params* params, float* d_sum);
+
 /* ---- bitmap (src/bitmap.h:26-30) ---- */
 illume_bitmap* illume_bitmap_new(size_t width, size_t height);
 void illume_bitmap_free(illume_bitmap* bitmap);
