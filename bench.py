@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--bvh", default="wide", choices=["wide", "binary"])
     ap.add_argument("--spp-per-step", type=int, default=4)
+    ap.add_argument("--trace-variant", type=int, default=0,
+                    help="8-wide traversal: 0 persistent state machine, 1 one ray per lane to completion")
     ap.add_argument("--tris", type=int, default=100_000)
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--depth", type=int, default=25)
@@ -215,6 +217,7 @@ def run_ours(args):
     p.intersector = C.ISECT_WATERTIGHT
     p.accum_mode = C.ACCUM_FP32
     p.sample_begin = rank * 1_000_000
+    p.reserved[0] = args.trace_variant
     r = Renderer(ctx, scene, params=p)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")   # > 129 MB L2
 

@@ -102,7 +102,8 @@ int Renderer::init(std::string* err) {
   knobs.exact_hg = p.exact_hg;
   knobs.bvh_kind = p.bvh_kind;
   knobs.accum_mode = p.accum_mode;
-  grid_trace = kernel_grid_blocks(trace_kernel_ptr(p.bvh_kind), 128, ctx->device);
+  knobs.trace_variant = p.reserved[0];
+  grid_trace = kernel_grid_blocks(trace_kernel_ptr(p.bvh_kind, p.reserved[0]), 128, ctx->device);
   grid_shade = kernel_grid_blocks(shade_kernel_ptr(), 128, ctx->device);
   grid_raygen = std::max(1, std::min((cap + 255) / 256, ctx->sm_count * 8));
   grid_acc = std::max(1, std::min((npix + 255) / 256, ctx->sm_count * 8));

@@ -39,6 +39,7 @@ struct RenderKnobs {
   int max_depth;
   float ray_bias;
   int isect, exact_hg, bvh_kind, accum_mode;
+  int trace_variant;   // 8-wide BVH: 0 = persistent state machine, 1 = one ray per lane to completion
 };
 
 struct Accumulators {
@@ -66,7 +67,7 @@ void launch_trace_hook(const SceneView& sc, const float* rays8, int n, int isect
                        cudaStream_t st);
 void launch_bsdf_batch(int type, int distribution, const float* in, int n, float* out, cudaStream_t st);
 
-const void* trace_kernel_ptr(int bvh_kind);
+const void* trace_kernel_ptr(int bvh_kind, int variant = 0);
 const void* shade_kernel_ptr();
 
 }  // namespace illume

@@ -250,6 +250,108 @@ __device__ __forceinline__ void traverse_wide(const DevMesh& m, const TraceRay& 
   }
 }
 
+// ---- 8-wide BVH, one traversal step at a time (persistent state machine) ----
+//
+// A lane's traversal of one instance is a small state: the next node to fetch, one
+// pending triangle group (base + bit mask) and a stack of postponed node groups
+// (child base, inner mask, pending visit ranks) and triangle groups (flag bit 31). A
+// step either fetches one node (testing its 8 quantised child boxes) or tests one
+// triangle. The kernel chooses per warp which kind of step to run, so that the lanes of
+// a warp execute the same code path, and refills lanes that finished their ray.
+static constexpr uint32_t kNoNode = 0xffffffffu;
+static constexpr uint32_t kTriGroup = 0x80000000u;
+
+struct WideState {
+  uint32_t fetch;       // node to fetch next, kNoNode if none
+  uint32_t tri_base;    // pending triangle group
+  uint32_t tri_mask;
+  int sp;
+};
+
+__device__ __forceinline__ bool wide_has_node_work(const WideState& s) {
+  return s.fetch != kNoNode || (s.sp > 0 && s.tri_mask == 0);
+}
+__device__ __forceinline__ bool wide_done(const WideState& s) {
+  return s.fetch == kNoNode && s.tri_mask == 0 && s.sp == 0;
+}
+
+// One node step: pop if needed, then fetch and test a node.
+template <bool COUNT>
+__device__ __forceinline__ void wide_node_step(const DevMesh& m, const TraceRay& r, const MeshBest& best, WideState& s,
+                                               uint2* stack, VisitCount& vc) {
+  if (s.fetch == kNoNode) {
+    uint2& g = stack[s.sp - 1];
+    if (g.y & kTriGroup) {
+      s.tri_base = g.x;
+      s.tri_mask = g.y & ~kTriGroup;
+      --s.sp;
+      return;
+    }
+    uint32_t pend = g.y & 0xff;
+    const uint32_t im = (g.y >> 8) & 0xff;
+    const int k = __ffs(pend) - 1;
+    pend &= pend - 1;
+    s.fetch = g.x + __popc(im & ((1u << (k ^ r.oct)) - 1));
+    if (pend) g.y = (im << 8) | pend;
+    else --s.sp;
+  }
+  if (COUNT) vc.nodes++;
+  const float4* np = reinterpret_cast<const float4*>(m.wide + s.fetch);
+  const float4 q0 = __ldg(np), q1 = __ldg(np + 1), q2 = __ldg(np + 2), q3 = __ldg(np + 3), q4 = __ldg(np + 4);
+  const uint32_t ew = __float_as_uint(q0.w);
+  const uint32_t imask = ew >> 24;
+  const uint32_t child_base = __float_as_uint(q1.x), tri_base = __float_as_uint(q1.y);
+  const float sx = exp2i(ew & 0xff) * r.idir.x, sy = exp2i((ew >> 8) & 0xff) * r.idir.y,
+              sz = exp2i((ew >> 16) & 0xff) * r.idir.z;
+  const float bx = (q0.x - r.o.x) * r.idir.x, by = (q0.y - r.o.y) * r.idir.y, bz = (q0.z - r.o.z) * r.idir.z;
+  const float tlim = best.t * kExitSlack;
+  uint32_t pending = 0, tmask = 0;
+#pragma unroll
+  for (int s8 = 0; s8 < 8; ++s8) {
+    const int w = s8 >> 2, sh = (s8 & 3) * 8;
+    const uint32_t me = (__float_as_uint(w ? q1.w : q1.z) >> sh) & 0xff;
+    const bool inner = (imask >> s8) & 1;
+    const float lx = (float)((__float_as_uint(w ? q2.y : q2.x) >> sh) & 0xff);
+    const float ly = (float)((__float_as_uint(w ? q2.w : q2.z) >> sh) & 0xff);
+    const float lz = (float)((__float_as_uint(w ? q3.y : q3.x) >> sh) & 0xff);
+    const float hx = (float)((__float_as_uint(w ? q3.w : q3.z) >> sh) & 0xff);
+    const float hy = (float)((__float_as_uint(w ? q4.y : q4.x) >> sh) & 0xff);
+    const float hz = (float)((__float_as_uint(w ? q4.w : q4.z) >> sh) & 0xff);
+    const float nx = r.idir.x >= 0.0f ? lx : hx, fx = r.idir.x >= 0.0f ? hx : lx;
+    const float ny = r.idir.y >= 0.0f ? ly : hy, fy = r.idir.y >= 0.0f ? hy : ly;
+    const float nz = r.idir.z >= 0.0f ? lz : hz, fz = r.idir.z >= 0.0f ? hz : lz;
+    const float t0 = fmaxf(fmaxf(__fmaf_rn(nx, sx, bx), __fmaf_rn(ny, sy, by)), fmaxf(__fmaf_rn(nz, sz, bz), 0.0f));
+    const float t1 = fminf(fminf(__fmaf_rn(fx, sx, bx), __fmaf_rn(fy, sy, by)), __fmaf_rn(fz, sz, bz)) * kExitSlack;
+    const bool hit = (inner || me != 0) && t0 <= t1 && t0 <= tlim;
+    if (hit) {
+      if (inner) pending |= 1u << (s8 ^ r.oct);
+      else tmask |= ((1u << (me >> 5)) - 1u) << (me & 31);
+    }
+  }
+  if (tmask) {
+    if (s.tri_mask && s.sp < kStack) stack[s.sp++] = make_uint2(s.tri_base, s.tri_mask | kTriGroup);
+    s.tri_base = tri_base;
+    s.tri_mask = tmask;
+  }
+  if (pending) {
+    const int k = __ffs(pending) - 1;
+    pending &= pending - 1;
+    s.fetch = child_base + __popc(imask & ((1u << (k ^ r.oct)) - 1));
+    if (pending && s.sp < kStack) stack[s.sp++] = make_uint2(child_base, (imask << 8) | pending);
+  } else {
+    s.fetch = kNoNode;
+  }
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
+                                              WideState& s, VisitCount& vc) {
+  const int k = __ffs(s.tri_mask) - 1;
+  s.tri_mask &= s.tri_mask - 1;
+  if (COUNT) vc.tris++;
+  test_triangle(m.wide_tris + 3 * (s.tri_base + k), isect, r, best);
+}
+
 // Full closest-hit query for a world-space ray (direction used as given).
 template <int KIND, bool COUNT = false>
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,

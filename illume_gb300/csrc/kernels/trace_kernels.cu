@@ -78,6 +78,159 @@ __global__ void __launch_bounds__(128) k_trace(WaveBuffers w, SceneView sc, Rend
   }
 }
 
+// Persistent trace kernel for the 8-wide BVH. Each lane owns one ray at a time and walks
+// it through a small state machine (spheres at load, then per instance: box cull, object
+// ray set-up, traversal steps); every loop iteration runs one traversal step per lane,
+// with the kind of step (node fetch or triangle test) chosen per warp by a vote, and a
+// lane whose ray is finished takes its next ray at once (rays are assigned statically:
+// lane i handles rays i, i + stride, ...). HOOK = test-hook variant (rays and illume_hit
+// records in caller buffers).
+enum { PH_IDLE = 0, PH_INST = 1, PH_TRAV = 2, PH_DONE = 3 };
+
+template <bool COUNT, bool HOOK>
+__global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, SceneView sc, RenderKnobs k, int bounce,
+                                                  const float4* hook_rays, int hook_n, illume_hit* hook_out) {
+  const unsigned FULL = 0xffffffffu;
+  const int parity = bounce & 1;
+  const int n = HOOK ? hook_n : w.counters[parity];
+  if (!HOOK && blockIdx.x == 0 && threadIdx.x == 0) w.counters[parity ^ 1] = 0;
+  int* counts = HOOK ? nullptr : ev_counts(w, parity);
+  const int sample_base = HOOK ? 0 : w.pass->sample_base;
+  const int stride = gridDim.x * blockDim.x;
+  int next = blockIdx.x * blockDim.x + threadIdx.x;
+  uint2 stack[kStack];
+  int slot = -1, phase = PH_IDLE, inst = 0, pid = 0, medium = -1, steps = 0;
+  V3 o = v3(0.0f, 0.0f, 0.0f), d = v3(0.0f, 0.0f, 1.0f);
+  HitRecord h;
+  h.t = FLT_MAX; h.u = h.v = 0.0f; h.prim = -1; h.geom = -1;
+  TraceRay r;
+  MeshBest b{FLT_MAX, -1, 0.0f, 0.0f};
+  WideState s{kNoNode, 0u, 0u, 0};
+  VisitCount vc;
+  TraceRay wr;
+  for (;;) {
+    if (phase == PH_IDLE && next < n) {
+      slot = next;
+      next += stride;
+      if (HOOK) {
+        const float4 a = hook_rays[2 * slot], c = hook_rays[2 * slot + 1];
+        o = v3(a.x, a.y, a.z);
+        d = v3(c.x, c.y, c.z);
+      } else {
+        const float4 qo = w.q_orig[parity][slot], qd = w.q_dir[parity][slot];
+        o = v3(qo.x, qo.y, qo.z);
+        d = v3(qd.x, qd.y, qd.z);
+        pid = __float_as_int(qo.w);
+        medium = __float_as_int(qd.w);
+      }
+      h.t = FLT_MAX; h.u = h.v = 0.0f; h.prim = -1; h.geom = -1;
+      for (int sidx = 0; sidx < sc.num_spheres; ++sidx) {
+        const DevSphere sp = sc.spheres[sidx];
+        const V3 l = sub(v3(sp.cx, sp.cy, sp.cz), o);
+        const float sd = dot(l, d), ls = dot(l, l), rs = sp.r * sp.r;
+        if (sd < 0.0f && ls > rs) continue;
+        const float ms = ls - sd * sd;
+        if (ms > rs) continue;
+        const float q = sqrtf(rs - ms);
+        const float t = ls > rs ? sd - q : sd + q;
+        if (t < h.t) { h.t = t; h.geom = -2 - sidx; h.prim = -1; }
+      }
+      wr.o = o;
+      wr.d = d;
+      wr.idir = v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+      inst = 0;
+      phase = PH_INST;
+    }
+    if (__all_sync(FULL, phase == PH_IDLE)) break;
+    if (phase == PH_INST) {
+      while (inst < sc.num_instances) {
+        const DevInstance& in = sc.instances[inst];
+        float te;
+        if (box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) {
+          setup_ray(r, xform(in.inv, o, 1.0f), xform(in.inv, d, 0.0f), k.isect);
+          b = MeshBest{h.t, -1, 0.0f, 0.0f};
+          s = WideState{0u, 0u, 0u, 0};
+          steps = 0;
+          phase = PH_TRAV;
+          break;
+        }
+        ++inst;
+      }
+      if (phase == PH_INST) phase = PH_DONE;
+    }
+    const bool trav = phase == PH_TRAV;
+    const bool has_tri = trav && s.tri_mask != 0;
+    const bool has_node = trav && wide_has_node_work(s);
+    const unsigned want_tri = __ballot_sync(FULL, has_tri);
+    const unsigned want_node = __ballot_sync(FULL, has_node);
+    if (want_tri | want_node) {
+      const bool do_tri = __popc(want_tri) >= __popc(want_node);
+      if (trav) {
+        const DevMesh& m = sc.meshes[sc.instances[inst].mesh];
+        if (do_tri) {
+          if (has_tri) wide_tri_step<COUNT>(m, r, k.isect, b, s, vc);
+        } else if (has_node) {
+          wide_node_step<COUNT>(m, r, b, s, stack, vc);
+        }
+      }
+    }
+    if (trav) {
+      if (++steps > kMaxNodeVisits) s = WideState{kNoNode, 0u, 0u, 0};
+      if (wide_done(s)) {
+        if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = inst; }
+        ++inst;
+        phase = PH_INST;
+      }
+    }
+    const unsigned fin = __ballot_sync(FULL, phase == PH_DONE);
+    if (phase == PH_DONE) {
+      if (HOOK) {
+        illume_hit out;
+        out.t = h.t;
+        out.u = h.geom >= 0 ? h.u : 0.0f;
+        out.v = h.geom >= 0 ? h.v : 0.0f;
+        out.inst = h.geom >= 0 ? h.geom : -1;
+        out.prim = h.geom >= 0 ? h.prim : -1;
+        out.sphere = h.geom <= -2 ? -2 - h.geom : -1;
+        out.pad[0] = out.pad[1] = 0;
+        hook_out[slot] = out;
+      } else {
+        int cls;
+        bool scattered = false;
+        if (medium >= 0 && sc.mediums[medium].active) {
+          const uint32_t pixel = (uint32_t)(pid % w.npix), sample = (uint32_t)(sample_base + pid / w.npix);
+          const Philox4 rr = philox4x32_10(pixel, sample, (uint32_t)(bounce + 1), 0u, k.seed, k.job);
+          const float dist = -logf(philox_unit(rr.x)) / sc.mediums[medium].scattering;
+          scattered = dist < h.t;
+        }
+        if (scattered) cls = EV_MEDIUM;
+        else if (h.geom == -1) cls = EV_MISS;
+        else {
+          const int mat = h.geom >= 0 ? sc.instances[h.geom].material : sc.spheres[-2 - h.geom].material;
+          cls = EV_SURFACE + sc.materials[mat].type;
+        }
+        w.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
+        w.hit_geom[slot] = h.geom;
+        const int pos = warp_append_keyed(fin, cls, counts);
+        w.evq[(size_t)cls * w.cap + pos] = slot;
+      }
+      phase = PH_IDLE;
+      slot = -1;
+    }
+  }
+  if (COUNT) {
+    unsigned long long my_nodes = vc.nodes, my_tris = vc.tris;
+    for (int off = 16; off > 0; off >>= 1) {
+      my_nodes += __shfl_down_sync(FULL, my_nodes, off);
+      my_tris += __shfl_down_sync(FULL, my_tris, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(w.visits, my_nodes);
+      atomicAdd(w.visits + 1, my_tris);
+    }
+  }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* rays, int n, int isect,
                                                     illume_hit* out) {
@@ -97,12 +250,19 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
   }
 }
 
-const void* trace_kernel_ptr(int bvh_kind) {
-  return bvh_kind == BVH_WIDE8 ? (const void*)k_trace<BVH_WIDE8, false> : (const void*)k_trace<BVH_BINARY, false>;
+const void* trace_kernel_ptr(int bvh_kind, int variant) {
+  if (bvh_kind == BVH_WIDE8)
+    return variant == 0 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
+  return (const void*)k_trace<BVH_BINARY, false>;
 }
 
 void launch_trace(const WaveBuffers& w, const SceneView& sc, const RenderKnobs& k, int bounce, int grid,
                   cudaStream_t st, bool count_visits) {
+  if (k.bvh_kind == BVH_WIDE8 && k.trace_variant == 0) {
+    if (count_visits) k_trace_sm<true, false><<<grid, 128, 0, st>>>(w, sc, k, bounce, nullptr, 0, nullptr);
+    else k_trace_sm<false, false><<<grid, 128, 0, st>>>(w, sc, k, bounce, nullptr, 0, nullptr);
+    return;
+  }
   if (count_visits) {
     if (k.bvh_kind == BVH_WIDE8) k_trace<BVH_WIDE8, true><<<grid, 128, 0, st>>>(w, sc, k, bounce);
     else k_trace<BVH_BINARY, true><<<grid, 128, 0, st>>>(w, sc, k, bounce);
@@ -115,11 +275,20 @@ void launch_trace(const WaveBuffers& w, const SceneView& sc, const RenderKnobs& 
 void launch_trace_hook(const SceneView& sc, const float* rays8, int n, int isect, int bvh_kind, void* hits,
                        cudaStream_t st) {
   if (n <= 0) return;
+  if (bvh_kind == BVH_WIDE8) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int cap = kernel_grid_blocks((const void*)k_trace_sm<false, true>, 128, dev);
+    const int grid = std::max(1, std::min(cap, (n + 127) / 128));
+    WaveBuffers w{};
+    RenderKnobs k{};
+    k.isect = isect;
+    k.bvh_kind = BVH_WIDE8;
+    k_trace_sm<false, true><<<grid, 128, 0, st>>>(w, sc, k, 0, (const float4*)rays8, n, (illume_hit*)hits);
+    return;
+  }
   const int grid = (n + 127) / 128;
-  if (bvh_kind == BVH_WIDE8)
-    k_trace_hook<BVH_WIDE8><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);
-  else
-    k_trace_hook<BVH_BINARY><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);
+  k_trace_hook<BVH_BINARY><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);
 }
 
 int kernel_grid_blocks(const void* fn, int block, int device) {
