@@ -48,10 +48,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--bvh", default="wide", choices=["wide", "binary"])
+    ap.add_argument("--bvh", default="binary", choices=["binary", "wide", "wide-persistent"])
     ap.add_argument("--spp-per-step", type=int, default=4)
     ap.add_argument("--trace-variant", type=int, default=0,
-                    help="8-wide traversal: 0 persistent state machine, 1 one ray per lane to completion")
+                    help="binary traversal: 0 compiler register choice, 1 at most 64 registers")
     ap.add_argument("--tris", type=int, default=100_000)
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--depth", type=int, default=25)
@@ -213,7 +213,7 @@ def run_ours(args):
     p = scene.default_params(args.spp_per_step, args.depth)
     p.width = p.height = args.res
     p.samples_per_pass = args.spp_per_step
-    p.bvh_kind = C.BVH_WIDE8 if args.bvh == "wide" else C.BVH_BINARY
+    p.bvh_kind = {"binary": C.BVH_BINARY, "wide": C.BVH_WIDE8, "wide-persistent": C.BVH_WIDE8_PERSISTENT}[args.bvh]
     p.intersector = C.ISECT_WATERTIGHT
     p.accum_mode = C.ACCUM_FP32
     p.sample_begin = rank * 1_000_000

@@ -26,14 +26,14 @@ int main(int argc, char** argv) {
   const int spp = (int)strtol(argv[3], nullptr, 10);
   const int max_depth = (int)strtol(argv[4], nullptr, 10);
   uint32_t seed = 0;
-  int accum = ILLUME_ACCUM_FP32, bvh = ILLUME_BVH_WIDE8, isect = ILLUME_ISECT_WATERTIGHT;
+  int accum = ILLUME_ACCUM_FP32, bvh = ILLUME_BVH_BINARY, isect = ILLUME_ISECT_WATERTIGHT;
   bool pfm = false;
   for (int i = 5; i < argc; ++i) {
     const std::string a = argv[i];
     const char* v = i + 1 < argc ? argv[i + 1] : "";
     if (a == "--seed") { seed = (uint32_t)strtoul(v, nullptr, 10); ++i; }
     else if (a == "--accum") { accum = !strcmp(v, "fp64") ? ILLUME_ACCUM_FP64 : !strcmp(v, "kahan") ? ILLUME_ACCUM_KAHAN : ILLUME_ACCUM_FP32; ++i; }
-    else if (a == "--bvh") { bvh = !strcmp(v, "binary") ? ILLUME_BVH_BINARY : ILLUME_BVH_WIDE8; ++i; }
+    else if (a == "--bvh") { bvh = !strcmp(v, "wide") ? ILLUME_BVH_WIDE8 : ILLUME_BVH_BINARY; ++i; }
     else if (a == "--isect") { isect = !strcmp(v, "mt") ? ILLUME_ISECT_MT : ILLUME_ISECT_WATERTIGHT; ++i; }
     else if (a == "--pfm") { pfm = true; }
   }

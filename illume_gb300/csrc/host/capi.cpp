@@ -178,7 +178,7 @@ int illume_render_params_default(const illume_scene* scene, int spp, int max_dep
   out->job = 0;
   out->accum_mode = ILLUME_ACCUM_FP32;
   out->intersector = ILLUME_ISECT_WATERTIGHT;
-  out->bvh_kind = ILLUME_BVH_WIDE8;
+  out->bvh_kind = ILLUME_BVH_BINARY;
   out->exact_hg = 0;
   out->samples_per_pass = 0;
   return ILLUME_OK;
@@ -307,7 +307,8 @@ int illume_trace_closest_device(illume_context* ctx, illume_scene* scene, const 
                                 int bvh_kind, illume_hit* d_hits) {
   CHECK_ARG(ctx && scene && (n == 0 || (d_rays && d_hits)) && n >= 0, "bad argument");
   CHECK_ARG(intersector == ILLUME_ISECT_MT || intersector == ILLUME_ISECT_WATERTIGHT, "unknown intersector");
-  CHECK_ARG(bvh_kind == ILLUME_BVH_BINARY || bvh_kind == ILLUME_BVH_WIDE8, "unknown BVH kind");
+  CHECK_ARG(bvh_kind == ILLUME_BVH_BINARY || bvh_kind == ILLUME_BVH_WIDE8 || bvh_kind == ILLUME_BVH_WIDE8_PERSISTENT,
+            "unknown BVH kind");
   CHECK_ARG(((uintptr_t)d_rays & 15) == 0, "rays must be 16-byte aligned");
   CHECK_ARG(scene->s.ctx == &ctx->c, "scene was not uploaded with this context");
   cudaSetDevice(ctx->c.device);

@@ -43,7 +43,7 @@ int Renderer::init(std::string* err) {
   if (p.width <= 0 || p.height <= 0 || p.spp < 0 || p.max_depth < 0) { *err = "invalid render size, spp or depth"; return ILLUME_ERR_INVALID; }
   if ((long long)p.width * p.height > (1LL << 28)) { *err = "image too large"; return ILLUME_ERR_INVALID; }
   if (p.intersector != ISECT_MT && p.intersector != ISECT_WATERTIGHT) { *err = "unknown intersector"; return ILLUME_ERR_INVALID; }
-  if (p.bvh_kind != BVH_BINARY && p.bvh_kind != BVH_WIDE8) { *err = "unknown BVH kind"; return ILLUME_ERR_INVALID; }
+  if (p.bvh_kind < BVH_BINARY || p.bvh_kind > 2) { *err = "unknown BVH kind"; return ILLUME_ERR_INVALID; }
   if (p.accum_mode < ACCUM_FP32 || p.accum_mode > ACCUM_FP64) { *err = "unknown accumulation mode"; return ILLUME_ERR_INVALID; }
   npix = p.width * p.height;
   const long long target = 1LL << 22;  // paths in flight per pass
@@ -100,10 +100,10 @@ int Renderer::init(std::string* err) {
   knobs.ray_bias = p.ray_bias;
   knobs.isect = p.intersector;
   knobs.exact_hg = p.exact_hg;
-  knobs.bvh_kind = p.bvh_kind;
+  knobs.bvh_kind = p.bvh_kind == 2 ? BVH_WIDE8 : p.bvh_kind;
   knobs.accum_mode = p.accum_mode;
-  knobs.trace_variant = p.reserved[0];
-  grid_trace = kernel_grid_blocks(trace_kernel_ptr(p.bvh_kind, p.reserved[0]), 128, ctx->device);
+  knobs.trace_variant = p.bvh_kind == 2 ? 1 : (p.bvh_kind == BVH_BINARY ? p.reserved[0] : 0);
+  grid_trace = kernel_grid_blocks(trace_kernel_ptr(knobs.bvh_kind, knobs.trace_variant), 128, ctx->device);
   grid_shade = kernel_grid_blocks(shade_kernel_ptr(), 128, ctx->device);
   grid_raygen = std::max(1, std::min((cap + 255) / 256, ctx->sm_count * 8));
   grid_acc = std::max(1, std::min((npix + 255) / 256, ctx->sm_count * 8));
@@ -231,7 +231,7 @@ int Renderer::profile(bool count_visits, illume_profile* out) {
   out->rays = (int64_t)(rays_after - rays_before);
   out->node_fetches = (int64_t)vis[0];
   out->tri_tests = (int64_t)vis[1];
-  out->node_bytes = p.bvh_kind == BVH_WIDE8 ? (int64_t)sizeof(WideNode) : (int64_t)sizeof(Bvh2Node);
+  out->node_bytes = knobs.bvh_kind == BVH_WIDE8 ? (int64_t)sizeof(WideNode) : (int64_t)sizeof(Bvh2Node);
   out->tri_bytes = 3 * (int64_t)sizeof(float4);
   for (auto& e : ev) cudaEventDestroy(e);
   samples_done += per_pass;

@@ -25,8 +25,8 @@ __device__ __forceinline__ int warp_append_keyed(unsigned mask, int key, int* co
 // (escape, medium scatter before the surface, or the hit material) and an append of the
 // ray's slot to that class's queue. The medium decision uses the first number of the
 // path's bounce stream, as src/renderer.cu:152-157 does.
-template <int KIND, bool COUNT>
-__global__ void __launch_bounds__(128) k_trace(WaveBuffers w, SceneView sc, RenderKnobs k, int bounce) {
+template <int KIND, bool COUNT, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, SceneView sc, RenderKnobs k, int bounce) {
   const int parity = bounce & 1;
   const int n = w.counters[parity];
   if (blockIdx.x == 0 && threadIdx.x == 0) w.counters[parity ^ 1] = 0;
@@ -250,32 +250,40 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
   }
 }
 
+// Trace kernel variants (RenderKnobs::trace_variant):
+//   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine;
+//   binary BVH: 0 = compiler's register choice, 1 = at most 64 registers (8 blocks per SM).
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (bvh_kind == BVH_WIDE8)
-    return variant == 0 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
-  return (const void*)k_trace<BVH_BINARY, false>;
+    return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
+  return variant == 1 ? (const void*)k_trace<BVH_BINARY, false, 8> : (const void*)k_trace<BVH_BINARY, false>;
 }
 
 void launch_trace(const WaveBuffers& w, const SceneView& sc, const RenderKnobs& k, int bounce, int grid,
                   cudaStream_t st, bool count_visits) {
-  if (k.bvh_kind == BVH_WIDE8 && k.trace_variant == 0) {
-    if (count_visits) k_trace_sm<true, false><<<grid, 128, 0, st>>>(w, sc, k, bounce, nullptr, 0, nullptr);
-    else k_trace_sm<false, false><<<grid, 128, 0, st>>>(w, sc, k, bounce, nullptr, 0, nullptr);
+  if (k.bvh_kind == BVH_WIDE8) {
+    if (k.trace_variant == 1) {
+      if (count_visits) k_trace_sm<true, false><<<grid, 128, 0, st>>>(w, sc, k, bounce, nullptr, 0, nullptr);
+      else k_trace_sm<false, false><<<grid, 128, 0, st>>>(w, sc, k, bounce, nullptr, 0, nullptr);
+    } else {
+      if (count_visits) k_trace<BVH_WIDE8, true><<<grid, 128, 0, st>>>(w, sc, k, bounce);
+      else k_trace<BVH_WIDE8, false><<<grid, 128, 0, st>>>(w, sc, k, bounce);
+    }
     return;
   }
-  if (count_visits) {
-    if (k.bvh_kind == BVH_WIDE8) k_trace<BVH_WIDE8, true><<<grid, 128, 0, st>>>(w, sc, k, bounce);
-    else k_trace<BVH_BINARY, true><<<grid, 128, 0, st>>>(w, sc, k, bounce);
+  if (k.trace_variant == 1) {
+    if (count_visits) k_trace<BVH_BINARY, true, 8><<<grid, 128, 0, st>>>(w, sc, k, bounce);
+    else k_trace<BVH_BINARY, false, 8><<<grid, 128, 0, st>>>(w, sc, k, bounce);
     return;
   }
-  if (k.bvh_kind == BVH_WIDE8) k_trace<BVH_WIDE8, false><<<grid, 128, 0, st>>>(w, sc, k, bounce);
+  if (count_visits) k_trace<BVH_BINARY, true><<<grid, 128, 0, st>>>(w, sc, k, bounce);
   else k_trace<BVH_BINARY, false><<<grid, 128, 0, st>>>(w, sc, k, bounce);
 }
 
 void launch_trace_hook(const SceneView& sc, const float* rays8, int n, int isect, int bvh_kind, void* hits,
                        cudaStream_t st) {
   if (n <= 0) return;
-  if (bvh_kind == BVH_WIDE8) {
+  if (bvh_kind == 2) {  // 8-wide BVH through the persistent state machine (internal test path)
     int dev = 0;
     cudaGetDevice(&dev);
     const int cap = kernel_grid_blocks((const void*)k_trace_sm<false, true>, 128, dev);
@@ -288,7 +296,10 @@ void launch_trace_hook(const SceneView& sc, const float* rays8, int n, int isect
     return;
   }
   const int grid = (n + 127) / 128;
-  k_trace_hook<BVH_BINARY><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);
+  if (bvh_kind == BVH_WIDE8)
+    k_trace_hook<BVH_WIDE8><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);
+  else
+    k_trace_hook<BVH_BINARY><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);
 }
 
 int kernel_grid_blocks(const void* fn, int block, int device) {

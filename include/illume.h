@@ -53,7 +53,10 @@ enum illume_texture_type { ILLUME_TEX_CONSTANT = 0, ILLUME_TEX_CHECKERBOARD = 1,
 enum illume_distribution { ILLUME_DIST_BECKMANN = 0, ILLUME_DIST_GGX = 1 };
 enum illume_tonemapper { ILLUME_TONE_LINEAR = 0, ILLUME_TONE_REINHARD = 1, ILLUME_TONE_FILMIC = 2, ILLUME_TONE_UNCHARTED = 3 }; /* src/tonemapper.h:10-13 */
 enum illume_intersector { ILLUME_ISECT_MT = 0, ILLUME_ISECT_WATERTIGHT = 1 };
-enum illume_bvh_kind { ILLUME_BVH_BINARY = 0, ILLUME_BVH_WIDE8 = 1 };
+/* BINARY: 64-byte nodes holding both child boxes (the default). WIDE8: 80-byte 8-wide nodes
+ * with 8-bit quantised child boxes. WIDE8_PERSISTENT: the same nodes traversed by a
+ * persistent kernel that schedules node and triangle steps per warp. */
+enum illume_bvh_kind { ILLUME_BVH_BINARY = 0, ILLUME_BVH_WIDE8 = 1, ILLUME_BVH_WIDE8_PERSISTENT = 2 };
 enum illume_accum_mode { ILLUME_ACCUM_FP32 = 0, ILLUME_ACCUM_KAHAN = 1, ILLUME_ACCUM_FP64 = 2 };
 
 /* ---- reference output types: same layout as src/bitmap.h:6-20 ---- */

@@ -2,9 +2,11 @@
 the oracle: FP32 GPU vs FP32 oracle (same arithmetic), and FP32 GPU vs the FP64 oracle
 within 1e-5 relative on well-conditioned inputs.
 
-Well conditioned: |wi.n| >= 0.05, every Fresnel/probability decision more than 1e-4
-from its threshold, and the kill test (wi.n)(wo.n) more than 1e-4 from zero; values
-are compared relative to max(|ref|, 1e-3) (unit-vector components absolutely).
+Decisions: |wi.n| >= 0.05, every Fresnel/probability decision more than 1e-4 from its
+threshold, and the kill test (wi.n)(wo.n) more than 1e-4 from zero: statuses must equal
+FP64's and directions be within 1e-5. Values (weight, D, pdf, G, F, eval): within 1e-5
+relative (to max(|ref|, 1e-3)) on >= 99.5% of the tuples whose FP64 values move by less
+than 4e-6 under a 4-ulp perturbation of the inputs, and within 5e-5 on all of them.
 """
 import numpy as np
 import pytest
@@ -71,15 +73,20 @@ def test_bsdf_against_oracle(ctx, mat, dist):
     live = ok & (f64[:, 12] > 0)
     d = np.abs(got[live, 0:3] - f64[live, 0:3])
     assert d.max() < 1e-5, d.max()
-    # values (weight, D, pdf_m, G, F, eval, pdf): within 1e-5 relative of FP64, except where
-    # the reference's own FP32 formulation (the FP32 oracle, glibc libm) is further off;
-    # there the GPU (CUDA libm, rounding differently) may differ from FP64 by at most 8x
-    # the formulation's error
+    # values (weight, D, pdf_m, G, F, eval, pdf) within 1e-5 relative of FP64 wherever the
+    # values are stable under a 4-ulp perturbation of the inputs (an FP32 evaluation
+    # cannot be more accurate than its inputs allow: near m = n the reference's
+    # (cos^2 - 1) / cos^2 amplifies an ulp of m by orders of magnitude)
     vals = [3, 4, 5, 6, 7, 8, 9, 10, 11]
-    ref = np.maximum(np.abs(f64[live][:, vals]), 1e-3)
-    rel_gpu = np.abs(got[live][:, vals] - f64[live][:, vals]) / ref
-    rel_f32 = np.abs(f32[live][:, vals] - f64[live][:, vals]) / ref
-    bound = np.maximum(1e-5, 8.0 * rel_f32 + 1e-6)
-    assert (rel_gpu <= bound).all(), (rel_gpu / bound).max(0)
-    frac = (rel_gpu < 1e-5).all(1).mean()
-    assert frac >= 0.85, frac
+    xp = x.copy()
+    xp[:, 0:6] *= np.float32(1.0 - 4.0 * 2.0 ** -24)
+    xp[:, 6:9] *= np.float32(1.0 - 4.0 * 2.0 ** -24)
+    f64p = pyoracle.bsdf_batch(mat, dist, xp, precision=64)
+    ref = np.maximum(np.abs(f64[:, vals]), 1e-3)
+    sens = (np.abs(f64p[:, vals] - f64[:, vals]) / ref).max(1)
+    stable = live & (sens < 4e-6) & (f64p[:, 12] == f64[:, 12])
+    assert stable.sum() >= 0.3 * live.sum(), (stable.sum(), live.sum())
+    rel_gpu = (np.abs(got[stable][:, vals] - f64[stable][:, vals]) / ref[stable]).max(1)
+    # the FP32 formulation itself (FP32 oracle) leaves a small tail above 1e-5 on these
+    assert (rel_gpu < 1e-5).mean() >= 0.995, (rel_gpu < 1e-5).mean()
+    assert rel_gpu.max() < 5e-5, rel_gpu.max()
