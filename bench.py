@@ -5,7 +5,7 @@ Workload (the configuration the headline metric is quoted on): displaced icosphe
 ~100k triangles (rough gold conductor, GGX alpha 0.2) over a checkerboard ground quad,
 2048x1024 HDR environment map with a sun lobe, 1024x1024 pixels, max depth 25, seeded
 synthetic data. One step = one wavefront pass of `--spp-per-step` samples of every pixel
-(4 by default, i.e. 4M paths); a full 1024-spp render is 256 such steps.
+(16 by default, i.e. 16M paths); a full 1024-spp render is 64 such steps.
 
 * value: rays traced (closest-hit queries, counted as the reference counts them) per
   second of device time, inputs resident in HBM, L2 flushed between timed steps.
@@ -45,16 +45,25 @@ WORKLOAD = "triangle-heavy traversal: displaced icosphere 100k tris, GGX rough g
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=64)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--bvh", default="binary", choices=["binary", "wide", "wide-persistent"])
-    ap.add_argument("--spp-per-step", type=int, default=4)
+    ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--trace-variant", type=int, default=0,
-                    help="binary traversal: 0 compiler register choice, 1 at most 64 registers")
+                    help="binary traversal: 0 at most 64 registers (8 blocks per SM), 1 compiler register choice")
     ap.add_argument("--tris", type=int, default=100_000)
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--depth", type=int, default=25)
+    ap.add_argument("--workload", default="traversal", choices=["traversal", "batched", "served"],
+                    help="traversal: the headline single-render workload; batched: 64 uneven jobs in one job "
+                         "table vs one job at a time; served: Poisson request stream, continuous batching vs "
+                         "one request at a time")
+    ap.add_argument("--jobs", type=int, default=64)
+    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--plain-1spp", action="store_true",
+                    help="batched: also time one job at a time with one sample per pass")
+    ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -82,7 +91,7 @@ class Clocks:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -333,10 +342,233 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def _job_params(scene, d, C, camera=None):
+    p = scene.default_params(d["spp"], d["max_depth"])
+    p.width, p.height = d["width"], d["height"]
+    p.seed, p.job = d.get("seed", 0), d["job"]
+    p.intersector = C.ISECT_WATERTIGHT
+    p.bvh_kind = C.BVH_BINARY
+    p.accum_mode = C.ACCUM_FP32
+    if camera is not None:
+        p.camera = C.fptr(camera)
+    return p
+
+
+def _upload_all(ctx, datas):
+    from illume_gb300.api import HostScene
+    return [HostScene.from_data(ctx, sd) for sd in datas]
+
+
+def run_batched(args):
+    """64 uneven jobs: one job at a time through the plain renderer versus all jobs in one
+    job table (illume_render_batch: continuous admission, slots shared between jobs,
+    autotuned slot count and trace kernel). Scenes are resident before timing; each arm's
+    images are compared bit for bit."""
+    import torch
+    import numpy as np
+    from illume_gb300 import _capi as C
+    from illume_gb300 import synth
+    from illume_gb300.api import Context, Renderer, render_batch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    t_gen = time.perf_counter()
+    pool = synth.MeshPool(seed=2)
+    jobs = synth.batch_jobs(args.jobs, seed=2, pool=pool)
+    ctx = Context(local)
+    scenes = _upload_all(ctx, [sd for sd, _ in jobs])
+    params = [_job_params(sc, d, C) for sc, (_, d) in zip(scenes, jobs)]
+    gen_s = time.perf_counter() - t_gen
+    paths = sum(p.width * p.height * p.spp for p in params)
+    tris = [sd.num_triangles() for sd, _ in jobs]
+
+    def plain(spp_per_pass):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rays, dev_ms, launches, means = 0, 0.0, 0, []
+        for sc, p in zip(scenes, params):
+            q = C.RenderParams.from_buffer_copy(p)
+            q.samples_per_pass = spp_per_pass
+            r = Renderer(ctx, sc, params=q)
+            st = r.render_device()
+            means.append(r.read(mean=True)["mean"])
+            r.close()
+            rays += st.rays
+            dev_ms += st.render_ms
+            launches += st.kernel_launches
+        wall = time.perf_counter() - t0
+        return dict(rays=rays, device_ms=dev_ms, wall_s=wall, launches=launches, means=means)
+
+    # warm-up: one small job through each path
+    small = int(np.argmin([p.width * p.height * p.spp for p in params]))
+    render_batch(ctx, [scenes[small]], [params[small]])
+    clocks = Clocks(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    means_b, _, jstats, bs = render_batch(ctx, scenes, params, autotune=bool(args.autotune))
+    torch.cuda.synchronize()
+    wall_b = time.perf_counter() - t0
+    clk = clocks.stop()
+    rays_b = sum(j.rays for j in jstats)
+    pl = plain(0)
+    pl1 = plain(1) if args.plain_1spp else None
+    same = all(np.array_equal(a, b) for a, b in zip(means_b, pl["means"]))
+    if pl1 is not None:
+        same = same and all(np.array_equal(a, b) for a, b in zip(means_b, pl1["means"]))
+    batched_dev = rays_b / (bs.device_ms * 1e-3) / 1e6
+    batched_wall = rays_b / wall_b / 1e6
+    plain_dev = pl["rays"] / (pl["device_ms"] * 1e-3) / 1e6
+    plain_wall = pl["rays"] / pl["wall_s"] / 1e6
+    line = {
+        "metric": METRIC, "value": round(batched_dev, 3), "unit": "Mrays/s", "n_gpus": 1, "steps": int(bs.passes),
+        "warmup": 1, "ms_per_step": round(bs.device_ms / max(bs.passes, 1), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched uneven jobs: {args.jobs} jobs, resolution U{{128,256,512,1024}}^2, spp "
+                               "U[64,1024], 1-8 displaced icospheres (5k-700k tris, 16-mesh pool) with random "
+                               "affine transforms, mixed materials, 2048x1024 env, depth 15",
+                   "mode": "one job table (continuous admission, shared path slots) vs one job at a time",
+                   "paths": int(paths), "triangles_per_job_min_max": [min(tris), max(tris)],
+                   "scene_gen_upload_s": round(gen_s, 1), "autotune": bool(args.autotune),
+                   "chosen_path_slots": int(bs.path_capacity), "chosen_trace_variant": int(bs.trace_variant),
+                   "l2": "inputs larger than L2 (scenes ~GBs)"},
+        "batched": {"mrays_device": round(batched_dev, 2), "mrays_wall": round(batched_wall, 2), "rays": int(rays_b),
+                    "device_s": round(bs.device_ms * 1e-3, 3), "wall_s": round(wall_b, 3), "passes": int(bs.passes)},
+        "plain": {"mrays_device": round(plain_dev, 2), "mrays_wall": round(plain_wall, 2), "rays": int(pl["rays"]),
+                  "device_s": round(pl["device_ms"] * 1e-3, 3), "wall_s": round(pl["wall_s"], 3),
+                  "samples_per_pass": "auto (min(spp, 4M / pixels))"},
+        "speedup_device": round(batched_dev / plain_dev, 3), "speedup_wall": round(batched_wall / plain_wall, 3),
+        "images_identical_across_arms": bool(same),
+        "e2e": {"value": round(batched_wall, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(sum(p.width * p.height * 12 for p in params) / max(bs.passes, 1))},
+        "gpu_launches": int(bs.kernel_launches),
+        "clocks": clk,
+    }
+    if pl1 is not None:
+        d1 = pl1["rays"] / (pl1["device_ms"] * 1e-3) / 1e6
+        line["plain_1spp"] = {"mrays_device": round(d1, 2), "mrays_wall": round(pl1["rays"] / pl1["wall_s"] / 1e6, 2),
+                              "device_s": round(pl1["device_ms"] * 1e-3, 3), "wall_s": round(pl1["wall_s"], 3)}
+        line["speedup_vs_1spp_device"] = round(batched_dev / d1, 3)
+    print(json.dumps(line), flush=True)
+
+
+def run_served(args):
+    """Poisson request stream over three resident scenes (the traversal scene, the
+    subsurface scene, 16 instanced 125k-triangle meshes); each request has its own
+    resolution, spp, depth and orbit camera. Served: continuous batching in one job table
+    under a 150 GB budget, requests admitted as they arrive. Plain: one request at a time
+    in arrival order. Latency = finish - arrival (wall)."""
+    import torch
+    import numpy as np
+    from illume_gb300 import _capi as C
+    from illume_gb300 import synth
+    from illume_gb300.api import Context, Renderer, Server
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    t_gen = time.perf_counter()
+    env = synth.environment_map(1)
+    datas = [synth.traversal_scene(100_000, seed=1), synth.sss_scene(700_000, seed=3),
+             synth.instanced_scene(16, 125_000, seed=5, env=env)]
+    ctx = Context(local)
+    scenes = _upload_all(ctx, datas)
+    reqs = synth.request_stream(args.requests, len(scenes), seed=4)
+    cams = [synth.orbit_camera(datas[r["scene"]], np.random.default_rng(r["pose_seed"])) for r in reqs]
+    params = [_job_params(scenes[r["scene"]], r, C, cam) for r, cam in zip(reqs, cams)]
+    gen_s = time.perf_counter() - t_gen
+    paths = sum(p.width * p.height * p.spp for p in params)
+
+    def pct(xs, q):
+        return float(np.percentile(np.asarray(xs), q))
+
+    # served arm
+    srv = Server(ctx, hbm_budget_bytes=150 << 30, max_jobs_in_flight=64, autotune=int(args.autotune))
+    warm = srv.submit(scenes[0], _job_params(scenes[0], dict(width=64, height=64, spp=4, max_depth=4, job=999), C))
+    srv.run()
+    srv.poll(warm)
+    s0 = srv.stats()
+    clocks = Clocks(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    nxt, ids, finish, means_s = 0, {}, {}, {}
+    while nxt < len(reqs) or len(finish) < len(reqs):
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt]["arrival"] <= now:
+            ids[srv.submit(scenes[reqs[nxt]["scene"]], params[nxt])] = nxt
+            nxt += 1
+        if len(ids) == len(finish):
+            time.sleep(max(0.0, min(0.002, reqs[nxt]["arrival"] - now)))
+            continue
+        srv.step()
+        t = time.perf_counter() - t0
+        for jid, k in ids.items():
+            if k in finish:
+                continue
+            out = srv.poll(jid)
+            if out is not None:
+                finish[k] = t
+                means_s[k] = out["mean"]
+    wall_s = max(finish.values()) - reqs[0]["arrival"]
+    clk = clocks.stop()
+    s1 = srv.stats()
+    rays_s = s1.rays - s0.rays
+    lat_s = [finish[k] - reqs[k]["arrival"] for k in range(len(reqs))]
+    srv.close()
+
+    # plain arm: one request at a time, in arrival order
+    t0 = time.perf_counter()
+    finish_p, rays_p, dev_p, same = {}, 0, 0.0, True
+    for k, (r, p) in enumerate(zip(reqs, params)):
+        now = time.perf_counter() - t0
+        if r["arrival"] > now:
+            time.sleep(r["arrival"] - now)
+        rr = Renderer(ctx, scenes[r["scene"]], params=p)
+        st = rr.render_device()
+        m = rr.read(mean=True)["mean"]
+        rr.close()
+        finish_p[k] = time.perf_counter() - t0
+        rays_p += st.rays
+        dev_p += st.render_ms
+        same = same and np.array_equal(m, means_s[k])
+    wall_p = max(finish_p.values()) - reqs[0]["arrival"]
+    lat_p = [finish_p[k] - reqs[k]["arrival"] for k in range(len(reqs))]
+    served = rays_s / wall_s / 1e6
+    plain = rays_p / wall_p / 1e6
+    line = {
+        "metric": METRIC, "value": round(served, 3), "unit": "Mrays/s", "n_gpus": 1, "steps": int(s1.passes - s0.passes),
+        "warmup": 1, "ms_per_step": round((s1.device_ms - s0.device_ms) / max(s1.passes - s0.passes, 1), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"served: {args.requests} Poisson requests (mean 40/s, seed 4) over 3 resident scenes "
+                               "(traversal 100k, subsurface 700k, 16 x 125k instanced); resolution log-uniform "
+                               "64^2-1920x1080, spp log-uniform 16-4096, depth U{10..25}, orbit cameras",
+                   "mode": "continuous batching (150 GB budget) vs one request at a time",
+                   "paths": int(paths), "scene_gen_upload_s": round(gen_s, 1),
+                   "chosen_path_slots": int(s1.path_capacity), "chosen_trace_variant": int(s1.trace_variant)},
+        "served": {"mrays_wall": round(served, 2), "mrays_device": round(rays_s / ((s1.device_ms - s0.device_ms) * 1e-3) / 1e6, 2),
+                   "p50_latency_s": round(pct(lat_s, 50), 3), "p99_latency_s": round(pct(lat_s, 99), 3),
+                   "wall_s": round(wall_s, 3), "rays": int(rays_s)},
+        "plain": {"mrays_wall": round(plain, 2), "mrays_device": round(rays_p / (dev_p * 1e-3) / 1e6, 2),
+                  "p50_latency_s": round(pct(lat_p, 50), 3), "p99_latency_s": round(pct(lat_p, 99), 3),
+                  "wall_s": round(wall_p, 3), "rays": int(rays_p)},
+        "speedup_wall": round(served / plain, 3),
+        "images_identical_across_arms": bool(same),
+        "e2e": {"value": round(served, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(sum(p.width * p.height * 12 for p in params) / max(s1.passes - s0.passes, 1))},
+        "gpu_launches": int(s1.kernel_launches - s0.kernel_launches),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload == "served":
+        run_served(args)
     else:
         run_ours(args)
 

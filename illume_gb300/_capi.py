@@ -34,6 +34,7 @@ TONE_LINEAR, TONE_REINHARD, TONE_FILMIC, TONE_UNCHARTED = range(4)
 ISECT_MT, ISECT_WATERTIGHT = range(2)
 BVH_BINARY, BVH_WIDE8, BVH_WIDE8_PERSISTENT = range(3)
 ACCUM_FP32, ACCUM_KAHAN, ACCUM_FP64 = range(3)
+SERVER_PATH_CAPACITY, SERVER_PASSES_PER_STEP, SERVER_AUTOTUNE, SERVER_TRACE_VARIANT = range(4)
 
 _pi32 = POINTER(c_int32)
 _pf = POINTER(c_float)
@@ -75,7 +76,7 @@ class RenderParams(ctypes.Structure):
         ("sample_begin", c_int32), ("ray_bias", c_float), ("tonemapper", c_int32),
         ("seed", c_uint32), ("job", c_uint32), ("accum_mode", c_int32), ("intersector", c_int32),
         ("bvh_kind", c_int32), ("exact_hg", c_int32), ("samples_per_pass", c_int32),
-        ("reserved", c_int32 * 6),
+        ("camera", _pf), ("reserved", c_int32 * 4),
     ]
 
 
@@ -92,6 +93,13 @@ class Profile(ctypes.Structure):
     _fields_ = [("raygen_ms", c_double), ("trace_ms", c_double), ("shade_ms", c_double), ("accumulate_ms", c_double),
                 ("trace_launches", c_int64), ("shade_launches", c_int64), ("rays", c_int64),
                 ("node_fetches", c_int64), ("tri_tests", c_int64), ("node_bytes", c_int64), ("tri_bytes", c_int64)]
+
+
+class ServerStats(ctypes.Structure):
+    """illume_server_stats"""
+    _fields_ = [("rays", c_int64), ("passes", c_int64), ("kernel_launches", c_int64), ("jobs_done", c_int64),
+                ("device_ms", c_double), ("path_capacity", c_int64), ("trace_variant", c_int32), ("tuned", c_int32),
+                ("device_bytes", c_int64)]
 
 
 class Hit(ctypes.Structure):
@@ -123,6 +131,8 @@ PROTOTYPES = {
     "illume_scene_describe": (c_int, [c_void_p, POINTER(SceneDesc)]),
     "illume_scene_device_bytes": (c_int, [c_void_p, POINTER(c_size_t)]),
     "illume_scene_check_bvh": (c_int, [c_void_p, c_char_p, c_size_t]),
+    "illume_bvh_cache_stats": (c_int, [POINTER(c_int64), POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
+    "illume_bvh_cache_clear": (c_int, []),
     "illume_scene_upload": (c_int, [c_void_p, POINTER(c_size_t)]),
     "illume_renderer_profile": (c_int, [c_void_p, c_int, POINTER(Profile)]),
     "illume_scene_destroy": (c_int, [c_void_p]),
@@ -151,6 +161,11 @@ PROTOTYPES = {
     "illume_server_step": (c_int, [c_void_p, POINTER(c_int)]),
     "illume_job_poll": (c_int, [c_void_p, c_int64, _pf, POINTER(c_uint8), POINTER(RenderStats)]),
     "illume_job_cancel": (c_int, [c_void_p, c_int64]),
+    "illume_server_set_option": (c_int, [c_void_p, c_int, c_int64]),
+    "illume_server_get_stats": (c_int, [c_void_p, POINTER(ServerStats)]),
+    "illume_plan_pass_shares": (c_int, [c_int, _pi32, _pi32, c_int64, _pi32]),
+    "illume_render_batch": (c_int, [c_void_p, c_int, POINTER(c_void_p), POINTER(RenderParams), POINTER(_pf),
+                                    POINTER(POINTER(c_uint8)), POINTER(RenderStats), c_int, POINTER(ServerStats)]),
 }
 
 _LIB = None

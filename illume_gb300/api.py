@@ -13,6 +13,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 from typing import Optional
 
 import numpy as np
@@ -22,12 +23,24 @@ from .scenedata import SceneData
 
 
 class Context:
+    """One device and one CUDA stream. Closing a context first closes the servers,
+    renderers and scenes made with it (newest first), which must not outlive it."""
+
     def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
         self.handle = ctypes.c_void_p()
+        self._children = []
         C.check(C.lib().illume_context_create(device, hbm_budget_bytes, ctypes.byref(self.handle)))
+
+    def _adopt(self, obj):
+        self._children.append(weakref.ref(obj))
 
     def close(self):
         if self.handle:
+            for ref in reversed(self._children):
+                obj = ref()
+                if obj is not None:
+                    obj.close()
+            self._children = []
             C.lib().illume_context_destroy(self.handle)
             self.handle = ctypes.c_void_p()
 
@@ -48,6 +61,7 @@ class HostScene:
     def __init__(self, ctx: Context, handle: ctypes.c_void_p):
         self.ctx = ctx
         self.handle = handle
+        ctx._adopt(self)
 
     @staticmethod
     def from_json_file(ctx: Context, path: str, base_dir: Optional[str] = None) -> "HostScene":
@@ -141,6 +155,7 @@ class Renderer:
         self.params = p
         self.handle = ctypes.c_void_p()
         C.check(C.lib().illume_renderer_create(ctx.handle, scene.handle, ctypes.byref(p), ctypes.byref(self.handle)))
+        ctx._adopt(self)
 
     def get_width(self) -> int:
         return C.lib().illume_renderer_get_width(self.handle)
@@ -197,3 +212,88 @@ def bsdf_batch(ctx: Context, material_type: int, distribution: int, inputs: np.n
     y = np.zeros_like(x)
     C.check(C.lib().illume_bsdf_batch(ctx.handle, material_type, distribution, C.fptr(x), x.shape[0], C.fptr(y)))
     return y
+
+
+class Server:
+    """Continuous-batching render server (illume_server_* of include/illume.h)."""
+
+    def __init__(self, ctx: Context, hbm_budget_bytes: int = 0, max_jobs_in_flight: int = 0, **options):
+        self.ctx = ctx
+        self.handle = ctypes.c_void_p()
+        C.check(C.lib().illume_server_create(ctx.handle, hbm_budget_bytes, max_jobs_in_flight, ctypes.byref(self.handle)))
+        ctx._adopt(self)
+        self._npix = {}
+        names = {"path_capacity": C.SERVER_PATH_CAPACITY, "passes_per_step": C.SERVER_PASSES_PER_STEP,
+                 "autotune": C.SERVER_AUTOTUNE, "trace_variant": C.SERVER_TRACE_VARIANT}
+        for k, v in options.items():
+            C.check(C.lib().illume_server_set_option(self.handle, names[k], int(v)))
+
+    def submit(self, scene: HostScene, params: C.RenderParams) -> int:
+        jid = ctypes.c_int64()
+        C.check(C.lib().illume_job_submit(self.handle, scene.handle, ctypes.byref(params), ctypes.byref(jid)))
+        self._npix[jid.value] = params.width * params.height
+        return jid.value
+
+    def step(self) -> int:
+        running = ctypes.c_int()
+        C.check(C.lib().illume_server_step(self.handle, ctypes.byref(running)))
+        return running.value
+
+    def run(self, max_steps: int = 1_000_000) -> int:
+        """Steps until no job is running or queued; returns the number of steps."""
+        n = 0
+        while self.step():
+            n += 1
+            if n >= max_steps:
+                raise RuntimeError("server did not drain")
+        return n + 1
+
+    def poll(self, job: int, rgb8: bool = False):
+        """None while the job runs, else {'mean', 'rgb8'?, 'stats'}; raises if cancelled or failed."""
+        n = self._npix[job]
+        mean = np.zeros((n, 3), np.float32)
+        px = np.zeros((n, 3), np.uint8) if rgb8 else None
+        st = C.RenderStats()
+        s = C.lib().illume_job_poll(self.handle, job, C.fptr(mean), C.u8ptr(px), ctypes.byref(st))
+        if s == C.ERR_NOT_READY:
+            return None
+        C.check(s)
+        out = {"mean": mean, "stats": st}
+        if rgb8:
+            out["rgb8"] = px
+        return out
+
+    def cancel(self, job: int):
+        C.check(C.lib().illume_job_cancel(self.handle, job))
+
+    def stats(self) -> C.ServerStats:
+        s = C.ServerStats()
+        C.check(C.lib().illume_server_get_stats(self.handle, ctypes.byref(s)))
+        return s
+
+    def close(self):
+        if self.handle:
+            C.lib().illume_server_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def render_batch(ctx: Context, scenes, params, autotune: bool = False, rgb8: bool = False):
+    """illume_render_batch: every job rendered together; returns ([mean per job], [rgb8 per job] or None,
+    [RenderStats per job], ServerStats)."""
+    n = len(scenes)
+    means = [np.zeros((p.width * p.height, 3), np.float32) for p in params]
+    pix = [np.zeros((p.width * p.height, 3), np.uint8) for p in params] if rgb8 else None
+    sc = (ctypes.c_void_p * n)(*[s.handle.value for s in scenes])
+    pa = (C.RenderParams * n)(*params)
+    mp = (C._pf * n)(*[C.fptr(m) for m in means])
+    rp = (ctypes.POINTER(ctypes.c_uint8) * n)(*[C.u8ptr(x) for x in pix]) if rgb8 else None
+    js = (C.RenderStats * n)()
+    bs = C.ServerStats()
+    C.check(C.lib().illume_render_batch(ctx.handle, n, sc, pa, mp, rp, js, int(autotune), ctypes.byref(bs)))
+    return means, pix, list(js), bs

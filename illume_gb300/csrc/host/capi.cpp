@@ -130,6 +130,21 @@ int illume_renderer_profile(illume_renderer* r, int count_visits, illume_profile
   return r->r.profile(count_visits != 0, out);
 }
 
+int illume_bvh_cache_stats(int64_t* entries, int64_t* bytes, int64_t* hits, int64_t* misses) {
+  long long e = 0, b = 0, h = 0, m = 0;
+  illume::bvh_cache_stats(&e, &b, &h, &m);
+  if (entries) *entries = e;
+  if (bytes) *bytes = b;
+  if (hits) *hits = h;
+  if (misses) *misses = m;
+  return ILLUME_OK;
+}
+
+int illume_bvh_cache_clear(void) {
+  illume::bvh_cache_clear();
+  return ILLUME_OK;
+}
+
 int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t report_len) {
   CHECK_ARG(scene, "null scene");
   const SceneHost& h = scene->s.host;
@@ -312,7 +327,7 @@ int illume_trace_closest_device(illume_context* ctx, illume_scene* scene, const 
   CHECK_ARG(((uintptr_t)d_rays & 15) == 0, "rays must be 16-byte aligned");
   CHECK_ARG(scene->s.ctx == &ctx->c, "scene was not uploaded with this context");
   cudaSetDevice(ctx->c.device);
-  launch_trace_hook(scene->s.view, d_rays, n, intersector, bvh_kind, d_hits, ctx->c.stream);
+  launch_trace_hook(scene->s.view, scene->s.view_dev, d_rays, n, intersector, bvh_kind, d_hits, ctx->c.stream);
   ILLUME_CUDA_TRY(cudaGetLastError());
   ctx->c.launches += n > 0 ? 1 : 0;
   return ILLUME_OK;

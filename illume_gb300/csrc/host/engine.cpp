@@ -1,0 +1,235 @@
+#include "engine.h"
+
+#include <stddef.h>
+
+#include <algorithm>
+
+namespace illume {
+
+Engine::~Engine() { drop_graphs(); }
+
+void Engine::drop_graphs() {
+  for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+  graphs.clear();
+}
+
+int Engine::alloc_paths(std::string* err) {
+  int st;
+#define ALLOC(buf, bytes) if ((st = (buf).alloc(ctx, (bytes))) != ILLUME_OK) { *err = last_error(); return st; }
+  for (int k = 0; k < 2; ++k) {
+    ALLOC(q_orig[k], sizeof(float4) * (size_t)cap);
+    ALLOC(q_dir[k], sizeof(float4) * (size_t)cap);
+    ALLOC(q_thr[k], sizeof(float4) * (size_t)cap);
+  }
+  ALLOC(hit, sizeof(float4) * (size_t)cap);
+  ALLOC(hit_geom, sizeof(int) * (size_t)cap);
+  ALLOC(evq, sizeof(int) * (size_t)cap * EV_COUNT);
+  ALLOC(contrib, sizeof(float4) * (size_t)cap);
+#undef ALLOC
+  return ILLUME_OK;
+}
+
+void Engine::point() {
+  for (int k = 0; k < 2; ++k) {
+    w.q_orig[k] = q_orig[k].as<float4>();
+    w.q_dir[k] = q_dir[k].as<float4>();
+    w.q_thr[k] = q_thr[k].as<float4>();
+  }
+  w.hit = hit.as<float4>();
+  w.hit_geom = hit_geom.as<int>();
+  w.evq = evq.as<int>();
+  w.counters = counters.as<int>();
+  w.contrib = contrib.as<float4>();
+  w.rays = rays.as<unsigned long long>();
+  w.visits = visits.as<unsigned long long>();
+  w.jobs = jobs.as<JobDesc>();
+  w.job_path_base = path_base.as<int>();
+  w.job_pixel_base = pixel_base.as<int>();
+  w.njobs = rows;
+  w.cap = cap;
+  const int sms = std::max(1, ctx->sm_count);
+  grid_raygen = std::max(1, std::min((cap + 255) / 256, sms * 8));
+  grid_acc = grid_raygen;
+}
+
+int Engine::init(Context* c, int nrows, int ncap, const RenderKnobs& k, std::string* err) {
+  ctx = c;
+  rows = nrows;
+  cap = ncap;
+  knobs = k;
+  if (rows < 1 || rows > kMaxJobRows) { *err = "job table rows out of range"; return ILLUME_ERR_INVALID; }
+  if (cap < 1 || cap > (1 << 30)) { *err = "path slots out of range"; return ILLUME_ERR_INVALID; }
+  int st;
+  if ((st = alloc_paths(err)) != ILLUME_OK) return st;
+#define ALLOC(buf, bytes) if ((st = (buf).alloc(ctx, (bytes))) != ILLUME_OK) { *err = last_error(); return st; }
+  ALLOC(counters, sizeof(int) * kCounterWords);
+  ALLOC(rays, sizeof(unsigned long long));
+  ALLOC(visits, 2 * sizeof(unsigned long long));
+  ALLOC(jobs, sizeof(JobDesc) * (size_t)rows);
+  ALLOC(path_base, sizeof(int) * (size_t)(rows + 1));
+  ALLOC(pixel_base, sizeof(int) * (size_t)(rows + 1));
+#undef ALLOC
+  mirror.assign(rows, JobDesc{});
+  ILLUME_CUDA_TRY(cudaMemsetAsync(counters.get(), 0, counters.size(), ctx->stream));
+  ILLUME_CUDA_TRY(cudaMemsetAsync(rays.get(), 0, rays.size(), ctx->stream));
+  ILLUME_CUDA_TRY(cudaMemsetAsync(visits.get(), 0, visits.size(), ctx->stream));
+  ILLUME_CUDA_TRY(cudaMemsetAsync(jobs.get(), 0, jobs.size(), ctx->stream));
+  point();
+  grid_trace = kernel_grid_blocks(trace_kernel_ptr(knobs.bvh_kind, knobs.trace_variant), 128, ctx->device);
+  grid_shade = kernel_grid_blocks(shade_kernel_ptr(), 128, ctx->device);
+  return ILLUME_OK;
+}
+
+int Engine::resize(int new_cap, std::string* err) {
+  if (new_cap == cap) return ILLUME_OK;
+  if (new_cap < 1 || new_cap > (1 << 30)) { *err = "path slots out of range"; return ILLUME_ERR_INVALID; }
+  ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  drop_graphs();
+  const int old = cap;
+  cap = new_cap;
+  const int st = alloc_paths(err);
+  if (st != ILLUME_OK) {
+    cap = old;
+    std::string e2;
+    alloc_paths(&e2);
+    point();
+    return st;
+  }
+  point();
+  return ILLUME_OK;
+}
+
+int Engine::set_trace_variant(int variant) {
+  if (variant == knobs.trace_variant) return ILLUME_OK;
+  drop_graphs();
+  knobs.trace_variant = variant;
+  grid_trace = kernel_grid_blocks(trace_kernel_ptr(knobs.bvh_kind, knobs.trace_variant), 128, ctx->device);
+  return ILLUME_OK;
+}
+
+int Engine::write_row(int r) {
+  ILLUME_CUDA_TRY(cudaMemcpyAsync(jobs.as<JobDesc>() + r, &mirror[r], sizeof(JobDesc), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  return ILLUME_OK;
+}
+
+int Engine::write_pass_state(int r) {
+  const size_t off = offsetof(JobDesc, sample_base);
+  static_assert(offsetof(JobDesc, per_pass) == offsetof(JobDesc, sample_base) + 3 * sizeof(int), "pass state words");
+  ILLUME_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(jobs.as<JobDesc>() + r) + off,
+                                  reinterpret_cast<const char*>(&mirror[r]) + off, 4 * sizeof(int),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+  return ILLUME_OK;
+}
+
+void Engine::advance_mirror() {
+  for (JobDesc& J : mirror) {
+    if (J.nsamples <= 0) continue;
+    J.sample_base += J.nsamples;
+    const int left = J.sample_end - J.sample_base;
+    J.nsamples = left < J.per_pass ? std::max(left, 0) : J.per_pass;
+  }
+}
+
+long long Engine::paths_in_pass() const {
+  long long n = 0;
+  for (const JobDesc& J : mirror)
+    if (J.nsamples > 0) n += (long long)J.nsamples * J.npix;
+  return n;
+}
+
+int Engine::free_rows() const {
+  int n = 0;
+  for (const JobDesc& J : mirror) n += J.nsamples <= 0;
+  return n;
+}
+
+void Engine::launch_pass(cudaStream_t st, int depth) {
+  launch_plan(w, st);
+  launch_raygen(w, grid_raygen, st);
+  for (int b = 0; b < depth; ++b) {
+    launch_trace(w, knobs, b, grid_trace, st);
+    launch_shade(w, b, grid_shade, st);
+  }
+  launch_accumulate(w, grid_acc, st);
+  launch_advance(w, st);
+}
+
+int Engine::run(int npasses, int depth) {
+  if (npasses <= 0) return ILLUME_OK;
+  if (paths_in_pass() > cap) {
+    set_error("job table needs more path slots than the engine has");
+    return ILLUME_ERR_INVALID;
+  }
+  cudaStream_t st = ctx->stream;
+  auto it = graphs.find(depth);
+  if (it == graphs.end()) {
+    cudaGraph_t g;
+    ILLUME_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    launch_pass(st, depth);
+    ILLUME_CUDA_TRY(cudaStreamEndCapture(st, &g));
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+      return ILLUME_ERR_CUDA;
+    }
+    it = graphs.emplace(depth, exec).first;
+  }
+  for (int i = 0; i < npasses; ++i) {
+    ILLUME_CUDA_TRY(cudaGraphLaunch(it->second, st));
+    advance_mirror();
+  }
+  passes += npasses;
+  launches += (long long)npasses * launches_per_pass(depth);
+  ctx->launches += (long long)npasses * launches_per_pass(depth);
+  return ILLUME_OK;
+}
+
+int Engine::run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>& ev) {
+  if (paths_in_pass() > cap) {
+    set_error("job table needs more path slots than the engine has");
+    return ILLUME_ERR_INVALID;
+  }
+  cudaStream_t st = ctx->stream;
+  ev.resize(3 + 2 * depth);
+  for (auto& e : ev) ILLUME_CUDA_TRY(cudaEventCreate(&e));
+  int k = 0;
+  cudaEventRecord(ev[k++], st);
+  launch_plan(w, st);
+  launch_raygen(w, grid_raygen, st);
+  cudaEventRecord(ev[k++], st);
+  for (int b = 0; b < depth; ++b) {
+    launch_trace(w, knobs, b, grid_trace, st, count_visits);
+    cudaEventRecord(ev[k++], st);
+    launch_shade(w, b, grid_shade, st);
+    cudaEventRecord(ev[k++], st);
+  }
+  launch_accumulate(w, grid_acc, st);
+  cudaEventRecord(ev[k++], st);
+  launch_advance(w, st);
+  ILLUME_CUDA_TRY(cudaGetLastError());
+  advance_mirror();
+  passes += 1;
+  launches += launches_per_pass(depth);
+  ctx->launches += launches_per_pass(depth);
+  return ILLUME_OK;
+}
+
+int Engine::read_row_rays(int r, unsigned long long* out) {
+  ILLUME_CUDA_TRY(cudaMemcpyAsync(out, reinterpret_cast<const char*>(jobs.as<JobDesc>() + r) + offsetof(JobDesc, rays),
+                                  sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+  ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ILLUME_OK;
+}
+
+size_t Engine::device_bytes() const {
+  size_t b = 0;
+  const DevBuffer* all[] = {&q_orig[0], &q_orig[1], &q_dir[0], &q_dir[1], &q_thr[0], &q_thr[1], &hit, &hit_geom,
+                            &evq, &counters, &contrib, &rays, &visits, &jobs, &path_base, &pixel_base};
+  for (const DevBuffer* d : all) b += d->size();
+  return b;
+}
+
+}  // namespace illume

@@ -1,0 +1,65 @@
+// Wavefront engine: the device buffers and captured passes of one job table.
+//
+// A pass renders the current sample range of every row of the table (see
+// kernels/launch.h). The host keeps a mirror of the table that it advances exactly as
+// k_advance advances the device copy, so it knows every row's sample range after any
+// number of replayed passes without reading the device. Rows are written to the device
+// only between passes (stream-ordered copies), whole when a job starts and as the
+// pass-state words when its share of the slots changes.
+#pragma once
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../kernels/launch.h"
+#include "runtime.h"
+
+namespace illume {
+
+struct Engine {
+  Context* ctx = nullptr;
+  int rows = 0;                  // job table rows
+  int cap = 0;                   // path slots of one pass
+  RenderKnobs knobs{};
+  DevBuffer q_orig[2], q_dir[2], q_thr[2], hit, hit_geom, evq, counters, contrib, rays, visits;
+  DevBuffer jobs, path_base, pixel_base;
+  WaveBuffers w{};
+  std::vector<JobDesc> mirror;   // the table as the device has it after the launched passes
+  int grid_trace = 0, grid_shade = 0, grid_raygen = 0, grid_acc = 0;
+  std::map<int, cudaGraphExec_t> graphs;   // captured pass by depth
+  long long passes = 0, launches = 0;
+
+  Engine() = default;
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+  ~Engine();
+
+  int init(Context* c, int rows, int cap, const RenderKnobs& k, std::string* err);
+  // Reallocates the per-path buffers for a new slot count (between passes only).
+  int resize(int new_cap, std::string* err);
+  // Selects another trace kernel instance (between passes only).
+  int set_trace_variant(int variant);
+  int write_row(int r);          // whole row (a job starts: its ray total restarts at 0)
+  int write_pass_state(int r);   // sample_base, nsamples, sample_end, per_pass of row r
+  // Replays the captured pass `npasses` times with `depth` bounces and advances the mirror.
+  int run(int npasses, int depth);
+  // One pass launched kernel by kernel, with events after every stage:
+  // ev[0] before plan, ev[1] after raygen, ev[2 + 2b] after trace b, ev[3 + 2b] after
+  // shade b, ev[2 + 2 depth] after accumulate. count_visits selects the instrumented trace.
+  int run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>& ev);
+  int read_row_rays(int r, unsigned long long* out);   // synchronous
+  int free_rows() const;
+  long long paths_in_pass() const;                      // of the next pass, from the mirror
+  static int launches_per_pass(int depth) { return 5 + 2 * depth; }
+  size_t device_bytes() const;
+
+ private:
+  int alloc_paths(std::string* err);
+  void point();
+  void advance_mirror();
+  void launch_pass(cudaStream_t st, int depth);
+  void drop_graphs();
+};
+
+}  // namespace illume

@@ -1,16 +1,15 @@
 // Renderer: the GB300 replacement of Renderer::render_to_bitmap (src/renderer.cu:498-597).
 //
-// A render is a sequence of wavefront passes. Each pass keeps `per_pass` samples of every
-// pixel in flight: raygen, max_depth x (trace, shade), accumulate, advance. The pass is
-// captured once into a CUDA graph and replayed; everything that changes from pass to
-// pass (first sample, samples in the pass) lives in device memory, so the host issues
-// one graph launch per pass and never waits inside the loop.
+// A render is a sequence of wavefront passes over a one-row job table (engine.h). Each
+// pass keeps `per_pass` samples of every pixel in flight: plan, raygen, max_depth x
+// (trace, shade), accumulate, advance. The pass is captured once into a CUDA graph and
+// replayed; the sample range lives in the device's job row, so the host issues one
+// graph launch per pass and never waits inside the loop.
 #pragma once
 
 #include <memory>
 
-#include "../kernels/launch.h"
-#include "runtime.h"
+#include "engine.h"
 
 namespace illume {
 
@@ -18,15 +17,10 @@ struct Renderer {
   Context* ctx = nullptr;
   Scene* scene = nullptr;
   illume_render_params p{};
-  int npix = 0, per_pass = 1, cap = 0;
-  DevBuffer q_orig[2], q_dir[2], q_thr[2], hit, hit_geom, evq, counters, contrib, rays, visits, pass;
+  int npix = 0, per_pass = 1;
+  Engine eng;
   DevBuffer sum32, comp32, sum64, sumsq, out_mean, out_rgb8;
-  WaveBuffers w{};
   Accumulators acc{};
-  CameraView cam{};
-  RenderKnobs knobs{};
-  int grid_trace = 0, grid_shade = 0, grid_raygen = 0, grid_acc = 0;
-  cudaGraphExec_t graph = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   long long samples_done = 0;   // samples accumulated since the last clear
   int next_sample = 0;          // first sample of the next progressive call
@@ -41,9 +35,18 @@ struct Renderer {
   size_t device_bytes() const;
 
  private:
-  int launch_pass(cudaStream_t st);
+  void set_range(int first, int count);
 };
 
 CameraView make_camera(const SceneHost& h, int width, int height);
+
+// Checks the parts of a render's parameters that every path of this library needs.
+int check_render_params(const illume_render_params& p, const Scene& scene, std::string* err);
+
+// Job row of a render: scene, camera, Philox key and depth of `p`, no sample range yet.
+JobDesc job_row(const Scene& scene, const illume_render_params& p, const Accumulators& acc);
+
+// Trace kernel settings of a render (intersector, BVH layout, kernel variant).
+RenderKnobs render_knobs(const illume_render_params& p);
 
 }  // namespace illume

@@ -7,6 +7,7 @@
 #include <chrono>
 #include <map>
 #include <mutex>
+#include <thread>
 
 namespace illume {
 
@@ -269,15 +270,108 @@ static float pad_up(double v, double pad) {
   return f;
 }
 
+// ---- BVH cache keyed by mesh content ----
+//
+// Scenes that share meshes (instanced assets, a pool of meshes reused across jobs) build
+// each distinct mesh once per process. The key is two independent 64-bit hashes of the
+// vertex and index words plus the counts; a hit copies the cached build.
+namespace {
+
+struct BvhKey {
+  uint64_t h1, h2;
+  int nv, nt;
+  bool operator<(const BvhKey& o) const {
+    if (h1 != o.h1) return h1 < o.h1;
+    if (h2 != o.h2) return h2 < o.h2;
+    if (nv != o.nv) return nv < o.nv;
+    return nt < o.nt;
+  }
+};
+
+inline uint64_t rotl64(uint64_t x, int r) { return (x << r) | (x >> (64 - r)); }
+
+BvhKey mesh_key(const float* P, int nv, const int* T, int nt) {
+  uint64_t h1 = 0x243f6a8885a308d3ULL, h2 = 0x13198a2e03707344ULL;
+  auto mix = [&](uint32_t w) {
+    h1 = rotl64(h1 ^ (w * 0x9e3779b97f4a7c15ULL), 29) * 0xbf58476d1ce4e5b9ULL;
+    h2 = rotl64(h2 + (uint64_t)w * 0xc2b2ae3d27d4eb4fULL, 31) ^ (h2 >> 17);
+  };
+  const uint32_t* pw = reinterpret_cast<const uint32_t*>(P);
+  for (size_t i = 0; i < 3 * (size_t)nv; ++i) mix(pw[i]);
+  for (size_t i = 0; i < 3 * (size_t)nt; ++i) mix((uint32_t)T[i]);
+  return BvhKey{h1, h2, nv, nt};
+}
+
+std::mutex g_bvh_mu;
+std::map<BvhKey, MeshBvh> g_bvh_cache;
+size_t g_bvh_bytes = 0;
+long long g_bvh_hits = 0, g_bvh_misses = 0;
+constexpr size_t kBvhCacheMaxBytes = size_t(4) << 30;
+
+size_t bvh_bytes(const MeshBvh& b) {
+  return b.bvh2.size() * sizeof(Bvh2Node) + b.bvh2_tris.size() * sizeof(float4) + b.wide.size() * sizeof(WideNode) +
+         b.wide_tris.size() * sizeof(float4);
+}
+
+void build_cached(const float* P, int nv, const int* T, int nt, MeshBvh* out) {
+  const BvhKey key = mesh_key(P, nv, T, nt);
+  {
+    std::lock_guard<std::mutex> lk(g_bvh_mu);
+    auto it = g_bvh_cache.find(key);
+    if (it != g_bvh_cache.end()) {
+      ++g_bvh_hits;
+      *out = it->second;
+      return;
+    }
+    ++g_bvh_misses;
+  }
+  build_mesh_bvh(P, nv, T, nt, out);
+  const size_t bytes = bvh_bytes(*out);
+  std::lock_guard<std::mutex> lk(g_bvh_mu);
+  if (bytes > kBvhCacheMaxBytes) return;
+  if (g_bvh_bytes + bytes > kBvhCacheMaxBytes) {
+    g_bvh_cache.clear();
+    g_bvh_bytes = 0;
+  }
+  if (g_bvh_cache.emplace(key, *out).second) g_bvh_bytes += bytes;
+}
+
+}  // namespace
+
+void bvh_cache_stats(long long* entries, long long* bytes, long long* hits, long long* misses) {
+  std::lock_guard<std::mutex> lk(g_bvh_mu);
+  *entries = (long long)g_bvh_cache.size();
+  *bytes = (long long)g_bvh_bytes;
+  *hits = g_bvh_hits;
+  *misses = g_bvh_misses;
+}
+
+void bvh_cache_clear() {
+  std::lock_guard<std::mutex> lk(g_bvh_mu);
+  g_bvh_cache.clear();
+  g_bvh_bytes = 0;
+}
+
+// Builds every mesh's BVHs, distinct meshes in parallel on the host cores.
 int Scene::build_host(std::string* err) {
   auto t0 = std::chrono::steady_clock::now();
   const SceneHost& h = host;
   const int nm = h.num_meshes();
-  bvhs.resize(nm);
+  bvhs.assign(nm, MeshBvh{});
+  const int nthreads = std::max(1, std::min<int>(nm, (int)std::thread::hardware_concurrency()));
+  std::vector<std::thread> pool;
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int i = next++; i < nm; i = next++) {
+      const float* P = h.positions.data() + 3 * (size_t)h.mesh_vertex_offset[i];
+      const int* T = h.tris.data() + 3 * (size_t)h.mesh_tri_offset[i];
+      build_cached(P, h.mesh_num_vertices[i], T, h.mesh_num_tris[i], &bvhs[i]);
+    }
+  };
+  for (int t = 1; t < nthreads; ++t) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
   for (int i = 0; i < nm; ++i) {
-    const float* P = h.positions.data() + 3 * (size_t)h.mesh_vertex_offset[i];
-    const int* T = h.tris.data() + 3 * (size_t)h.mesh_tri_offset[i];
-    build_mesh_bvh(P, h.mesh_num_vertices[i], T, h.mesh_num_tris[i], &bvhs[i]);
     if (bvhs[i].stats.bvh2_depth > 60) {
       *err = "binary BVH deeper than the traversal stack (mesh " + std::to_string(i) + ")";
       return ILLUME_ERR_UNSUPPORTED;
@@ -426,6 +520,12 @@ int Scene::build_and_upload(std::string* err) {
   v.num_materials = nmat;
   v.env_tex = h.env_tex;
   view = v;
+  {
+    void* p_ = nullptr;
+    const int st_ = up(&view, sizeof(SceneView), &p_);
+    if (st_ != ILLUME_OK) { *err = last_error(); return st_; }
+    view_dev = reinterpret_cast<SceneView*>(p_);
+  }
   ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   upload_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
   return ILLUME_OK;

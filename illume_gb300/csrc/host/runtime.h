@@ -98,6 +98,7 @@ struct Scene {
   std::vector<MeshBvh> bvhs;
   std::vector<std::unique_ptr<DevBuffer>> buffers;
   SceneView view{};
+  SceneView* view_dev = nullptr;   // device copy of `view`
   size_t device_bytes = 0;
   // device tables (kept for re-uploads) and the host source of every device buffer
   std::vector<DevMesh> t_meshes;
@@ -113,6 +114,10 @@ struct Scene {
   int build_host(std::string* err);        // BVHs only (host-only scenes)
   int build_and_upload(std::string* err);  // BVHs + device tables
 };
+
+// Process-wide cache of mesh BVH builds keyed by mesh content (runtime.cpp).
+void bvh_cache_stats(long long* entries, long long* bytes, long long* hits, long long* misses);
+void bvh_cache_clear();
 
 // JSON scene ingest (src/scene/scene.cpp:11-99 and the *_from_json functions it calls).
 int load_scene_json(const std::string& text, const std::string& base_dir, SceneHost* out, std::string* err);

@@ -1,6 +1,7 @@
 #include "server.h"
 #include "handles.h"
 
+#include <stddef.h>
 #include <string.h>
 
 #include <algorithm>
@@ -14,34 +15,48 @@ double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-int Server::chunk_for(const illume_render_params& p) {
-  const long long npix = (long long)p.width * p.height;
-  const long long target = 1LL << 21;
-  return (int)std::max(1LL, std::min<long long>(std::max(p.spp, 1), target / std::max(npix, 1LL)));
+static constexpr size_t kBytesPerPath = 6 * sizeof(float4) + sizeof(float4) + sizeof(int) + EV_COUNT * sizeof(int) +
+                                        sizeof(float4);
+
+static int engine_key(const illume_render_params& p) { return p.intersector * 16 + p.bvh_kind; }
+
+Server::~Server() {
+  if (ctx) cudaStreamSynchronize(ctx->stream);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
 }
 
-// Device bytes a job holds while running: wavefront queues for one chunk of samples plus
-// the per-pixel accumulators and output staging (the layout Renderer::init allocates).
-size_t Server::footprint(const illume_render_params& p, int chunk) {
+// Device bytes a running job holds: its accumulators and output staging.
+size_t Server::footprint(const illume_render_params& p) {
   const size_t npix = (size_t)p.width * p.height;
-  const size_t paths = npix * (size_t)chunk;
-  const size_t per_path = 6 * 16 + 16 + 4 + 4 * EV_COUNT + 16;
-  const size_t per_pixel = (p.accum_mode == ACCUM_FP64 ? 24 : (p.accum_mode == ACCUM_KAHAN ? 24 : 12)) + 24 + 12 + 3;
-  return paths * per_path + npix * per_pixel + 4096;
+  const size_t acc = p.accum_mode == ACCUM_FP32 ? 12 : 24;
+  return npix * (acc + 12 + 3) + 4096;
+}
+
+size_t Server::engines_bytes() const {
+  size_t b = 0;
+  for (const auto& kv : engines) b += kv.second.eng->device_bytes();
+  return b;
 }
 
 int Server::submit(Scene* scene, const illume_render_params& p, int64_t* id) {
-  const int chunk = chunk_for(p);
-  const size_t fp = footprint(p, chunk);
-  if (budget && fp > budget) {
-    set_error("job footprint " + std::to_string(fp) + " bytes exceeds the server budget");
+  std::string err;
+  int st = check_render_params(p, *scene, &err);
+  if (st != ILLUME_OK) { set_error(err); return st; }
+  const size_t fp = footprint(p);
+  const size_t min_engine = (size_t)std::max<long long>((long long)p.width * p.height, 1) * kBytesPerPath;
+  if (budget && fp + min_engine + (1 << 20) > budget) {
+    set_error("job footprint " + std::to_string(fp + min_engine) + " bytes exceeds the server budget");
     return ILLUME_ERR_BUDGET;
   }
   std::unique_ptr<ServerJob> j(new ServerJob);
   j->id = next_id++;
   j->scene = scene;
   j->params = p;
-  j->params.samples_per_pass = chunk;
+  if (p.camera) {
+    memcpy(j->camera, p.camera, sizeof(j->camera));
+    j->params.camera = j->camera;
+  }
   j->footprint = fp;
   j->submit_ms = now_ms();
   *id = j->id;
@@ -50,66 +65,292 @@ int Server::submit(Scene* scene, const illume_render_params& p, int64_t* id) {
   return ILLUME_OK;
 }
 
-int Server::step(int* running_out) {
-  // admission: FIFO while the budget and the slot count allow
-  int running = 0;
-  for (auto& kv : jobs) running += kv.second->state == 1;
-  while (!queue.empty()) {
-    ServerJob* j = jobs[queue.front()].get();
-    if (j->state == 3) { queue.pop_front(); continue; }
-    if (running >= max_in_flight || (budget && reserved + j->footprint > budget)) break;
-    queue.pop_front();
-    j->r.reset(new Renderer);
-    j->r->ctx = ctx;
-    j->r->scene = j->scene;
-    j->r->p = j->params;
-    std::string err;
-    const int st = j->r->init(&err);
-    if (st != ILLUME_OK) {
-      j->state = 4;
-      j->error = err;
-      j->r.reset();
-      continue;
+// Admits queued jobs in arrival order while a row, one sample of every pixel and the
+// job's footprint fit; a job that does not fit yet keeps its place and later jobs may
+// pass it.
+int Server::admit() {
+  if (budget && !queue.empty()) {
+    // under a budget, idle tables give their memory back to the queue
+    for (auto eit = engines.begin(); eit != engines.end();) {
+      bool idle = true;
+      for (int64_t id : eit->second.row_job) idle &= id == 0;
+      if (idle) eit = engines.erase(eit);
+      else ++eit;
     }
-    reserved += j->footprint;
+  }
+  for (auto it = queue.begin(); it != queue.end();) {
+    ServerJob* j = jobs[*it].get();
+    if (j->state == 3) { it = queue.erase(it); continue; }
+    const illume_render_params& p = j->params;
+    const int npix = p.width * p.height;
+    const int key = engine_key(p);
+    auto eit = engines.find(key);
+    if (eit == engines.end()) {
+      long long cap = std::max(path_capacity, npix);
+      if (budget) {
+        const long long used = (long long)(reserved + engines_bytes() + j->footprint + (1 << 20));
+        const long long affordable = ((long long)budget - used) / (long long)kBytesPerPath;
+        cap = std::min(cap, affordable);
+        if (cap < npix) { ++it; continue; }
+      }
+      ServerEngine se;
+      se.eng.reset(new Engine);
+      RenderKnobs k = render_knobs(p);
+      k.trace_variant = trace_variant >= 0 ? trace_variant : (p.bvh_kind == 2 ? 1 : 0);
+      std::string err;
+      const int st = se.eng->init(ctx, rows, (int)cap, k, &err);
+      if (st != ILLUME_OK) { set_error(err); return st; }
+      se.row_job.assign(rows, 0);
+      eit = engines.emplace(key, std::move(se)).first;
+    }
+    ServerEngine& se = eit->second;
+    Engine& e = *se.eng;
+    int running = 0;
+    long long min_paths = 0;
+    int free_row = -1;
+    for (int r = 0; r < e.rows; ++r) {
+      if (se.row_job[r]) { ++running; min_paths += e.mirror[r].npix; }
+      else if (free_row < 0) free_row = r;
+    }
+    if (free_row < 0) { ++it; continue; }
+    if (npix > e.cap) {
+      if (running) { ++it; continue; }
+      if (budget && reserved + engines_bytes() + ((size_t)npix - e.cap) * kBytesPerPath + j->footprint > budget) {
+        ++it;
+        continue;
+      }
+      std::string err;
+      const int st = e.resize(npix, &err);
+      if (st != ILLUME_OK) { set_error(err); return st; }
+    }
+    if (min_paths + npix > e.cap) { ++it; continue; }
+    if (budget && reserved + engines_bytes() + j->footprint > budget) { ++it; continue; }
+    // job buffers
+    int st;
+    const size_t n3 = 3 * (size_t)npix;
+    Accumulators acc{};
+    if (p.accum_mode == ACCUM_FP64) { if ((st = j->sum64.alloc(ctx, sizeof(double) * n3)) != ILLUME_OK) return st; }
+    else if ((st = j->sum32.alloc(ctx, sizeof(float) * n3)) != ILLUME_OK) return st;
+    if (p.accum_mode == ACCUM_KAHAN && (st = j->comp32.alloc(ctx, sizeof(float) * n3)) != ILLUME_OK) return st;
+    if ((st = j->out_mean.alloc(ctx, sizeof(float) * n3)) != ILLUME_OK) return st;
+    if ((st = j->out_rgb8.alloc(ctx, n3)) != ILLUME_OK) return st;
+    acc.sum32 = j->sum32.as<float>();
+    acc.comp32 = j->comp32.as<float>();
+    acc.sum64 = j->sum64.as<double>();
+    acc.sumsq = nullptr;
+    launch_clear_accumulators(acc, npix, ctx->stream);
+    JobDesc row = job_row(*j->scene, p, acc);
+    row.sample_base = p.sample_begin;
+    row.sample_end = p.sample_begin + p.spp;
+    row.per_pass = 1;
+    row.nsamples = p.spp > 0 ? 1 : 0;
+    e.mirror[free_row] = row;
+    if ((st = e.write_row(free_row)) != ILLUME_OK) return st;
+    se.row_job[free_row] = j->id;
+    j->key = key;
+    j->row = free_row;
     j->state = 1;
     j->start_ms = now_ms();
-    ++running;
+    reserved += j->footprint;
+    it = queue.erase(it);
   }
-  // one progressive chunk of every running job
-  for (auto& kv : jobs) {
-    ServerJob* j = kv.second.get();
-    if (j->state != 1) continue;
-    const int left = j->params.spp - j->spp_done;
-    j->r->p.spp = std::min(left, j->params.samples_per_pass);
-    illume_render_stats s{};
-    const int st = j->r->render_device(j->spp_done > 0, &s);
-    if (st != ILLUME_OK) {
-      j->state = 4;
-      j->error = last_error();
-      reserved -= j->footprint;
-      j->r.reset();
-      continue;
+  return ILLUME_OK;
+}
+
+// Splits `cap` path slots between jobs of npix[i] pixels with left[i] samples to go:
+// one sample of every pixel each (the caller guarantees that these fit), then the rest
+// in equal shares, repeatedly, capped by each job's remaining samples.
+void plan_shares(const std::vector<long long>& npix, const std::vector<int>& left, long long cap,
+                 std::vector<int>* out) {
+  const size_t n = npix.size();
+  std::vector<int>& pp = *out;
+  pp.assign(n, 1);
+  long long R = cap;
+  for (size_t i = 0; i < n; ++i) R -= npix[i];
+  for (int iter = 0; iter < 64 && R > 0; ++iter) {
+    int want = 0;
+    for (size_t i = 0; i < n; ++i) want += pp[i] < left[i] && npix[i] <= R;
+    if (!want) break;
+    const long long share = R / want;
+    bool progress = false;
+    for (size_t i = 0; i < n; ++i) {
+      if (pp[i] >= left[i] || npix[i] > R) continue;
+      const long long add = std::min<long long>(std::max<long long>(share / npix[i], 1), left[i] - pp[i]);
+      if (add * npix[i] > R) continue;
+      pp[i] += (int)add;
+      R -= add * npix[i];
+      progress = true;
     }
-    j->spp_done += j->r->p.spp;
-    j->stats.rays += s.rays;
-    j->stats.paths += s.paths;
-    j->stats.render_ms += s.render_ms;
-    j->stats.kernel_launches += s.kernel_launches;
-    if (j->spp_done >= j->params.spp) {
-      const size_t n = 3 * (size_t)j->r->npix;
-      j->mean.resize(n);
-      j->rgb8.resize(n);
-      j->r->p.spp = j->params.spp;
-      const int rs = j->r->read(j->mean.data(), nullptr, nullptr, j->rgb8.data());
-      j->state = rs == ILLUME_OK ? 2 : 4;
-      j->finish_ms = now_ms();
-      j->stats.total_ms = j->finish_ms - j->submit_ms;
-      reserved -= j->footprint;
-      j->r.reset();
+    if (!progress) break;
+  }
+}
+
+void Server::rebalance(ServerEngine& se) {
+  Engine& e = *se.eng;
+  std::vector<int> live, left, pp;
+  std::vector<long long> npix;
+  long long need = 0;
+  for (int r = 0; r < e.rows; ++r) {
+    const JobDesc& J = e.mirror[r];
+    if (se.row_job[r] && J.nsamples > 0) {
+      live.push_back(r);
+      npix.push_back(J.npix);
+      left.push_back(J.sample_end - J.sample_base);
+      need += J.npix;
     }
   }
-  running = 0;
+  if (live.empty() || need > e.cap) return;
+  plan_shares(npix, left, e.cap, &pp);
+  for (size_t i = 0; i < live.size(); ++i) {
+    JobDesc& J = e.mirror[live[i]];
+    const int ns = std::min(pp[i], left[i]);
+    if (J.per_pass != pp[i] || J.nsamples != ns) {
+      J.per_pass = pp[i];
+      J.nsamples = ns;
+      e.write_pass_state(live[i]);
+    }
+  }
+}
+
+// Jobs whose rows went idle: tonemap, copy out, free the row and the buffers.
+int Server::retire(ServerEngine& se, std::vector<ServerJob*>* done) {
+  Engine& e = *se.eng;
+  cudaStream_t st = ctx->stream;
+  std::vector<std::pair<int, unsigned long long>> rays;
+  for (int r = 0; r < e.rows; ++r) {
+    if (!se.row_job[r] || e.mirror[r].nsamples > 0) continue;
+    ServerJob* j = jobs[se.row_job[r]].get();
+    const illume_render_params& p = j->params;
+    const int npix = p.width * p.height;
+    Accumulators acc{};
+    acc.sum32 = j->sum32.as<float>();
+    acc.comp32 = j->comp32.as<float>();
+    acc.sum64 = j->sum64.as<double>();
+    launch_tonemap(acc, p.accum_mode, npix, (float)std::max(p.spp, 1), p.tonemapper, j->out_rgb8.as<uint8_t>(),
+                   j->out_mean.as<float>(), st);
+    ILLUME_CUDA_TRY(cudaGetLastError());
+    j->mean.resize(3 * (size_t)npix);
+    j->rgb8.resize(3 * (size_t)npix);
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(j->mean.data(), j->out_mean.get(), sizeof(float) * j->mean.size(),
+                                    cudaMemcpyDeviceToHost, st));
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(j->rgb8.data(), j->out_rgb8.get(), j->rgb8.size(), cudaMemcpyDeviceToHost, st));
+    unsigned long long n = 0;
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&n, reinterpret_cast<const char*>(e.w.jobs + r) + offsetof(JobDesc, rays), 8,
+                                    cudaMemcpyDeviceToHost, st));
+    ILLUME_CUDA_TRY(cudaStreamSynchronize(st));
+    j->stats.rays = (int64_t)n;
+    j->stats.paths = (int64_t)p.spp * npix;
+    j->stats.d2h_bytes = (int64_t)(j->mean.size() * sizeof(float) + j->rgb8.size());
+    j->sum32.release();
+    j->comp32.release();
+    j->sum64.release();
+    j->out_mean.release();
+    j->out_rgb8.release();
+    reserved -= j->footprint;
+    se.row_job[r] = 0;
+    e.mirror[r] = JobDesc{};
+    j->row = -1;
+    j->state = 2;
+    done->push_back(j);
+  }
+  return ILLUME_OK;
+}
+
+int Server::apply_candidate(ServerEngine& se, int idx) {
+  Engine& e = *se.eng;
+  const int cap = se.candidates[idx].first;
+  long long min_paths = 0;
+  for (int r = 0; r < e.rows; ++r)
+    if (se.row_job[r]) min_paths += e.mirror[r].npix;
+  if (min_paths > cap) return ILLUME_ERR_INVALID;
+  std::string err;
+  int st = e.resize(cap, &err);
+  if (st != ILLUME_OK) { set_error(err); return st; }
+  return e.set_trace_variant(se.candidates[idx].second);
+}
+
+// Online autotuner: every candidate runs a window of steps on the live jobs; the rate
+// of the window's steps after the first (rays per device ms) decides.
+void Server::tune(ServerEngine& se, double rays, double ms) {
+  static constexpr int kWindow = 3;
+  if (se.tune_state == 0) {
+    for (int cap : {1 << 21, 1 << 22, 1 << 23}) {
+      if (budget && reserved + engines_bytes() - se.eng->device_bytes() + (size_t)cap * kBytesPerPath > budget) continue;
+      for (int v = 0; v < 2; ++v) se.candidates.push_back({cap, v});
+    }
+    se.rate.assign(se.candidates.size(), 0.0);
+    se.tune_state = 1;
+    se.tune_idx = -1;
+  } else {
+    ++se.tune_steps;
+    if (se.tune_steps > 1) { se.tune_rays += rays; se.tune_ms += ms; }
+    if (se.tune_steps < kWindow) return;
+    se.rate[se.tune_idx] = se.tune_ms > 0 ? se.tune_rays / se.tune_ms : 0.0;
+  }
+  // next candidate that fits the running jobs
+  for (++se.tune_idx; se.tune_idx < (int)se.candidates.size(); ++se.tune_idx)
+    if (apply_candidate(se, se.tune_idx) == ILLUME_OK) break;
+  if (se.tune_idx < (int)se.candidates.size()) {
+    se.tune_rays = se.tune_ms = 0;
+    se.tune_steps = 0;
+    return;
+  }
+  int best = -1;
+  for (size_t i = 0; i < se.rate.size(); ++i)
+    if (se.rate[i] > 0 && (best < 0 || se.rate[i] > se.rate[best])) best = (int)i;
+  if (best >= 0) apply_candidate(se, best);
+  se.tune_state = 2;
+}
+
+int Server::step(int* running_out) {
+  if (!ev0) {
+    ILLUME_CUDA_TRY(cudaEventCreate(&ev0));
+    ILLUME_CUDA_TRY(cudaEventCreate(&ev1));
+  }
+  int st = admit();
+  if (st != ILLUME_OK) return st;
+  std::vector<ServerJob*> done;
+  for (auto& kv : engines) {
+    ServerEngine& se = kv.second;
+    Engine& e = *se.eng;
+    if ((st = retire(se, &done)) != ILLUME_OK) return st;   // jobs with no samples
+    rebalance(se);
+    int depth = 0, k = passes_per_step;
+    for (int r = 0; r < e.rows; ++r) {
+      const JobDesc& J = e.mirror[r];
+      if (!se.row_job[r] || J.nsamples <= 0) continue;
+      depth = std::max(depth, J.max_depth);
+      k = std::min(k, (J.sample_end - J.sample_base + J.per_pass - 1) / J.per_pass);
+    }
+    if (depth == 0 && e.paths_in_pass() == 0) continue;
+    k = std::max(k, 1);
+    ILLUME_CUDA_TRY(cudaEventRecord(ev0, ctx->stream));
+    if ((st = e.run(k, depth)) != ILLUME_OK) return st;
+    ILLUME_CUDA_TRY(cudaEventRecord(ev1, ctx->stream));
+    for (int r = 0; r < e.rows; ++r)
+      if (se.row_job[r]) jobs[se.row_job[r]]->stats.kernel_launches += (int64_t)k * Engine::launches_per_pass(depth);
+    unsigned long long total = 0;
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&total, e.w.rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    const double rays = (double)(total - se.rays_seen);
+    se.rays_seen = total;
+    totals.rays += (int64_t)rays;
+    totals.passes += k;
+    totals.kernel_launches += (int64_t)k * Engine::launches_per_pass(depth);
+    totals.device_ms += ms;
+    if ((st = retire(se, &done)) != ILLUME_OK) return st;
+    if (autotune && se.tune_state != 2) tune(se, rays, ms);
+  }
+  const double t = now_ms();
+  for (ServerJob* j : done) {
+    j->finish_ms = t;
+    j->stats.total_ms = t - j->submit_ms;
+    j->stats.render_ms = t - j->start_ms;
+    totals.jobs_done++;
+  }
+  int running = 0;
   for (auto& kv : jobs) running += kv.second->state == 1;
   if (running_out) *running_out = running + (int)queue.size();
   return ILLUME_OK;
@@ -133,12 +374,58 @@ int Server::cancel(int64_t id) {
   if (it == jobs.end()) { set_error("unknown job"); return ILLUME_ERR_INVALID; }
   ServerJob* j = it->second.get();
   if (j->state == 1) {
-    cudaStreamSynchronize(ctx->stream);
+    ServerEngine& se = engines[j->key];
+    se.eng->mirror[j->row].nsamples = 0;
+    se.eng->write_pass_state(j->row);
+    ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    se.row_job[j->row] = 0;
+    se.eng->mirror[j->row] = JobDesc{};
+    j->row = -1;
+    j->sum32.release();
+    j->comp32.release();
+    j->sum64.release();
+    j->out_mean.release();
+    j->out_rgb8.release();
     reserved -= j->footprint;
-    j->r.reset();
   }
   if (j->state <= 1) j->state = 3;
   return ILLUME_OK;
+}
+
+int Server::set_option(int option, int64_t value) {
+  switch (option) {
+    case ILLUME_SERVER_PATH_CAPACITY:
+      if (value < 1 || value > (1 << 30)) { set_error("path capacity out of range"); return ILLUME_ERR_INVALID; }
+      path_capacity = (int)value;
+      return ILLUME_OK;
+    case ILLUME_SERVER_PASSES_PER_STEP:
+      if (value < 1 || value > 1000000) { set_error("passes per step out of range"); return ILLUME_ERR_INVALID; }
+      passes_per_step = (int)value;
+      return ILLUME_OK;
+    case ILLUME_SERVER_AUTOTUNE:
+      autotune = value != 0;
+      return ILLUME_OK;
+    case ILLUME_SERVER_TRACE_VARIANT:
+      if (value < -1 || value > 1) { set_error("unknown trace kernel variant"); return ILLUME_ERR_INVALID; }
+      trace_variant = (int)value;
+      return ILLUME_OK;
+    default:
+      set_error("unknown server option");
+      return ILLUME_ERR_INVALID;
+  }
+}
+
+void Server::get_stats(illume_server_stats* out) const {
+  *out = totals;
+  out->path_capacity = 0;
+  out->trace_variant = -1;
+  out->tuned = 0;
+  for (const auto& kv : engines) {
+    out->path_capacity = std::max<int64_t>(out->path_capacity, kv.second.eng->cap);
+    out->trace_variant = kv.second.eng->knobs.trace_variant;
+    out->tuned |= kv.second.tune_state == 2;
+  }
+  out->device_bytes = (int64_t)(engines_bytes() + reserved);
 }
 
 }  // namespace illume
@@ -148,28 +435,33 @@ extern "C" {
 
 int illume_server_create(illume_context* ctx, size_t hbm_budget_bytes, int max_jobs_in_flight, illume_server** out) {
   if (!ctx || !out) { illume::set_error("null argument"); return ILLUME_ERR_INVALID; }
+  if (max_jobs_in_flight < 0 || max_jobs_in_flight > illume::kMaxJobRows) {
+    illume::set_error("max_jobs_in_flight out of range");
+    return ILLUME_ERR_INVALID;
+  }
   illume_server* s = new illume_server;
   s->s.ctx = &ctx->c;
   s->s.budget = hbm_budget_bytes;
-  s->s.max_in_flight = max_jobs_in_flight > 0 ? max_jobs_in_flight : 8;
+  s->s.rows = max_jobs_in_flight > 0 ? max_jobs_in_flight : 64;
   *out = s;
   return ILLUME_OK;
 }
 
 int illume_server_destroy(illume_server* s) {
   if (!s) return ILLUME_OK;
-  if (s->s.ctx) cudaStreamSynchronize(s->s.ctx->stream);
   delete s;
   return ILLUME_OK;
 }
 
 int illume_job_submit(illume_server* s, illume_scene* scene, const illume_render_params* params, illume_job_id* out) {
   if (!s || !scene || !params || !out) { illume::set_error("null argument"); return ILLUME_ERR_INVALID; }
+  if (scene->s.ctx != s->s.ctx) { illume::set_error("scene was not uploaded with the server's context"); return ILLUME_ERR_INVALID; }
   return s->s.submit(&scene->s, *params, out);
 }
 
 int illume_server_step(illume_server* s, int* jobs_running) {
   if (!s) { illume::set_error("null server"); return ILLUME_ERR_INVALID; }
+  cudaSetDevice(s->s.ctx->device);
   return s->s.step(jobs_running);
 }
 
@@ -181,6 +473,58 @@ int illume_job_poll(illume_server* s, illume_job_id id, float* out_mean, uint8_t
 int illume_job_cancel(illume_server* s, illume_job_id id) {
   if (!s) { illume::set_error("null server"); return ILLUME_ERR_INVALID; }
   return s->s.cancel(id);
+}
+
+int illume_server_set_option(illume_server* s, int option, int64_t value) {
+  if (!s) { illume::set_error("null server"); return ILLUME_ERR_INVALID; }
+  return s->s.set_option(option, value);
+}
+
+int illume_server_get_stats(const illume_server* s, illume_server_stats* out) {
+  if (!s || !out) { illume::set_error("null argument"); return ILLUME_ERR_INVALID; }
+  s->s.get_stats(out);
+  return ILLUME_OK;
+}
+
+int illume_plan_pass_shares(int n, const int32_t* npix, const int32_t* left, int64_t cap, int32_t* per_pass) {
+  if (n < 0 || (n > 0 && (!npix || !left || !per_pass))) { illume::set_error("null argument"); return ILLUME_ERR_INVALID; }
+  std::vector<long long> px(n);
+  std::vector<int> lf(n), pp;
+  long long need = 0;
+  for (int i = 0; i < n; ++i) {
+    if (npix[i] < 1 || left[i] < 1) { illume::set_error("pixels and samples must be positive"); return ILLUME_ERR_INVALID; }
+    px[i] = npix[i];
+    lf[i] = left[i];
+    need += npix[i];
+  }
+  if (need > cap) { illume::set_error("one sample of every job does not fit the path slots"); return ILLUME_ERR_BUDGET; }
+  illume::plan_shares(px, lf, cap, &pp);
+  for (int i = 0; i < n; ++i) per_pass[i] = pp[i];
+  return ILLUME_OK;
+}
+
+int illume_render_batch(illume_context* ctx, int n, illume_scene* const* scenes, const illume_render_params* params,
+                        float* const* out_mean, uint8_t* const* out_rgb8, illume_render_stats* job_stats,
+                        int autotune, illume_server_stats* batch_stats) {
+  if (!ctx || n < 0 || (n > 0 && (!scenes || !params))) { illume::set_error("null argument"); return ILLUME_ERR_INVALID; }
+  illume_server* s = nullptr;
+  int st = illume_server_create(ctx, 0, std::max(1, std::min(n, 1024)), &s);
+  if (st != ILLUME_OK) return st;
+  s->s.autotune = autotune != 0;
+  s->s.passes_per_step = 8;
+  std::vector<illume_job_id> ids(n);
+  for (int i = 0; i < n && st == ILLUME_OK; ++i) {
+    if (!scenes[i]) { illume::set_error("null scene"); st = ILLUME_ERR_INVALID; break; }
+    st = illume_job_submit(s, scenes[i], &params[i], &ids[i]);
+  }
+  int running = n;
+  while (st == ILLUME_OK && running > 0) st = illume_server_step(s, &running);
+  for (int i = 0; i < n && st == ILLUME_OK; ++i)
+    st = s->s.poll(ids[i], out_mean ? out_mean[i] : nullptr, out_rgb8 ? out_rgb8[i] : nullptr,
+                   job_stats ? &job_stats[i] : nullptr);
+  if (st == ILLUME_OK && batch_stats) s->s.get_stats(batch_stats);
+  illume_server_destroy(s);
+  return st;
 }
 
 }  // extern "C"

@@ -1,7 +1,22 @@
-// Render server: admits jobs by device-memory footprint, keeps scenes and accumulators
-// resident, and interleaves progressive sample chunks across the running jobs. A job's
-// image depends only on (scene, params): random numbers are keyed by (pixel, sample,
-// bounce) and (seed, job), never by which jobs share the device.
+// Render server with continuous batching.
+//
+// Jobs share one wavefront job table per trace-kernel setting (intersector, BVH layout):
+// every pass renders the next sample range of every running job together, so a small
+// job's paths fill the slots a large job leaves free and late bounces stay full. A
+// queued job is admitted as soon as a table row, its minimum path share (one sample of
+// every pixel) and its device footprint fit; running jobs split the path slots between
+// them (water-filling), and a job that finishes frees its row and slots for the next
+// pass. Scenes, BVHs and accumulators stay resident on the device between passes.
+//
+// A job's image depends only on its own scene and parameters: random numbers are keyed
+// by (pixel, sample, bounce) and (seed, job), and each pixel's samples are summed in
+// sample order whatever the pass split, so the result is bit-identical alone and in
+// any mix.
+//
+// The autotuner picks the table's path slots and trace kernel variant from measured
+// throughput on the live workload: each candidate runs a few passes of the real jobs
+// (no work is thrown away, since the split of samples into passes and the kernel
+// variant do not change any result), then the fastest is kept.
 #pragma once
 
 #include <deque>
@@ -17,10 +32,11 @@ struct ServerJob {
   int64_t id = 0;
   Scene* scene = nullptr;
   illume_render_params params{};
-  std::unique_ptr<Renderer> r;
+  float camera[15] = {};    // copy of params.camera when given
   int state = 0;            // 0 queued, 1 running, 2 done, 3 cancelled, 4 failed
-  int spp_done = 0;
+  int key = -1, row = -1;   // engine and job-table row while running
   size_t footprint = 0;
+  DevBuffer sum32, comp32, sum64, out_mean, out_rgb8;
   std::vector<float> mean;
   std::vector<uint8_t> rgb8;
   illume_render_stats stats{};
@@ -28,23 +44,55 @@ struct ServerJob {
   double submit_ms = 0, start_ms = 0, finish_ms = 0;
 };
 
+struct ServerEngine {
+  std::unique_ptr<Engine> eng;
+  std::vector<int64_t> row_job;          // job id per row, 0 = free
+  unsigned long long rays_seen = 0;      // engine ray total at the last read
+  // autotuner
+  int tune_state = 0;                    // 0 not started, 1 measuring, 2 done
+  int tune_idx = 0, tune_steps = 0;
+  double tune_rays = 0, tune_ms = 0;
+  std::vector<std::pair<int, int>> candidates;   // (path slots, trace variant)
+  std::vector<double> rate;                      // rays per ms of each candidate
+};
+
 struct Server {
   Context* ctx = nullptr;
-  size_t budget = 0;
-  int max_in_flight = 8;
-  size_t reserved = 0;
+  size_t budget = 0;          // device bytes for engines and job buffers (0 = unlimited)
+  int rows = 64;              // job-table rows per engine
+  int path_capacity = 1 << 22;
+  int passes_per_step = 1;
+  int autotune = 0;
+  int trace_variant = -1;     // -1 = per-layout default
+  size_t reserved = 0;        // job footprints
   int64_t next_id = 1;
   std::map<int64_t, std::unique_ptr<ServerJob>> jobs;
   std::deque<int64_t> queue;
+  std::map<int, ServerEngine> engines;
+  illume_server_stats totals{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
-  static size_t footprint(const illume_render_params& p, int chunk);
-  static int chunk_for(const illume_render_params& p);
+  ~Server();
+  static size_t footprint(const illume_render_params& p);
   int submit(Scene* scene, const illume_render_params& p, int64_t* id);
   int step(int* running);
   int poll(int64_t id, float* mean, uint8_t* rgb8, illume_render_stats* stats);
   int cancel(int64_t id);
+  int set_option(int option, int64_t value);
+  void get_stats(illume_server_stats* out) const;
+
+ private:
+  size_t engines_bytes() const;
+  int admit();
+  void rebalance(ServerEngine& se);
+  int retire(ServerEngine& se, std::vector<ServerJob*>* done);
+  void tune(ServerEngine& se, double rays, double ms);
+  int apply_candidate(ServerEngine& se, int idx);
 };
 
 double now_ms();
+
+void plan_shares(const std::vector<long long>& npix, const std::vector<int>& left, long long cap,
+                 std::vector<int>* per_pass);
 
 }  // namespace illume

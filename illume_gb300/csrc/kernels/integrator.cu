@@ -1,11 +1,14 @@
-// Wavefront integrator stages: camera-ray generation, material-sorted shading,
-// radiance accumulation and tonemapping, plus the BSDF test hook.
+// Wavefront integrator stages over a job table: pass planning, camera-ray generation,
+// material-sorted shading, radiance accumulation, pass advance and tonemapping, plus
+// the BSDF test hook.
 //
-// One pass renders `per_pass` samples of every pixel: raygen fills the bounce-0 queue,
-// then max_depth x (trace, shade), then accumulate and advance. The bounce loop of
-// src/renderer.cu:538-557 (host compaction after every bounce) becomes device-side
-// warp-aggregated appends; the per-path arithmetic is that of pathtrace_kernel
-// (src/renderer.cu:139-388).
+// One pass renders the current sample range of every job in the table: k_plan lays the
+// jobs' paths out in slots, raygen fills the bounce-0 queue, then depth x (trace,
+// shade), then accumulate and advance. The bounce loop of src/renderer.cu:538-557 (host
+// compaction after every bounce) becomes device-side warp-aggregated appends; the
+// per-path arithmetic is that of pathtrace_kernel (src/renderer.cu:139-388). A path
+// depends only on its own job row (scene, camera, Philox key, sample index), never on
+// which other jobs share the pass.
 #include "launch.h"
 #include "shading.cuh"
 #include "../common/philox.cuh"
@@ -14,20 +17,103 @@ namespace illume {
 
 __device__ __forceinline__ int* ev_counts2(const WaveBuffers& w, int parity) { return w.counters + 2 + 16 * parity; }
 
-// init_rays, src/renderer.cu:81-110, for path slots pid = sample_in_pass * npix + pixel.
-__global__ void __launch_bounds__(256) k_raygen(WaveBuffers w, CameraView cam, RenderKnobs k) {
-  const PassState ps = *w.pass;
-  const int npaths = ps.nsamples * w.npix;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    w.counters[0] = npaths;
+// Row of the job table that owns index x of a pass-wide numbering (paths or pixels):
+// the last row whose first index is <= x. Rows with nothing in the pass share their
+// first index with the next row, so the search passes over them.
+__device__ __forceinline__ int find_row(const int* base, int n, int x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(base + mid) <= x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo - 1;
+}
+
+__device__ __forceinline__ float pack_job_medium(int job, int medium) {
+  return __int_as_float((job << kMediumBits) | (medium + 1));
+}
+
+// Prefix sums of the pass's paths and pixels over the job table (one block). A table
+// whose paths would exceed the slot capacity runs no pass and raises counters[42].
+__global__ void __launch_bounds__(1024) k_plan(WaveBuffers w) {
+  const unsigned FULL = 0xffffffffu;
+  __shared__ int wsum[2][32];
+  __shared__ long long carry[2];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  if (tid == 0) carry[0] = carry[1] = 0;
+  __syncthreads();
+  for (int base = 0; base < w.njobs; base += blockDim.x) {
+    const int j = base + tid;
+    int np = 0, nx = 0;
+    if (j < w.njobs) {
+      const int ns = w.jobs[j].nsamples;
+      if (ns > 0) {
+        np = ns * w.jobs[j].npix;
+        nx = w.jobs[j].npix;
+      }
+    }
+    int sp = np, sx = nx;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int a = __shfl_up_sync(FULL, sp, o), b = __shfl_up_sync(FULL, sx, o);
+      if (lane >= o) { sp += a; sx += b; }
+    }
+    if (lane == 31) { wsum[0][wid] = sp; wsum[1][wid] = sx; }
+    __syncthreads();
+    if (wid == 0) {
+      int a = lane < nw ? wsum[0][lane] : 0, b = lane < nw ? wsum[1][lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int c = __shfl_up_sync(FULL, a, o), d = __shfl_up_sync(FULL, b, o);
+        if (lane >= o) { a += c; b += d; }
+      }
+      wsum[0][lane] = a;
+      wsum[1][lane] = b;
+    }
+    __syncthreads();
+    if (j < w.njobs) {
+      const long long pb = carry[0] + (wid > 0 ? wsum[0][wid - 1] : 0) + sp - np;
+      const long long xb = carry[1] + (wid > 0 ? wsum[1][wid - 1] : 0) + sx - nx;
+      const int pbi = pb > w.cap ? w.cap : (int)pb, xbi = xb > w.cap ? w.cap : (int)xb;
+      w.jobs[j].path_base = pbi;
+      w.jobs[j].pixel_base = xbi;
+      w.job_path_base[j] = pbi;
+      w.job_pixel_base[j] = xbi;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      carry[0] += wsum[0][nw - 1];
+      carry[1] += wsum[1][nw - 1];
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    const bool over = carry[0] > (long long)w.cap;
+    const int paths = over ? 0 : (int)carry[0], pixels = over ? 0 : (int)carry[1];
+    w.job_path_base[w.njobs] = paths;
+    w.job_pixel_base[w.njobs] = pixels;
+    w.counters[kCounterPaths] = paths;
+    w.counters[kCounterPixels] = pixels;
+    w.counters[0] = paths;
     w.counters[1] = 0;
+    if (over) w.counters[42] = 1;
     for (int c = 0; c < EV_COUNT; ++c) ev_counts2(w, 0)[c] = 0;
   }
-  for (int pid = blockIdx.x * blockDim.x + threadIdx.x; pid < npaths; pid += gridDim.x * blockDim.x) {
-    const int pixel = pid % w.npix;
-    const int sample = ps.sample_base + pid / w.npix;
+}
+
+// init_rays, src/renderer.cu:81-110, for path slot g of job row j: pid = g - path_base
+// = sample_in_pass * npix + pixel.
+__global__ void __launch_bounds__(256) k_raygen(WaveBuffers w) {
+  const int total = w.counters[kCounterPaths];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    const int j = find_row(w.job_path_base, w.njobs, g);
+    const JobDesc& J = w.jobs[j];
+    const int pid = g - J.path_base;
+    const int npix = J.npix;
+    const int pixel = pid % npix;
+    const int sample = J.sample_base + pid / npix;
+    const CameraView& cam = J.cam;
     RngStream rng;
-    rng.init((uint32_t)pixel, (uint32_t)sample, 0u, k.seed, k.job);
+    rng.init((uint32_t)pixel, (uint32_t)sample, 0u, J.seed, J.job);
     const int x = pixel % cam.width, y = pixel / cam.width;
     const float left_edge = cam.left + cam.pixel_size * (float)x;
     const float top_edge = cam.top - cam.pixel_size * (float)y;
@@ -41,10 +127,10 @@ __global__ void __launch_bounds__(256) k_raygen(WaveBuffers w, CameraView cam, R
     const V3 origin = xform(cam.m, pos, 1.0f);
     const V3 image_pos = xform(cam.m, v3(r_x, r_y, cam.dof), 1.0f);
     const V3 dir = normalize(sub(image_pos, origin));
-    w.q_orig[0][pid] = make_float4(origin.x, origin.y, origin.z, __int_as_float(pid));
-    w.q_dir[0][pid] = make_float4(dir.x, dir.y, dir.z, __int_as_float(-1));
-    w.q_thr[0][pid] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    w.contrib[pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    w.q_orig[0][g] = make_float4(origin.x, origin.y, origin.z, __int_as_float(g));
+    w.q_dir[0][g] = make_float4(dir.x, dir.y, dir.z, pack_job_medium(j, -1));
+    w.q_thr[0][g] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    w.contrib[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
 }
 
@@ -54,7 +140,7 @@ struct BounceRng {
 };
 
 // Shading of one bounce over the material-sorted event queues.
-__global__ void __launch_bounds__(128) k_shade(WaveBuffers w, SceneView sc, RenderKnobs k, int bounce) {
+__global__ void __launch_bounds__(128) k_shade(WaveBuffers w, int bounce) {
   const int parity = bounce & 1;
   const int* counts = ev_counts2(w, parity);
   __shared__ int prefix[EV_COUNT + 1];
@@ -70,43 +156,51 @@ __global__ void __launch_bounds__(128) k_shade(WaveBuffers w, SceneView sc, Rend
     atomicAdd(w.rays, (unsigned long long)w.counters[parity]);
   }
   const int total = prefix[EV_COUNT];
-  const int sample_base = w.pass->sample_base;
   int* next_count = w.counters + (parity ^ 1);
-  const float bias = k.ray_bias;
   for (int base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
-    const int g = base + threadIdx.x;
+    const int gi = base + threadIdx.x;
     bool cont = false;
+    int myjob = -1;
     float4 no = make_float4(0, 0, 0, 0), nd = no, nt = no;
-    if (g < total) {
+    const unsigned live = __ballot_sync(0xffffffffu, gi < total);
+    if (gi < total) {
       int cls = 0;
-      while (cls + 1 < EV_COUNT && g >= prefix[cls + 1]) ++cls;
-      const int i = w.evq[(size_t)cls * w.cap + (g - prefix[cls])];
+      while (cls + 1 < EV_COUNT && gi >= prefix[cls + 1]) ++cls;
+      const int i = w.evq[(size_t)cls * w.cap + (gi - prefix[cls])];
       const float4 qo = w.q_orig[parity][i];
       const float4 qd = w.q_dir[parity][i];
       const float4 qt = w.q_thr[parity][i];
       const float4 hv = w.hit[i];
       const int geom = w.hit_geom[i];
-      const int pid = __float_as_int(qo.w);
-      int medium = __float_as_int(qd.w);
+      const int g = __float_as_int(qo.w);
+      const int packed = __float_as_int(qd.w);
+      const int job = packed >> kMediumBits;
+      myjob = job;
+      int medium = (packed & ((1 << kMediumBits) - 1)) - 1;
+      const JobDesc& J = w.jobs[job];
+      const SceneView sc = J.sc;
+      const int pid = g - J.path_base;
+      const int npix = J.npix;
       const V3 o = v3(qo.x, qo.y, qo.z), d = v3(qd.x, qd.y, qd.z);
       V3 thr = v3(qt.x, qt.y, qt.z);
       const float t = hv.x;
       BounceRng rng;
-      rng.s.init((uint32_t)(pid % w.npix), (uint32_t)(sample_base + pid / w.npix), (uint32_t)(bounce + 1), k.seed,
-                 k.job);
-      float4* contrib = w.contrib + pid;
+      rng.s.init((uint32_t)(pid % npix), (uint32_t)(J.sample_base + pid / npix), (uint32_t)(bounce + 1), J.seed,
+                 J.job);
+      float4* contrib = w.contrib + g;
+      const bool last = bounce + 1 >= J.max_depth;
       if (medium >= 0 && sc.mediums[medium].active) {
         const DevMedium md = sc.mediums[medium];
         const float u = rng();
         const float dist = -logf(u) / md.scattering;
         if (cls == EV_MEDIUM) {
           const float u1 = rng(), u2 = rng();
-          const V3 dir = to_basis(sample_hg(md.g, u1, u2, k.exact_hg != 0), d);
+          const V3 dir = to_basis(sample_hg(md.g, u1, u2, J.exact_hg != 0), d);
           const V3 no3 = add(o, mul(d, dist));
           const V3 nd3 = normalize(dir);
           thr = mulv(thr, v3(expf(-1.0f * dist * md.absorption[0]), expf(-1.0f * dist * md.absorption[1]),
                              expf(-1.0f * dist * md.absorption[2])));
-          if (!((double)length2(thr) < 1e-4)) {
+          if (!((double)length2(thr) < 1e-4) && !last) {
             cont = true;
             no = make_float4(no3.x, no3.y, no3.z, qo.w);
             nd = make_float4(nd3.x, nd3.y, nd3.z, qd.w);
@@ -172,18 +266,22 @@ __global__ void __launch_bounds__(128) k_shade(WaveBuffers w, SceneView sc, Rend
           *contrib = make_float4(L.x, L.y, L.z, 0.0f);
           goto done;
         }
+        if (last) goto done;   // the path has used all its closest-hit queries
         const ScatterResult s = scatter(mat, d, N, albedo, roughness, rng);
         if (s.status == SCATTER_KILLED) goto done;
         if (s.medium != kMediumUnchanged) medium = s.medium;
         thr = mulv(thr, s.weight);
-        const V3 p = add(add(o, mul(d, t)), mul(s.offset_dir, s.offset_sign * bias));
+        const V3 p = add(add(o, mul(d, t)), mul(s.offset_dir, s.offset_sign * J.ray_bias));
         const V3 dir = normalize(s.dir);
         cont = true;
         no = make_float4(p.x, p.y, p.z, qo.w);
-        nd = make_float4(dir.x, dir.y, dir.z, __int_as_float(medium));
+        nd = make_float4(dir.x, dir.y, dir.z, pack_job_medium(job, medium));
         nt = make_float4(thr.x, thr.y, thr.z, 0.0f);
       }
     done:;
+      // closest-hit queries of this bounce, per job
+      const unsigned peers = __match_any_sync(live, myjob);
+      if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&w.jobs[myjob].rays, (unsigned long long)__popc(peers));
     }
     // compacted append of the continuing paths into the next bounce's queue
     const unsigned ballot = __ballot_sync(0xffffffffu, cont);
@@ -203,11 +301,16 @@ __global__ void __launch_bounds__(128) k_shade(WaveBuffers w, SceneView sc, Rend
   }
 }
 
-// Adds the pass's per-path radiance into the per-pixel accumulators, sample by sample
-// in sample order (deterministic), in the selected precision.
-__global__ void __launch_bounds__(256) k_accumulate(WaveBuffers w, Accumulators acc, int mode) {
-  const int ns = w.pass->nsamples;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < w.npix; p += gridDim.x * blockDim.x) {
+// Adds the pass's per-path radiance into each job's per-pixel accumulators, sample by
+// sample in sample order (deterministic), in the job's precision.
+__global__ void __launch_bounds__(256) k_accumulate(WaveBuffers w) {
+  const int total = w.counters[kCounterPixels];
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < total; x += gridDim.x * blockDim.x) {
+    const int j = find_row(w.job_pixel_base, w.njobs, x);
+    const JobDesc& J = w.jobs[j];
+    const int p = x - J.pixel_base;
+    const int ns = J.nsamples, npix = J.npix, mode = J.accum_mode, path_base = J.path_base;
+    const Accumulators acc = J.acc;
     float s32[3], c32[3];
     double s64[3], q64[3];
     for (int c = 0; c < 3; ++c) {
@@ -217,7 +320,7 @@ __global__ void __launch_bounds__(256) k_accumulate(WaveBuffers w, Accumulators 
       q64[c] = acc.sumsq ? acc.sumsq[3 * p + c] : 0.0;
     }
     for (int s = 0; s < ns; ++s) {
-      const float4 L = w.contrib[(size_t)s * w.npix + p];
+      const float4 L = w.contrib[path_base + (size_t)s * npix + p];
       const float l[3] = {L.x, L.y, L.z};
       for (int c = 0; c < 3; ++c) {
         if (mode == ACCUM_FP32) {
@@ -243,10 +346,15 @@ __global__ void __launch_bounds__(256) k_accumulate(WaveBuffers w, Accumulators 
   }
 }
 
-__global__ void k_advance_pass(PassState* ps) {
-  ps->sample_base += ps->nsamples;
-  const int left = ps->sample_end - ps->sample_base;
-  ps->nsamples = left < ps->per_pass ? (left > 0 ? left : 0) : ps->per_pass;
+// Moves every job row to its next sample range.
+__global__ void k_advance(JobDesc* jobs, int njobs) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= njobs) return;
+  JobDesc& J = jobs[j];
+  if (J.nsamples <= 0) return;
+  J.sample_base += J.nsamples;
+  const int left = J.sample_end - J.sample_base;
+  J.nsamples = left < J.per_pass ? (left > 0 ? left : 0) : J.per_pass;
 }
 
 // Tonemap of mean radiance: src/renderer.cu:426-441 and src/tonemapper.cu:32-76.
@@ -352,17 +460,18 @@ __global__ void k_bsdf_batch(int type, int dist, const float* in, int n, float* 
 
 const void* shade_kernel_ptr() { return (const void*)k_shade; }
 
-void launch_raygen(const WaveBuffers& w, const CameraView& cam, const RenderKnobs& k, int grid, cudaStream_t st) {
-  k_raygen<<<grid, 256, 0, st>>>(w, cam, k);
+void launch_plan(const WaveBuffers& w, cudaStream_t st) {
+  const int threads = w.njobs >= 1024 ? 1024 : ((w.njobs + 31) / 32) * 32;
+  k_plan<<<1, threads > 32 ? threads : 32, 0, st>>>(w);
 }
-void launch_shade(const WaveBuffers& w, const SceneView& sc, const RenderKnobs& k, int bounce, int grid,
-                  cudaStream_t st) {
-  k_shade<<<grid, 128, 0, st>>>(w, sc, k, bounce);
+void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st) { k_raygen<<<grid, 256, 0, st>>>(w); }
+void launch_shade(const WaveBuffers& w, int bounce, int grid, cudaStream_t st) {
+  k_shade<<<grid, 128, 0, st>>>(w, bounce);
 }
-void launch_accumulate(const WaveBuffers& w, const Accumulators& acc, int mode, int grid, cudaStream_t st) {
-  k_accumulate<<<grid, 256, 0, st>>>(w, acc, mode);
+void launch_accumulate(const WaveBuffers& w, int grid, cudaStream_t st) { k_accumulate<<<grid, 256, 0, st>>>(w); }
+void launch_advance(const WaveBuffers& w, cudaStream_t st) {
+  k_advance<<<(w.njobs + 255) / 256, 256, 0, st>>>(w.jobs, w.njobs);
 }
-void launch_advance_pass(const WaveBuffers& w, cudaStream_t st) { k_advance_pass<<<1, 1, 0, st>>>(w.pass); }
 void launch_tonemap(const Accumulators& acc, int mode, int npix, float samples, int op, uint8_t* rgb8, float* mean,
                     cudaStream_t st) {
   const int grid = (npix + 255) / 256;

@@ -1,4 +1,9 @@
 // Host-side launchers of the sm_103a kernels (defined in the .cu files of this folder).
+//
+// Every wavefront pass runs over a table of jobs. A job is one render (scene, camera,
+// Philox key, depth, accumulators, sample range); a plain render is a table of one job.
+// The device advances each job's sample range after every pass, so a captured pass can
+// be replayed any number of times without the host.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -8,40 +13,6 @@
 
 namespace illume {
 
-// Device-side pass bookkeeping, advanced by the last kernel of every wavefront pass so
-// that a captured pass can be replayed without host involvement.
-struct PassState {
-  int sample_base;   // first sample index of the current pass
-  int nsamples;      // samples of every pixel in the current pass
-  int sample_end;    // one past the last sample of the render
-  int per_pass;      // samples per pass
-};
-
-// Wavefront buffers. Queues are double-buffered by bounce parity.
-struct WaveBuffers {
-  float4* q_orig[2];     // origin xyz, path id (int bits)
-  float4* q_dir[2];      // direction xyz, medium index (int bits, -1 = air)
-  float4* q_thr[2];      // throughput xyz
-  float4* hit;           // t, u, v, prim (int bits), per slot of the current queue
-  int* hit_geom;         // instance >= 0, sphere -2 - s, miss -1
-  int* evq;              // EV_COUNT queues of `cap` slot indices each
-  int* counters;         // [0..1] queue sizes, [2 + 16 * parity + class] event counts
-  float4* contrib;       // per path radiance of the current pass (sample-major)
-  unsigned long long* rays;   // closest-hit queries traced (running total)
-  unsigned long long* visits; // [node fetches, triangle tests] of the instrumented trace kernel
-  PassState* pass;
-  int cap;               // path slots (pixels * samples per pass)
-  int npix, width, height;
-};
-
-struct RenderKnobs {
-  uint32_t seed, job;
-  int max_depth;
-  float ray_bias;
-  int isect, exact_hg, bvh_kind, accum_mode;
-  int trace_variant;   // 8-wide BVH: 0 = persistent state machine, 1 = one ray per lane to completion
-};
-
 struct Accumulators {
   float* sum32;          // FP32 / Kahan sum (3 per pixel)
   float* comp32;         // Kahan compensation (3 per pixel)
@@ -49,22 +20,81 @@ struct Accumulators {
   double* sumsq;         // sum of squares of per-sample radiance (3 per pixel), nullable
 };
 
+// One row of the job table (256 bytes).
+struct JobDesc {
+  SceneView sc;
+  CameraView cam;
+  Accumulators acc;
+  uint32_t seed, job;        // Philox key
+  int max_depth;             // closest-hit queries per path
+  float ray_bias;
+  int exact_hg, accum_mode;
+  int npix, width;
+  // pass state: samples [sample_base, sample_base + nsamples) of every pixel are in the
+  // current pass; advanced by k_advance after every pass; nsamples == 0 = idle row
+  int sample_base, nsamples, sample_end, per_pass;
+  int path_base;             // first path slot of this job in the current pass (k_plan)
+  int pixel_base;            // first index of this job's pixels in the accumulation sweep (k_plan)
+  unsigned long long rays;   // closest-hit queries traced for this job (running total)
+};
+static_assert(sizeof(JobDesc) == 256, "JobDesc layout");
+
+// A queued ray's fourth direction word packs its job row and medium:
+// (job << kMediumBits) | (medium + 1), medium -1 = air.
+static constexpr int kMediumBits = 12;
+static constexpr int kMaxMediums = (1 << kMediumBits) - 2;
+static constexpr int kMaxJobRows = 1 << 18;
+
+// Wavefront buffers. Queues are double-buffered by bounce parity; a path's slot in the
+// current pass indexes its radiance in `contrib`.
+struct WaveBuffers {
+  float4* q_orig[2];     // origin xyz, path slot (int bits)
+  float4* q_dir[2];      // direction xyz, packed job / medium (int bits)
+  float4* q_thr[2];      // throughput xyz
+  float4* hit;           // t, u, v, prim (int bits), per slot of the current queue
+  int* hit_geom;         // instance >= 0, sphere -2 - s, miss -1
+  int* evq;              // EV_COUNT queues of `cap` slot indices each
+  int* counters;         // see kCounter* below
+  float4* contrib;       // per path radiance of the current pass
+  unsigned long long* rays;   // closest-hit queries traced (running total)
+  unsigned long long* visits; // [node fetches, triangle tests] of the instrumented trace kernel
+  JobDesc* jobs;
+  int* job_path_base;    // njobs + 1 prefix sums of the pass's paths (k_plan)
+  int* job_pixel_base;   // njobs + 1 prefix sums of the pass's pixels (k_plan)
+  int njobs;
+  int cap;               // path slots
+};
+
+// counters[]: [0..1] queue sizes by parity, [2 + 16 * parity + class] event counts,
+// [kCounterPaths] paths of the pass, [kCounterPixels] pixels of the pass.
+static constexpr int kCounterPaths = 40;
+static constexpr int kCounterPixels = 41;
+static constexpr int kCounterWords = 64;
+
+// Settings shared by every job of a table (they select kernel instances).
+struct RenderKnobs {
+  int isect;           // illume_intersector
+  int bvh_kind;        // BVH_BINARY or BVH_WIDE8
+  int trace_variant;   // see trace_kernel_ptr
+};
+
 int kernel_grid_blocks(const void* fn, int block, int device);
 
-void launch_raygen(const WaveBuffers& w, const CameraView& cam, const RenderKnobs& k, int grid, cudaStream_t st);
-void launch_trace(const WaveBuffers& w, const SceneView& sc, const RenderKnobs& k, int bounce, int grid,
-                  cudaStream_t st, bool count_visits = false);
-void launch_shade(const WaveBuffers& w, const SceneView& sc, const RenderKnobs& k, int bounce, int grid,
-                  cudaStream_t st);
-void launch_accumulate(const WaveBuffers& w, const Accumulators& acc, int accum_mode, int grid, cudaStream_t st);
-void launch_advance_pass(const WaveBuffers& w, cudaStream_t st);
+void launch_plan(const WaveBuffers& w, cudaStream_t st);
+void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st);
+void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st,
+                  bool count_visits = false);
+void launch_shade(const WaveBuffers& w, int bounce, int grid, cudaStream_t st);
+void launch_accumulate(const WaveBuffers& w, int grid, cudaStream_t st);
+void launch_advance(const WaveBuffers& w, cudaStream_t st);
 void launch_tonemap(const Accumulators& acc, int accum_mode, int npix, float samples, int op, uint8_t* rgb8,
                     float* mean, cudaStream_t st);
 void launch_clear_accumulators(const Accumulators& acc, int npix, cudaStream_t st);
 
 // test hooks
-void launch_trace_hook(const SceneView& sc, const float* rays8, int n, int isect, int bvh_kind, void* hits,
-                       cudaStream_t st);
+// d_view: a device copy of sc (read by the persistent 8-wide kernel, bvh_kind 2)
+void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float* rays8, int n, int isect,
+                       int bvh_kind, void* hits, cudaStream_t st);
 void launch_bsdf_batch(int type, int distribution, const float* in, int n, float* out, cudaStream_t st);
 
 const void* trace_kernel_ptr(int bvh_kind, int variant = 0);

@@ -32,7 +32,7 @@ namespace illume {
 static constexpr size_t kNoAllocMaxPaths = ILLUME_NOALLOC_MAX_PIXELS;
 static constexpr size_t kNoAllocPerPath = 6 * sizeof(float4) + sizeof(float4) + sizeof(int) + EV_COUNT * sizeof(int) +
                                           sizeof(float4);
-static constexpr size_t kNoAllocScratchBytes = kNoAllocMaxPaths * kNoAllocPerPath + 4096;
+static constexpr size_t kNoAllocScratchBytes = kNoAllocMaxPaths * kNoAllocPerPath + 8192;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -40,18 +40,15 @@ static std::mutex g_noalloc_mu;
 static void* g_noalloc_ptr[256];
 
 // Clears what must start at zero (counters, ray and visit totals, the output sums) and
-// sets the pass state for the first sample.
-__global__ void k_noalloc_begin(int* counters, unsigned long long* rays, unsigned long long* visits, PassState* ps,
-                                float* sum, int npix, int sample_begin, int spp) {
+// writes the one-row job table.
+__global__ void k_noalloc_begin(int* counters, unsigned long long* rays, unsigned long long* visits, JobDesc* job,
+                                JobDesc row, float* sum, int npix) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < 64) counters[i] = 0;
+  if (i < kCounterWords) counters[i] = 0;
   if (i == 0) {
     *rays = 0;
     visits[0] = visits[1] = 0;
-    ps->sample_base = sample_begin;
-    ps->per_pass = 1;
-    ps->sample_end = sample_begin + spp;
-    ps->nsamples = spp > 0 ? 1 : 0;
+    *job = row;
   }
   for (int k = i; k < 3 * npix; k += gridDim.x * blockDim.x) sum[k] = 0.0f;
 }
@@ -110,46 +107,46 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
   w.hit_geom = reinterpret_cast<int*>(carve(cur, sizeof(int) * cap));
   w.evq = reinterpret_cast<int*>(carve(cur, sizeof(int) * (size_t)cap * EV_COUNT));
   w.contrib = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
-  w.counters = reinterpret_cast<int*>(carve(cur, sizeof(int) * 64));
+  w.counters = reinterpret_cast<int*>(carve(cur, sizeof(int) * kCounterWords));
   w.rays = reinterpret_cast<unsigned long long*>(carve(cur, 8));
   w.visits = reinterpret_cast<unsigned long long*>(carve(cur, 16));
-  w.pass = reinterpret_cast<PassState*>(carve(cur, sizeof(PassState)));
+  w.jobs = reinterpret_cast<JobDesc*>(carve(cur, sizeof(JobDesc)));
+  w.job_path_base = reinterpret_cast<int*>(carve(cur, 2 * sizeof(int)));
+  w.job_pixel_base = reinterpret_cast<int*>(carve(cur, 2 * sizeof(int)));
   if ((size_t)(cur - static_cast<unsigned char*>(base)) > kNoAllocScratchBytes) {
     set_error("scratch layout exceeds the fixed array");
     return ILLUME_ERR_INVALID;
   }
   w.cap = cap;
-  w.npix = cap;
-  w.width = p.width;
-  w.height = p.height;
+  w.njobs = 1;
   Accumulators acc{};
   acc.sum32 = d_sum;
+  JobDesc row = job_row(scene->s, p, acc);
+  row.sample_base = p.sample_begin;
+  row.sample_end = p.sample_begin + p.spp;
+  row.per_pass = 1;
+  row.nsamples = p.spp > 0 ? 1 : 0;
   RenderKnobs k{};
-  k.seed = p.seed;
-  k.job = p.job;
-  k.max_depth = p.max_depth;
-  k.ray_bias = p.ray_bias;
   k.isect = p.intersector;
-  k.exact_hg = p.exact_hg;
   k.bvh_kind = p.bvh_kind;
-  k.accum_mode = ILLUME_ACCUM_FP32;
-  const CameraView cam = make_camera(scene->s.host, p.width, p.height);
+  k.trace_variant = 0;
   cudaStream_t st = ctx->c.stream;
   const int sms = ctx->c.sm_count > 0 ? ctx->c.sm_count : 1;
-  const int grid_trace = kernel_grid_blocks(trace_kernel_ptr(p.bvh_kind), 128, dev);
+  const int grid_trace = kernel_grid_blocks(trace_kernel_ptr(p.bvh_kind, 0), 128, dev);
   const int grid_shade = kernel_grid_blocks(shade_kernel_ptr(), 128, dev);
   const int grid_small = std::max(1, std::min((cap + 255) / 256, sms * 8));
-  k_noalloc_begin<<<grid_small, 256, 0, st>>>(w.counters, w.rays, w.visits, w.pass, d_sum, cap, p.sample_begin, p.spp);
+  k_noalloc_begin<<<grid_small, 256, 0, st>>>(w.counters, w.rays, w.visits, w.jobs, row, d_sum, cap);
   for (int s = 0; s < p.spp; ++s) {
-    launch_raygen(w, cam, k, grid_small, st);
+    launch_plan(w, st);
+    launch_raygen(w, grid_small, st);
     for (int b = 0; b < p.max_depth; ++b) {
-      launch_trace(w, scene->s.view, k, b, grid_trace, st);
-      launch_shade(w, scene->s.view, k, b, grid_shade, st);
+      launch_trace(w, k, b, grid_trace, st);
+      launch_shade(w, b, grid_shade, st);
     }
-    launch_accumulate(w, acc, ILLUME_ACCUM_FP32, grid_small, st);
-    launch_advance_pass(w, st);
+    launch_accumulate(w, grid_small, st);
+    launch_advance(w, st);
   }
   ILLUME_CUDA_TRY(cudaGetLastError());
-  ctx->c.launches += 1 + (long long)p.spp * (3 + 2 * p.max_depth);
+  ctx->c.launches += 1 + (long long)p.spp * (4 + 2 * p.max_depth);
   return ILLUME_OK;
 }

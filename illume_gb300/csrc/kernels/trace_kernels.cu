@@ -21,17 +21,31 @@ __device__ __forceinline__ int warp_append_keyed(unsigned mask, int key, int* co
   return base + __popc(peers & ((1u << lane) - 1));
 }
 
-// Trace stage of one bounce: closest hit of every queued ray, then the event class
-// (escape, medium scatter before the surface, or the hit material) and an append of the
-// ray's slot to that class's queue. The medium decision uses the first number of the
-// path's bounce stream, as src/renderer.cu:152-157 does.
+// Event class of a traced ray: escape, medium scatter before the surface, or the hit
+// material. The medium decision uses the first number of the path's bounce stream, as
+// src/renderer.cu:152-157 does.
+__device__ __forceinline__ int event_class(const WaveBuffers& w, const JobDesc& J, const SceneView& sc,
+                                           const HitRecord& h, int g, int medium, int bounce) {
+  if (medium >= 0 && sc.mediums[medium].active) {
+    const int pid = g - J.path_base;
+    const uint32_t pixel = (uint32_t)(pid % J.npix), sample = (uint32_t)(J.sample_base + pid / J.npix);
+    const Philox4 r = philox4x32_10(pixel, sample, (uint32_t)(bounce + 1), 0u, J.seed, J.job);
+    const float dist = -logf(philox_unit(r.x)) / sc.mediums[medium].scattering;
+    if (dist < h.t) return EV_MEDIUM;
+  }
+  if (h.geom == -1) return EV_MISS;
+  const int mat = h.geom >= 0 ? sc.instances[h.geom].material : sc.spheres[-2 - h.geom].material;
+  return EV_SURFACE + sc.materials[mat].type;
+}
+
+// Trace stage of one bounce: closest hit of every queued ray in its job's scene, then
+// an append of the ray's queue position to its event class's queue.
 template <int KIND, bool COUNT, int MINB = 1>
-__global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, SceneView sc, RenderKnobs k, int bounce) {
+__global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
   const int parity = bounce & 1;
   const int n = w.counters[parity];
   if (blockIdx.x == 0 && threadIdx.x == 0) w.counters[parity ^ 1] = 0;
   int* counts = ev_counts(w, parity);
-  const int sample_base = w.pass->sample_base;
   typename std::conditional<KIND == BVH_WIDE8, uint2, int>::type stack[kStack];
   unsigned long long my_nodes = 0, my_tris = 0;
   for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
@@ -41,26 +55,13 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, SceneView sc
     if (!valid) continue;
     const float4 qo = w.q_orig[parity][i];
     const float4 qd = w.q_dir[parity][i];
+    const int packed = __float_as_int(qd.w);
+    const JobDesc& J = w.jobs[packed >> kMediumBits];
+    const SceneView& sc = J.sc;
     VisitCount vc;
     const HitRecord h = closest_hit<KIND, COUNT>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack, &vc);
     if (COUNT) { my_nodes += vc.nodes; my_tris += vc.tris; }
-    int cls;
-    const int medium = __float_as_int(qd.w);
-    bool scattered = false;
-    if (medium >= 0 && sc.mediums[medium].active) {
-      const int pid = __float_as_int(qo.w);
-      const uint32_t pixel = (uint32_t)(pid % w.npix), sample = (uint32_t)(sample_base + pid / w.npix);
-      const Philox4 r = philox4x32_10(pixel, sample, (uint32_t)(bounce + 1), 0u, k.seed, k.job);
-      const float u = philox_unit(r.x);
-      const float dist = -logf(u) / sc.mediums[medium].scattering;
-      scattered = dist < h.t;
-    }
-    if (scattered) cls = EV_MEDIUM;
-    else if (h.geom == -1) cls = EV_MISS;
-    else {
-      const int mat = h.geom >= 0 ? sc.instances[h.geom].material : sc.spheres[-2 - h.geom].material;
-      cls = EV_SURFACE + sc.materials[mat].type;
-    }
+    const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
     w.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
     w.hit_geom[i] = h.geom;
     const int pos = warp_append_keyed(mask, cls, counts);
@@ -88,18 +89,19 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, SceneView sc
 enum { PH_IDLE = 0, PH_INST = 1, PH_TRAV = 2, PH_DONE = 3 };
 
 template <bool COUNT, bool HOOK>
-__global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, SceneView sc, RenderKnobs k, int bounce,
+__global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, const SceneView* hook_view, RenderKnobs k, int bounce,
                                                   const float4* hook_rays, int hook_n, illume_hit* hook_out) {
   const unsigned FULL = 0xffffffffu;
   const int parity = bounce & 1;
   const int n = HOOK ? hook_n : w.counters[parity];
   if (!HOOK && blockIdx.x == 0 && threadIdx.x == 0) w.counters[parity ^ 1] = 0;
   int* counts = HOOK ? nullptr : ev_counts(w, parity);
-  const int sample_base = HOOK ? 0 : w.pass->sample_base;
   const int stride = gridDim.x * blockDim.x;
   int next = blockIdx.x * blockDim.x + threadIdx.x;
   uint2 stack[kStack];
-  int slot = -1, phase = PH_IDLE, inst = 0, pid = 0, medium = -1, steps = 0;
+  int slot = -1, phase = PH_IDLE, inst = 0, g = 0, medium = -1, steps = 0;
+  const SceneView* scp = hook_view;
+  const JobDesc* jp = nullptr;
   V3 o = v3(0.0f, 0.0f, 0.0f), d = v3(0.0f, 0.0f, 1.0f);
   HitRecord h;
   h.t = FLT_MAX; h.u = h.v = 0.0f; h.prim = -1; h.geom = -1;
@@ -120,12 +122,15 @@ __global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, SceneView sc, R
         const float4 qo = w.q_orig[parity][slot], qd = w.q_dir[parity][slot];
         o = v3(qo.x, qo.y, qo.z);
         d = v3(qd.x, qd.y, qd.z);
-        pid = __float_as_int(qo.w);
-        medium = __float_as_int(qd.w);
+        g = __float_as_int(qo.w);
+        const int packed = __float_as_int(qd.w);
+        jp = w.jobs + (packed >> kMediumBits);
+        scp = &jp->sc;
+        medium = (packed & ((1 << kMediumBits) - 1)) - 1;
       }
       h.t = FLT_MAX; h.u = h.v = 0.0f; h.prim = -1; h.geom = -1;
-      for (int sidx = 0; sidx < sc.num_spheres; ++sidx) {
-        const DevSphere sp = sc.spheres[sidx];
+      for (int sidx = 0; sidx < scp->num_spheres; ++sidx) {
+        const DevSphere sp = scp->spheres[sidx];
         const V3 l = sub(v3(sp.cx, sp.cy, sp.cz), o);
         const float sd = dot(l, d), ls = dot(l, l), rs = sp.r * sp.r;
         if (sd < 0.0f && ls > rs) continue;
@@ -143,8 +148,8 @@ __global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, SceneView sc, R
     }
     if (__all_sync(FULL, phase == PH_IDLE)) break;
     if (phase == PH_INST) {
-      while (inst < sc.num_instances) {
-        const DevInstance& in = sc.instances[inst];
+      while (inst < scp->num_instances) {
+        const DevInstance& in = scp->instances[inst];
         float te;
         if (box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) {
           setup_ray(r, xform(in.inv, o, 1.0f), xform(in.inv, d, 0.0f), k.isect);
@@ -166,7 +171,7 @@ __global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, SceneView sc, R
     if (want_tri | want_node) {
       const bool do_tri = __popc(want_tri) >= __popc(want_node);
       if (trav) {
-        const DevMesh& m = sc.meshes[sc.instances[inst].mesh];
+        const DevMesh& m = scp->meshes[scp->instances[inst].mesh];
         if (do_tri) {
           if (has_tri) wide_tri_step<COUNT>(m, r, k.isect, b, s, vc);
         } else if (has_node) {
@@ -195,20 +200,7 @@ __global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, SceneView sc, R
         out.pad[0] = out.pad[1] = 0;
         hook_out[slot] = out;
       } else {
-        int cls;
-        bool scattered = false;
-        if (medium >= 0 && sc.mediums[medium].active) {
-          const uint32_t pixel = (uint32_t)(pid % w.npix), sample = (uint32_t)(sample_base + pid / w.npix);
-          const Philox4 rr = philox4x32_10(pixel, sample, (uint32_t)(bounce + 1), 0u, k.seed, k.job);
-          const float dist = -logf(philox_unit(rr.x)) / sc.mediums[medium].scattering;
-          scattered = dist < h.t;
-        }
-        if (scattered) cls = EV_MEDIUM;
-        else if (h.geom == -1) cls = EV_MISS;
-        else {
-          const int mat = h.geom >= 0 ? sc.instances[h.geom].material : sc.spheres[-2 - h.geom].material;
-          cls = EV_SURFACE + sc.materials[mat].type;
-        }
+        const int cls = event_class(w, *jp, *scp, h, g, medium, bounce);
         w.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
         w.hit_geom[slot] = h.geom;
         const int pos = warp_append_keyed(fin, cls, counts);
@@ -251,39 +243,39 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 }
 
 // Trace kernel variants (RenderKnobs::trace_variant):
-//   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine;
-//   binary BVH: 0 = compiler's register choice, 1 = at most 64 registers (8 blocks per SM).
+//   binary BVH: 0 = at most 64 registers (8 blocks of 128 per SM), 1 = compiler's register choice;
+//   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine.
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (bvh_kind == BVH_WIDE8)
     return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
-  return variant == 1 ? (const void*)k_trace<BVH_BINARY, false, 8> : (const void*)k_trace<BVH_BINARY, false>;
+  return variant == 1 ? (const void*)k_trace<BVH_BINARY, false> : (const void*)k_trace<BVH_BINARY, false, 8>;
 }
 
-void launch_trace(const WaveBuffers& w, const SceneView& sc, const RenderKnobs& k, int bounce, int grid,
-                  cudaStream_t st, bool count_visits) {
+void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st,
+                  bool count_visits) {
   if (k.bvh_kind == BVH_WIDE8) {
     if (k.trace_variant == 1) {
-      if (count_visits) k_trace_sm<true, false><<<grid, 128, 0, st>>>(w, sc, k, bounce, nullptr, 0, nullptr);
-      else k_trace_sm<false, false><<<grid, 128, 0, st>>>(w, sc, k, bounce, nullptr, 0, nullptr);
+      if (count_visits) k_trace_sm<true, false><<<grid, 128, 0, st>>>(w, nullptr, k, bounce, nullptr, 0, nullptr);
+      else k_trace_sm<false, false><<<grid, 128, 0, st>>>(w, nullptr, k, bounce, nullptr, 0, nullptr);
     } else {
-      if (count_visits) k_trace<BVH_WIDE8, true><<<grid, 128, 0, st>>>(w, sc, k, bounce);
-      else k_trace<BVH_WIDE8, false><<<grid, 128, 0, st>>>(w, sc, k, bounce);
+      if (count_visits) k_trace<BVH_WIDE8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE8, false><<<grid, 128, 0, st>>>(w, k, bounce);
     }
     return;
   }
   if (k.trace_variant == 1) {
-    if (count_visits) k_trace<BVH_BINARY, true, 8><<<grid, 128, 0, st>>>(w, sc, k, bounce);
-    else k_trace<BVH_BINARY, false, 8><<<grid, 128, 0, st>>>(w, sc, k, bounce);
+    if (count_visits) k_trace<BVH_BINARY, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    else k_trace<BVH_BINARY, false><<<grid, 128, 0, st>>>(w, k, bounce);
     return;
   }
-  if (count_visits) k_trace<BVH_BINARY, true><<<grid, 128, 0, st>>>(w, sc, k, bounce);
-  else k_trace<BVH_BINARY, false><<<grid, 128, 0, st>>>(w, sc, k, bounce);
+  if (count_visits) k_trace<BVH_BINARY, true, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+  else k_trace<BVH_BINARY, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
 }
 
-void launch_trace_hook(const SceneView& sc, const float* rays8, int n, int isect, int bvh_kind, void* hits,
-                       cudaStream_t st) {
+void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float* rays8, int n, int isect,
+                       int bvh_kind, void* hits, cudaStream_t st) {
   if (n <= 0) return;
-  if (bvh_kind == 2) {  // 8-wide BVH through the persistent state machine (internal test path)
+  if (bvh_kind == 2) {  // 8-wide BVH through the persistent state machine
     int dev = 0;
     cudaGetDevice(&dev);
     const int cap = kernel_grid_blocks((const void*)k_trace_sm<false, true>, 128, dev);
@@ -292,7 +284,7 @@ void launch_trace_hook(const SceneView& sc, const float* rays8, int n, int isect
     RenderKnobs k{};
     k.isect = isect;
     k.bvh_kind = BVH_WIDE8;
-    k_trace_sm<false, true><<<grid, 128, 0, st>>>(w, sc, k, 0, (const float4*)rays8, n, (illume_hit*)hits);
+    k_trace_sm<false, true><<<grid, 128, 0, st>>>(w, d_view, k, 0, (const float4*)rays8, n, (illume_hit*)hits);
     return;
   }
   const int grid = (n + 127) / 128;

@@ -278,3 +278,156 @@ def sss_scene(tris: int = 700_000, seed: int = 3, width: int = 960, height: int 
     M[:, 3] = (277.5, 140.0, 277.5)
     s.add_instance(m, glass, M)
     return s
+
+
+# ---------------------------------------------------------------- batched and served workloads
+def random_rotation(rng) -> np.ndarray:
+    """Uniform random rotation (unit quaternion from four normals)."""
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def mixed_material(s: SceneData, rng) -> int:
+    """One of: lambert (albedo U[0.1, 0.9]), GGX rough dielectric (alpha U[0.05, 0.5],
+    ior 1.5), smooth plastic (ior 1.5, diffuse U[0.1, 0.9]), rough copper (GGX alpha
+    U[0.05, 0.5])."""
+    kind = int(rng.integers(4))
+    if kind == 0:
+        return s.add_material(Material(C.MAT_LAMBERT, s.constant(rng.uniform(0.1, 0.9, 3)), s.constant((1e-4,) * 3)))
+    if kind == 1:
+        a = float(rng.uniform(0.05, 0.5))
+        return s.add_material(Material(C.MAT_ROUGHREFRACTIVE, s.constant((1, 1, 1)), s.constant((a, a, a)), ior=1.5,
+                                       distribution=C.DIST_GGX))
+    if kind == 2:
+        return s.add_material(Material(C.MAT_PLASTIC, s.constant(rng.uniform(0.1, 0.9, 3)), s.constant((1e-4,) * 3),
+                                       ior=1.5))
+    a = float(rng.uniform(0.05, 0.5))
+    return s.add_material(Material(C.MAT_ROUGHCONDUCTOR, s.constant((0, 0, 0)), s.constant((a, a, a)),
+                                   eta=COPPER_ETA, k=COPPER_K, distribution=C.DIST_GGX))
+
+
+class MeshPool:
+    """Displaced icospheres of `count` sizes log-uniformly spaced in [lo, hi] triangles
+    (distinct seeds); instances draw a log-uniform size and take the nearest pool mesh."""
+
+    def __init__(self, count: int = 16, lo: int = 5_000, hi: int = 700_000, seed: int = 2):
+        self.sizes = np.exp(np.linspace(math.log(lo), math.log(hi), count))
+        self.lo, self.hi, self.seed = lo, hi, seed
+        self.meshes = {}
+
+    def get(self, k: int):
+        if k not in self.meshes:
+            self.meshes[k] = displaced_icosphere(freq_for_tris(int(self.sizes[k])), self.seed * 1000 + k)
+        return self.meshes[k]
+
+    def draw(self, rng) -> int:
+        n = math.exp(rng.uniform(math.log(self.lo), math.log(self.hi)))
+        return int(np.argmin(np.abs(np.log(self.sizes) - math.log(n))))
+
+
+def scene_bounds(s: SceneData):
+    lo, hi = np.full(3, np.inf), np.full(3, -np.inf)
+    for (m, _, M, _, _) in s.instances:
+        P = s.meshes[m].positions.astype(np.float64) @ M[:, :3].T.astype(np.float64) + M[:, 3]
+        lo, hi = np.minimum(lo, P.min(0)), np.maximum(hi, P.max(0))
+    for (c, r, _) in s.spheres:
+        lo, hi = np.minimum(lo, np.array(c) - r), np.maximum(hi, np.array(c) + r)
+    return lo, hi
+
+
+def batch_jobs(n: int = 64, seed: int = 2, pool: MeshPool = None, env=None, depth: int = 15,
+               resolutions=(128, 256, 512, 1024), spp_range=(64, 1024)):
+    """Uneven jobs: resolution uniform in `resolutions` (square), spp uniform in spp_range,
+    1-8 displaced icospheres (5k-700k triangles, log-uniform, from a mesh pool) with random
+    affine transforms (uniform rotation, scale U[0.5, 2], translation in a 10-unit box),
+    mixed materials, the traversal scene's environment map. Returns [(SceneData, dict)]
+    with the render settings of each job (width, height, spp, max_depth, seed, job)."""
+    rng = np.random.default_rng(seed)
+    pool = pool or MeshPool(seed=seed)
+    env = environment_map(1) if env is None else env
+    out = []
+    for j in range(n):
+        s = SceneData()
+        res = int(rng.choice(resolutions))
+        spp = int(rng.integers(spp_range[0], spp_range[1] + 1))
+        ninst = int(rng.integers(1, 9))
+        used = {}
+        for _ in range(ninst):
+            k = pool.draw(rng)
+            if k not in used:
+                P, T = pool.get(k)
+                used[k] = s.add_mesh(Mesh(P, T))
+            M = np.zeros((3, 4))
+            M[:, :3] = random_rotation(rng) * rng.uniform(0.5, 2.0)
+            M[:, 3] = rng.uniform(-5.0, 5.0, 3)
+            s.add_instance(used[k], mixed_material(s, rng), M.astype(np.float32))
+        s.env_tex = s.add_texture(Texture(C.TEX_BITMAP, texels=env, hdr=1))
+        lo, hi = scene_bounds(s)
+        c = 0.5 * (lo + hi)
+        radius = 0.5 * float(np.linalg.norm(hi - lo))
+        s.camera_transform = lookat(c + np.array([0.0, 0.35, -1.0]) / np.linalg.norm([0.0, 0.35, -1.0]) * 2.6 * radius, c)
+        s.camera_fov, s.camera_dof, s.camera_aperture = 40.0, 1.0, 0.0
+        s.width = s.height = res
+        s.ray_bias = 1e-3
+        s.tonemapper = C.TONE_LINEAR
+        out.append((s, dict(width=res, height=res, spp=spp, max_depth=depth, seed=seed, job=j)))
+    return out
+
+
+def instanced_scene(count: int = 16, tris: int = 125_000, seed: int = 5, env=None) -> SceneData:
+    """`count` distinct displaced icospheres of ~`tris` triangles each on a 4-wide grid
+    (spacing 3, uniform random rotations), mixed materials, environment lighting."""
+    rng = np.random.default_rng(seed)
+    s = SceneData()
+    f = freq_for_tris(tris)
+    for i in range(count):
+        P, T = displaced_icosphere(f, seed * 1000 + i)
+        m = s.add_mesh(Mesh(P, T))
+        M = np.zeros((3, 4))
+        M[:, :3] = random_rotation(rng)
+        M[:, 3] = (3.0 * (i % 4) - 4.5, 0.0, 3.0 * (i // 4) - 4.5)
+        s.add_instance(m, mixed_material(s, rng), M.astype(np.float32))
+    s.env_tex = s.add_texture(Texture(C.TEX_BITMAP, texels=environment_map(1) if env is None else env, hdr=1))
+    s.camera_transform = lookat((0.0, 8.0, -14.0), (0.0, 0.0, 0.0))
+    s.width, s.height = 1024, 1024
+    s.ray_bias = 1e-3
+    return s
+
+
+def orbit_camera(s: SceneData, rng, fov: float = 40.0) -> np.ndarray:
+    """15 floats (camera rows, fov, dof, aperture) of a camera on an orbit around the
+    scene: azimuth U[0, 2 pi), elevation U[5, 60] degrees, radius 3x the scene radius."""
+    lo, hi = scene_bounds(s)
+    c = 0.5 * (lo + hi)
+    radius = 0.5 * float(np.linalg.norm(hi - lo))
+    az = rng.uniform(0.0, 2 * math.pi)
+    el = math.radians(rng.uniform(5.0, 60.0))
+    pos = c + 3.0 * radius * np.array([math.cos(el) * math.cos(az), math.sin(el), math.cos(el) * math.sin(az)])
+    out = np.zeros(15, np.float32)
+    out[:12] = lookat(pos, c).reshape(-1)
+    out[12], out[13], out[14] = fov, 1.0, 0.0
+    return out
+
+
+def request_stream(n: int, scenes: int, seed: int = 4, rate: float = 40.0, max_res=(1920, 1080), min_res=64,
+                   spp_range=(16, 4096), depth_range=(10, 25)):
+    """Seeded Poisson arrivals (mean `rate` per second). Each request: scene index,
+    resolution log-uniform between min_res^2 and max_res (one draw scales both sides),
+    spp log-uniform in spp_range, depth uniform in depth_range, an orbit-pose seed."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        a = rng.uniform()
+        w = int(round(min_res * (max_res[0] / min_res) ** a))
+        h = int(round(min_res * (max_res[1] / min_res) ** a))
+        spp = int(round(math.exp(rng.uniform(math.log(spp_range[0]), math.log(spp_range[1])))))
+        depth = int(rng.integers(depth_range[0], depth_range[1] + 1))
+        out.append(dict(arrival=t, scene=int(rng.integers(scenes)), width=w, height=h, spp=spp, max_depth=depth,
+                        pose_seed=int(rng.integers(1 << 30)), job=i))
+    return out

@@ -148,7 +148,11 @@ typedef struct {
   int32_t bvh_kind;           /* illume_bvh_kind */
   int32_t exact_hg;           /* 0 = reference Henyey-Greenstein sampler, 1 = exact */
   int32_t samples_per_pass;   /* samples of every pixel kept in flight per wavefront pass (0 = auto) */
-  int32_t reserved[6];
+  /* Nullable camera override, read when a renderer is created or a job is submitted: 12
+   * floats of the camera-to-world rows (3x4, the layout of illume_scene_desc's
+   * camera_transform), then fov (degrees), dof and aperture. NULL = the scene's camera. */
+  const float* camera;
+  int32_t reserved[4];        /* reserved[0]: binary-BVH trace kernel variant (0 default, 1 other) */
 } illume_render_params;
 
 typedef struct {
@@ -201,6 +205,11 @@ int illume_scene_upload(illume_scene* scene, size_t* bytes);
  * boxes inside their parent's, quantised boxes containing the exact boxes) and writes a
  * one-line summary per mesh (node counts, depths) into report. */
 int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t report_len);
+/* Process-wide cache of mesh BVH builds, keyed by mesh content (vertex and index words):
+ * scenes that share a mesh build it once. Not in the reference, which caches one BVH
+ * file per OBJ path (src/accel/bvh.cpp:363-439). */
+int illume_bvh_cache_stats(int64_t* entries, int64_t* bytes, int64_t* hits, int64_t* misses);
+int illume_bvh_cache_clear(void);
 int illume_scene_destroy(illume_scene* scene);
 
 /* ---- renderer ---- */
@@ -279,18 +288,67 @@ int illume_trace_closest_device(illume_context* ctx, illume_scene* scene, const 
 int illume_bsdf_batch(illume_context* ctx, int material_type, int distribution, const float* inputs, int n,
                       float* outputs);
 
-/* ---- batched and served rendering ---- */
+/* ---- batched and served rendering ----
+ * Not in the reference, which renders one scene per call (src/renderer.cu:498-597).
+ * Jobs with the same intersector and BVH layout share one wavefront job table: every
+ * pass advances all running jobs, jobs are admitted while they run (continuous
+ * batching), and each job's image is bit-identical to its render alone. */
 typedef struct illume_server illume_server;
 typedef int64_t illume_job_id;
+/* max_jobs_in_flight: job-table rows (0 = 64). hbm_budget_bytes gates admission by the
+ * server's device bytes (job accumulators and output staging plus the tables' path
+ * buffers; scenes are the caller's and not counted); 0 = unlimited. */
 int illume_server_create(illume_context* ctx, size_t hbm_budget_bytes, int max_jobs_in_flight, illume_server** out);
 int illume_server_destroy(illume_server* s);
-/* Admit a job when its footprint fits the budget (ILLUME_ERR_BUDGET if it never can). */
+/* Queue a job (ILLUME_ERR_BUDGET if its footprint can never fit the budget). The
+ * server ignores params->samples_per_pass and the binary-kernel variant word. */
 int illume_job_submit(illume_server* s, illume_scene* scene, const illume_render_params* params, illume_job_id* out);
-/* Advance the server by one scheduling round (one wavefront pass over all running jobs). */
+/* One scheduling round: admit what fits, rebalance path slots, run up to
+ * ILLUME_SERVER_PASSES_PER_STEP wavefront passes (fewer if a job finishes sooner),
+ * retire finished jobs. *jobs_running = running + queued jobs afterwards. */
 int illume_server_step(illume_server* s, int* jobs_running);
-/* ILLUME_OK when done (results copied to the nullable buffers), ILLUME_ERR_NOT_READY otherwise. */
+/* ILLUME_OK when done (results copied to the nullable buffers), ILLUME_ERR_NOT_READY
+ * otherwise. stats: rays of this job, paths, render_ms = submit-to-finish minus queue
+ * wait (wall), total_ms = submit to finish (wall), kernel_launches of the passes the
+ * job took part in. */
 int illume_job_poll(illume_server* s, illume_job_id id, float* out_mean, uint8_t* out_rgb8, illume_render_stats* stats);
+/* Cancels a queued or running job (its row and buffers are freed before the next pass);
+ * a finished job keeps its results. */
 int illume_job_cancel(illume_server* s, illume_job_id id);
+
+typedef enum {
+  ILLUME_SERVER_PATH_CAPACITY = 0,    /* path slots of each job table (default 4194304) */
+  ILLUME_SERVER_PASSES_PER_STEP = 1,  /* passes per illume_server_step (default 1) */
+  ILLUME_SERVER_AUTOTUNE = 2,         /* 1 = choose path slots and trace kernel from measured throughput */
+  ILLUME_SERVER_TRACE_VARIANT = 3     /* trace kernel variant (-1 = default) */
+} illume_server_option;
+int illume_server_set_option(illume_server* s, int option, int64_t value);
+
+typedef struct {
+  int64_t rays;               /* closest-hit queries traced by all jobs */
+  int64_t passes;             /* wavefront passes run */
+  int64_t kernel_launches;
+  int64_t jobs_done;
+  double device_ms;           /* device time of the passes (CUDA events) */
+  int64_t path_capacity;      /* path slots per table in use */
+  int32_t trace_variant;      /* trace kernel variant in use */
+  int32_t tuned;              /* 1 once the autotuner has chosen */
+  int64_t device_bytes;       /* bytes the server holds on the device */
+} illume_server_stats;
+int illume_server_get_stats(const illume_server* s, illume_server_stats* out);
+
+/* The server's split of `cap` path slots between n running jobs of npix[i] pixels with
+ * left[i] samples to go (host only; exposed for tests and schedulers): per_pass[i] >= 1
+ * samples of job i go into each pass, sum(per_pass[i] * npix[i]) <= cap.
+ * ILLUME_ERR_BUDGET when one sample of every job does not fit. */
+int illume_plan_pass_shares(int n, const int32_t* npix, const int32_t* left, int64_t cap, int32_t* per_pass);
+
+/* Renders n jobs together through one server (all submitted at once) and returns each
+ * job's mean radiance (3 floats per pixel) and RGB8 in the nullable per-job buffers.
+ * autotune: see ILLUME_SERVER_AUTOTUNE. batch_stats is nullable. */
+int illume_render_batch(illume_context* ctx, int n, illume_scene* const* scenes, const illume_render_params* params,
+                        float* const* out_mean, uint8_t* const* out_rgb8, illume_render_stats* job_stats,
+                        int autotune, illume_server_stats* batch_stats);
 
 #ifdef __cplusplus
 }

@@ -1,7 +1,7 @@
-"""Served rendering: jobs admitted by device-memory footprint, progressive samples
-interleaved across running jobs; every job's image is the same alone and in the mix."""
-import ctypes
-
+"""Batched and served rendering on the GPU: jobs share one wavefront job table (continuous
+batching), and every job's image is bit-identical to its render alone, whatever the mix,
+the admission order, the split of path slots, the autotuner's choices or cancellations
+around it."""
 import numpy as np
 import pytest
 
@@ -10,84 +10,124 @@ from illume_gb300 import _capi as C
 pytestmark = pytest.mark.gpu
 
 
-def make_server(ctx, budget=0, slots=8):
-    s = ctypes.c_void_p()
-    C.check(C.lib().illume_server_create(ctx.handle, budget, slots, ctypes.byref(s)))
-    return s
-
-
-def run_all(server, ids, npix):
-    L = C.lib()
-    running = ctypes.c_int(1)
-    steps = 0
-    while running.value:
-        C.check(L.illume_server_step(server, ctypes.byref(running)))
-        steps += 1
-        assert steps < 10000
-    out = {}
-    for j, n in zip(ids, npix):
-        m = np.zeros((n, 3), np.float32)
-        st = C.RenderStats()
-        C.check(L.illume_job_poll(server, j, C.fptr(m), None, ctypes.byref(st)))
-        out[j] = (m, st)
-    return out
-
-
-def params(scene, w, h, spp, depth, seed=0, job=0):
+def params(scene, w, h, spp, depth, seed=0, job=0, accum=C.ACCUM_FP32):
     p = scene.default_params(spp, depth)
-    p.width, p.height, p.seed, p.job = w, h, seed, job
+    p.width, p.height, p.seed, p.job, p.accum_mode = w, h, seed, job, accum
     return p
 
 
-def test_same_alone_and_in_the_mix(ctx):
+@pytest.fixture(scope="module")
+def scenes(ctx):
     from illume_gb300 import synth
     from illume_gb300.api import HostScene
-    L = C.lib()
     a = HostScene.from_data(ctx, synth.cornell_scene(48, 48))
     b = HostScene.from_data(ctx, synth.traversal_scene(tris=5000, env_size=(64, 32), width=64, height=48))
-    jobs = [(a, params(a, 48, 48, 40, 8, seed=1, job=1)), (b, params(b, 64, 48, 24, 12, seed=2, job=2)),
-            (a, params(a, 32, 24, 64, 6, seed=3, job=3))]
-    alone = []
-    for sc, p in jobs:
-        srv = make_server(ctx)
-        jid = ctypes.c_int64()
-        C.check(L.illume_job_submit(srv, sc.handle, ctypes.byref(p), ctypes.byref(jid)))
-        alone.append(run_all(srv, [jid.value], [p.width * p.height])[jid.value][0])
-        L.illume_server_destroy(srv)
-    srv = make_server(ctx)
-    ids = []
-    for sc, p in jobs:
-        jid = ctypes.c_int64()
-        C.check(L.illume_job_submit(srv, sc.handle, ctypes.byref(p), ctypes.byref(jid)))
-        ids.append(jid.value)
-    mixed = run_all(srv, ids, [p.width * p.height for _, p in jobs])
-    for k, j in enumerate(ids):
-        assert np.array_equal(mixed[j][0], alone[k]), k
-        assert mixed[j][1].rays > 0
-    L.illume_server_destroy(srv)
+    return a, b
 
 
-def test_budget_admission_and_cancel(ctx):
-    from illume_gb300 import synth
-    from illume_gb300.api import HostScene
-    L = C.lib()
-    sc = HostScene.from_data(ctx, synth.cornell_scene(64, 64))
-    p = params(sc, 64, 64, 16, 6)
-    srv = make_server(ctx, budget=1 << 20)   # far below one job's footprint
-    jid = ctypes.c_int64()
-    assert L.illume_job_submit(srv, sc.handle, ctypes.byref(p), ctypes.byref(jid)) == C.ERR_BUDGET
-    L.illume_server_destroy(srv)
-    srv = make_server(ctx, budget=64 << 20, slots=1)
-    ids = []
-    for k in range(3):
-        C.check(L.illume_job_submit(srv, sc.handle, ctypes.byref(p), ctypes.byref(jid)))
-        ids.append(jid.value)
-    C.check(L.illume_job_cancel(srv, ids[1]))
-    running = ctypes.c_int(1)
-    while running.value:
-        C.check(L.illume_server_step(srv, ctypes.byref(running)))
-    m = np.zeros((64 * 64, 3), np.float32)
-    assert L.illume_job_poll(srv, ids[0], C.fptr(m), None, None) == C.OK
-    assert L.illume_job_poll(srv, ids[1], C.fptr(m), None, None) == C.ERR_CANCELLED
-    assert L.illume_job_poll(srv, ids[2], C.fptr(m), None, None) == C.OK
-    L.illume_server_destroy(srv)
+def job_list(scenes):
+    a, b = scenes
+    return [(a, params(a, 48, 48, 40, 8, seed=1, job=1)), (b, params(b, 64, 48, 24, 12, seed=2, job=2)),
+            (a, params(a, 32, 24, 64, 6, seed=3, job=3)), (b, params(b, 40, 40, 9, 20, seed=4, job=4, accum=C.ACCUM_KAHAN)),
+            (a, params(a, 24, 16, 100, 8, seed=5, job=5, accum=C.ACCUM_FP64))]
+
+
+def alone(ctx, sc, p):
+    from illume_gb300.api import Server
+    srv = Server(ctx)
+    j = srv.submit(sc, p)
+    srv.run()
+    out = srv.poll(j, rgb8=True)
+    srv.close()
+    return out
+
+
+def test_same_alone_and_in_the_mix(ctx, scenes):
+    from illume_gb300.api import Server
+    jobs = job_list(scenes)
+    ref = [alone(ctx, sc, p) for sc, p in jobs]
+    for opts in ({}, {"path_capacity": 40000}, {"passes_per_step": 4}, {"trace_variant": 1}):
+        srv = Server(ctx, **opts)
+        ids = [srv.submit(sc, p) for sc, p in jobs]
+        srv.run()
+        for k, j in enumerate(ids):
+            out = srv.poll(j, rgb8=True)
+            assert np.array_equal(out["mean"], ref[k]["mean"]), (opts, k)
+            assert np.array_equal(out["rgb8"], ref[k]["rgb8"]), (opts, k)
+            assert out["stats"].rays == ref[k]["stats"].rays, (opts, k)
+        assert srv.stats().jobs_done == len(jobs)
+        srv.close()
+
+
+def test_server_equals_renderer(ctx, scenes):
+    """A served job's image equals the plain renderer's image of the same parameters."""
+    from illume_gb300.api import Renderer
+    for sc, p in job_list(scenes):
+        r = Renderer(ctx, sc, params=p)
+        want = r.render(mean=True, rgb8=True)
+        got = alone(ctx, sc, p)
+        assert np.array_equal(got["mean"], want["mean"])
+        assert np.array_equal(got["rgb8"], want["rgb8"])
+        assert got["stats"].rays == want["stats"].rays
+
+
+def test_arrivals_while_running_and_cancel(ctx, scenes):
+    """Jobs submitted while others are on the device join the next pass; cancelling a
+    running job leaves the others' images unchanged."""
+    from illume_gb300.api import Server
+    jobs = job_list(scenes)
+    ref = [alone(ctx, sc, p) for sc, p in jobs]
+    a, b = scenes
+    srv = Server(ctx, path_capacity=20000)
+    ids = [srv.submit(*jobs[0]), srv.submit(*jobs[1])]
+    srv.step()
+    victim = srv.submit(b, params(b, 40, 40, 4000, 20, seed=9, job=9))   # far from done when cancelled
+    srv.step()
+    ids.append(srv.submit(*jobs[2]))
+    srv.step()
+    srv.cancel(victim)
+    ids.append(srv.submit(*jobs[4]))
+    srv.run()
+    for k, j in zip([0, 1, 2, 4], ids):
+        out = srv.poll(j, rgb8=True)
+        assert np.array_equal(out["mean"], ref[k]["mean"]), k
+    with pytest.raises(C.IllumeError):
+        srv.poll(victim)
+    srv.close()
+
+
+def test_batch_and_autotune(ctx, scenes):
+    from illume_gb300.api import render_batch
+    jobs = job_list(scenes) * 3
+    ref = [alone(ctx, sc, p) for sc, p in jobs[:5]]
+    for tune in (False, True):
+        means, pix, stats, bs = render_batch(ctx, [s for s, _ in jobs], [p for _, p in jobs], autotune=tune, rgb8=True)
+        for k in range(len(jobs)):
+            assert np.array_equal(means[k], ref[k % 5]["mean"]), (tune, k)
+            assert np.array_equal(pix[k], ref[k % 5]["rgb8"]), (tune, k)
+            assert stats[k].rays == ref[k % 5]["stats"].rays
+        assert bs.jobs_done == len(jobs) and bs.rays == sum(s.rays for s in stats)
+        assert bs.passes > 0 and bs.device_ms > 0
+
+
+def test_budget_admission(ctx, scenes):
+    from illume_gb300.api import Server
+    a, _ = scenes
+    p = params(a, 64, 64, 16, 6)
+    srv = Server(ctx, hbm_budget_bytes=1 << 16)   # below one job's footprint
+    with pytest.raises(C.IllumeError) as e:
+        srv.submit(a, p)
+    assert e.value.status == C.ERR_BUDGET
+    srv.close()
+    # room for one job's buffers and a small table at a time: jobs run one after another
+    srv = Server(ctx, hbm_budget_bytes=16 << 20, max_jobs_in_flight=1, path_capacity=64 * 64 * 4)
+    ids = [srv.submit(a, p) for _ in range(3)]
+    srv.cancel(ids[1])
+    srv.run()
+    m0 = srv.poll(ids[0])["mean"]
+    with pytest.raises(C.IllumeError) as e:
+        srv.poll(ids[1])
+    assert e.value.status == C.ERR_CANCELLED
+    assert np.array_equal(srv.poll(ids[2])["mean"], m0)
+    assert srv.stats().device_bytes <= 16 << 20
+    srv.close()
