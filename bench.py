@@ -51,11 +51,15 @@ def parse():
     ap.add_argument("--bvh", default="binary", choices=["binary", "wide", "wide-persistent"])
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--trace-variant", type=int, default=0,
-                    help="binary traversal: 0 at most 64 registers (8 blocks per SM), 1 compiler register choice")
+                    help="binary traversal: 0 64 registers + fused box tests + dynamic ray fetch (default), "
+                         "1 compiler register choice, 2 variant 1 held to 64 registers")
     ap.add_argument("--tris", type=int, default=100_000)
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--depth", type=int, default=25)
-    ap.add_argument("--workload", default="traversal", choices=["traversal", "batched", "served"],
+    ap.add_argument("--sss-res", type=int, nargs=2, default=[96, 72],
+                    help="sss: image size (the accumulation study needs the per-pixel spp, not the pixels)")
+    ap.add_argument("--sss-spp", type=int, default=20000)
+    ap.add_argument("--workload", default="traversal", choices=["traversal", "batched", "served", "sss"],
                     help="traversal: the headline single-render workload; batched: 64 uneven jobs in one job "
                          "table vs one job at a time; served: Poisson request stream, continuous batching vs "
                          "one request at a time")
@@ -413,9 +417,10 @@ def run_batched(args):
     rays_b = sum(j.rays for j in jstats)
     pl = plain(0)
     pl1 = plain(1) if args.plain_1spp else None
-    same = all(np.array_equal(a, b) for a, b in zip(means_b, pl["means"]))
+    same = all(np.array_equal(a, b, equal_nan=True) for a, b in zip(means_b, pl["means"]))
     if pl1 is not None:
-        same = same and all(np.array_equal(a, b) for a, b in zip(means_b, pl1["means"]))
+        same = same and all(np.array_equal(a, b, equal_nan=True) for a, b in zip(means_b, pl1["means"]))
+    nan_pixels = int(sum(np.isnan(m).any(1).sum() for m in means_b))
     batched_dev = rays_b / (bs.device_ms * 1e-3) / 1e6
     batched_wall = rays_b / wall_b / 1e6
     plain_dev = pl["rays"] / (pl["device_ms"] * 1e-3) / 1e6
@@ -438,7 +443,7 @@ def run_batched(args):
                   "device_s": round(pl["device_ms"] * 1e-3, 3), "wall_s": round(pl["wall_s"], 3),
                   "samples_per_pass": "auto (min(spp, 4M / pixels))"},
         "speedup_device": round(batched_dev / plain_dev, 3), "speedup_wall": round(batched_wall / plain_wall, 3),
-        "images_identical_across_arms": bool(same),
+        "images_identical_across_arms": bool(same), "nan_pixels": nan_pixels,
         "e2e": {"value": round(batched_wall, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(sum(p.width * p.height * 12 for p in params) / max(bs.passes, 1))},
         "gpu_launches": int(bs.kernel_launches),
@@ -530,7 +535,7 @@ def run_served(args):
         finish_p[k] = time.perf_counter() - t0
         rays_p += st.rays
         dev_p += st.render_ms
-        same = same and np.array_equal(m, means_s[k])
+        same = same and np.array_equal(m, means_s[k], equal_nan=True)
     wall_p = max(finish_p.values()) - reqs[0]["arrival"]
     lat_p = [finish_p[k] - reqs[k]["arrival"] for k in range(len(reqs))]
     served = rays_s / wall_s / 1e6
@@ -561,6 +566,73 @@ def run_served(args):
     print(json.dumps(line), flush=True)
 
 
+def run_sss(args):
+    """Accumulation precision at high spp: the subsurface scene (700k-triangle dielectric
+    boundary around a scattering medium in the Cornell box, depth 50) rendered with the
+    FP32, compensated-FP32 and FP64 per-pixel accumulators, both Henyey-Greenstein
+    samplers. Reported per mode: Mrays/s, the accumulation error against the FP64 sum of
+    the same samples (every pixel), and the RMSE against the FP64 host oracle (same
+    Philox streams) on a pixel subset."""
+    import torch
+    import numpy as np
+    from illume_gb300 import _capi as C
+    from illume_gb300 import synth
+    from illume_gb300.api import Context, HostScene, Renderer
+    from oracle import pyoracle
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    W, H = args.sss_res
+    spp, depth = args.sss_spp, 50
+    sd = synth.sss_scene(700_000, seed=3, width=W, height=H)
+    ctx = Context(local)
+    scene = HostScene.from_data(ctx, sd)
+    stride = max(1, (W * H) // 24)
+    subset = np.arange(stride // 2, W * H, stride, dtype=np.int32)
+    out = {"metric": METRIC, "unit": "Mrays/s", "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"subsurface accumulation: 700k-tri dielectric (ior 1.3) around a medium "
+                                  f"(sigma_a 0.01/0.08/0.3, sigma_s 1, g 0.7) in the Cornell box, {W}x{H}, depth "
+                                  f"{depth}, {spp} spp per pixel", "oracle_pixels": int(len(subset))},
+           "modes": {}}
+    mrays0 = None
+    for hg in (0, 1):
+        sums = {}
+        for mode, name in ((C.ACCUM_FP64, "fp64"), (C.ACCUM_KAHAN, "kahan"), (C.ACCUM_FP32, "fp32")):
+            p = scene.default_params(spp, depth)
+            p.width, p.height, p.seed, p.job, p.exact_hg, p.accum_mode = W, H, 7, 0, hg, mode
+            r = Renderer(ctx, scene, params=p)
+            st = r.render_device()
+            sums[name] = r.read(mean=False, sums=True)["sum"]
+            r.close()
+            mr = st.rays / (st.render_ms * 1e-3) / 1e6
+            if mrays0 is None and name == "fp32":
+                mrays0 = (mr, st.render_ms)
+            out["modes"][f"{name}_hg{hg}"] = {"mrays": round(mr, 2), "render_s": round(st.render_ms * 1e-3, 3),
+                                               "rays": int(st.rays)}
+        t0 = time.perf_counter()
+        osum, _, orays = pyoracle.OracleScene(sd).render(W, H, spp, depth, seed=7, job=0, isect=C.ISECT_WATERTIGHT,
+                                                        exact_hg=hg, precision=64, pixels=subset)
+        oracle_s = time.perf_counter() - t0
+        ref = sums["fp64"]
+        scale = np.maximum(np.abs(ref), 1e-6)
+        omean = osum / spp
+        for name in ("fp64", "kahan", "fp32"):
+            m = out["modes"][f"{name}_hg{hg}"]
+            rel = np.abs(sums[name] - ref) / scale
+            m["accum_rel_err_max"] = float(rel.max())
+            m["accum_rel_err_mean"] = float(rel.mean())
+            gm = sums[name][subset] / spp
+            m["rmse_vs_fp64_oracle"] = float(np.sqrt(np.mean((gm - omean) ** 2)))
+            m["rel_rmse_vs_fp64_oracle"] = float(np.sqrt(np.mean((gm - omean) ** 2)) / max(np.mean(np.abs(omean)), 1e-12))
+        out["config"][f"oracle_s_hg{hg}"] = round(oracle_s, 1)
+        out["config"][f"oracle_rays_hg{hg}"] = int(orays)
+    out["value"] = round(mrays0[0], 3)
+    out["ms_per_step"] = round(mrays0[1], 3)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -569,6 +641,8 @@ def main():
         run_batched(args)
     elif args.workload == "served":
         run_served(args)
+    elif args.workload == "sss":
+        run_sss(args)
     else:
         run_ours(args)
 

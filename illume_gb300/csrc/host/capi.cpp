@@ -39,6 +39,7 @@ int illume_context_create(int device, size_t hbm_budget_bytes, illume_context** 
   ctx->c.device = device;
   ctx->c.budget = hbm_budget_bytes;
   ILLUME_CUDA_TRY(cudaDeviceGetAttribute(&ctx->c.sm_count, cudaDevAttrMultiProcessorCount, device));
+  ILLUME_CUDA_TRY(cudaDeviceGetAttribute(&ctx->c.l2_bytes, cudaDevAttrL2CacheSize, device));
   ILLUME_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
   *out = ctx.release();
   return ILLUME_OK;

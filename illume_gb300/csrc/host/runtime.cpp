@@ -377,6 +377,11 @@ int Scene::build_host(std::string* err) {
       return ILLUME_ERR_UNSUPPORTED;
     }
   }
+  trace_bytes[0] = trace_bytes[1] = 0;
+  for (const MeshBvh& b : bvhs) {
+    trace_bytes[0] += b.bvh2.size() * sizeof(Bvh2Node) + b.bvh2_tris.size() * sizeof(float4);
+    trace_bytes[1] += b.wide.size() * sizeof(WideNode) + b.wide_tris.size() * sizeof(float4);
+  }
   build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return ILLUME_OK;
 }

@@ -34,6 +34,7 @@ struct Context {
   size_t budget = 0;                 // 0 = unlimited
   std::atomic<size_t> used{0};
   int sm_count = 0;
+  int l2_bytes = 0;
   std::atomic<long long> launches{0};
 };
 
@@ -100,6 +101,7 @@ struct Scene {
   SceneView view{};
   SceneView* view_dev = nullptr;   // device copy of `view`
   size_t device_bytes = 0;
+  size_t trace_bytes[2] = {0, 0};   // node + triangle bytes a traversal reads: binary, 8-wide
   // device tables (kept for re-uploads) and the host source of every device buffer
   std::vector<DevMesh> t_meshes;
   std::vector<DevInstance> t_instances;

@@ -65,9 +65,9 @@ int Server::submit(Scene* scene, const illume_render_params& p, int64_t* id) {
   return ILLUME_OK;
 }
 
-// Admits queued jobs in arrival order while a row, one sample of every pixel and the
-// job's footprint fit; a job that does not fit yet keeps its place and later jobs may
-// pass it.
+// Admits queued jobs in arrival order while a table row and the job's footprint fit
+// (compose decides which admitted jobs run in each pass); a job that does not fit yet
+// keeps its place and later jobs may pass it.
 int Server::admit() {
   if (budget && !queue.empty()) {
     // under a budget, idle tables give their memory back to the queue
@@ -106,10 +106,9 @@ int Server::admit() {
     ServerEngine& se = eit->second;
     Engine& e = *se.eng;
     int running = 0;
-    long long min_paths = 0;
     int free_row = -1;
     for (int r = 0; r < e.rows; ++r) {
-      if (se.row_job[r]) { ++running; min_paths += e.mirror[r].npix; }
+      if (se.row_job[r]) ++running;
       else if (free_row < 0) free_row = r;
     }
     if (free_row < 0) { ++it; continue; }
@@ -123,7 +122,6 @@ int Server::admit() {
       const int st = e.resize(npix, &err);
       if (st != ILLUME_OK) { set_error(err); return st; }
     }
-    if (min_paths + npix > e.cap) { ++it; continue; }
     if (budget && reserved + engines_bytes() + j->footprint > budget) { ++it; continue; }
     // job buffers
     int st;
@@ -185,40 +183,97 @@ void plan_shares(const std::vector<long long>& npix, const std::vector<int>& lef
   }
 }
 
-void Server::rebalance(ServerEngine& se) {
+// Chooses the jobs of the next passes and splits the path slots between them.
+//
+// Running jobs are grouped by scene, because a pass whose rays traverse one scene's BVH
+// keeps it in L2 while rays of many scenes evict each other. Groups enter the pass in
+// order of their smallest remaining job (remaining paths = pixels x samples to go), so
+// short requests finish first; a group enters while its jobs' one-sample minimum fits
+// the slots and either the traversal data of the groups taken so far plus its own stays
+// within three quarters of L2, or the pass is less than half full. Jobs left out are
+// paused for these passes (no samples); the chosen ones share the slots by water-filling.
+void Server::compose(ServerEngine& se) {
   Engine& e = *se.eng;
-  std::vector<int> live, left, pp;
-  std::vector<long long> npix;
-  long long need = 0;
+  struct Group {
+    Scene* scene;
+    double key;
+    std::vector<int> rows;
+  };
+  std::vector<Group> groups;
+  std::map<Scene*, size_t> index;
   for (int r = 0; r < e.rows; ++r) {
+    if (!se.row_job[r]) continue;
     const JobDesc& J = e.mirror[r];
-    if (se.row_job[r] && J.nsamples > 0) {
-      live.push_back(r);
-      npix.push_back(J.npix);
-      left.push_back(J.sample_end - J.sample_base);
-      need += J.npix;
+    if (J.sample_base >= J.sample_end) continue;
+    ServerJob* j = jobs[se.row_job[r]].get();
+    auto it = index.find(j->scene);
+    if (it == index.end()) {
+      it = index.emplace(j->scene, groups.size()).first;
+      groups.push_back(Group{j->scene, 1e300, {}});
+    }
+    Group& g = groups[it->second];
+    g.key = std::min(g.key, (double)J.npix * (double)(J.sample_end - J.sample_base));
+    g.rows.push_back(r);
+  }
+  std::stable_sort(groups.begin(), groups.end(), [](const Group& a, const Group& b) { return a.key < b.key; });
+  const size_t l2_target = ctx->l2_bytes > 0 ? (size_t)ctx->l2_bytes * 3 / 4 : ((size_t)96 << 20);
+  const int kind = e.knobs.bvh_kind == BVH_WIDE8 ? 1 : 0;
+  std::vector<char> chosen(e.rows, 0);
+  long long paths = 0;
+  size_t bytes = 0;
+  bool any = false;
+  for (Group& g : groups) {
+    const size_t gb = g.scene->trace_bytes[kind];
+    if (any && bytes + gb > l2_target && 2 * paths >= e.cap) continue;
+    // the group's jobs, smallest remaining work first, while one sample of each fits
+    std::stable_sort(g.rows.begin(), g.rows.end(), [&](int a, int b) {
+      const JobDesc &A = e.mirror[a], &B = e.mirror[b];
+      return (double)A.npix * (A.sample_end - A.sample_base) < (double)B.npix * (B.sample_end - B.sample_base);
+    });
+    bool took = false;
+    for (int r : g.rows) {
+      if (paths + e.mirror[r].npix > e.cap) continue;
+      chosen[r] = 1;
+      paths += e.mirror[r].npix;
+      took = true;
+    }
+    if (took) {
+      any = true;
+      bytes += gb;
     }
   }
-  if (live.empty() || need > e.cap) return;
+  std::vector<int> live, left, pp;
+  std::vector<long long> npix;
+  for (int r = 0; r < e.rows; ++r) {
+    if (!chosen[r]) continue;
+    const JobDesc& J = e.mirror[r];
+    live.push_back(r);
+    npix.push_back(J.npix);
+    left.push_back(J.sample_end - J.sample_base);
+  }
   plan_shares(npix, left, e.cap, &pp);
-  for (size_t i = 0; i < live.size(); ++i) {
-    JobDesc& J = e.mirror[live[i]];
-    const int ns = std::min(pp[i], left[i]);
-    if (J.per_pass != pp[i] || J.nsamples != ns) {
-      J.per_pass = pp[i];
+  std::vector<int> want_pp(e.rows, -1);
+  for (size_t i = 0; i < live.size(); ++i) want_pp[live[i]] = pp[i];
+  for (int r = 0; r < e.rows; ++r) {
+    if (!se.row_job[r]) continue;
+    JobDesc& J = e.mirror[r];
+    const int per = want_pp[r] > 0 ? want_pp[r] : J.per_pass;
+    const int ns = want_pp[r] > 0 ? std::min(want_pp[r], J.sample_end - J.sample_base) : 0;
+    if (J.per_pass != per || J.nsamples != ns) {
+      J.per_pass = per;
       J.nsamples = ns;
-      e.write_pass_state(live[i]);
+      e.write_pass_state(r);
     }
   }
 }
 
-// Jobs whose rows went idle: tonemap, copy out, free the row and the buffers.
+// Jobs that have all their samples: tonemap, copy out, free the row and the buffers.
 int Server::retire(ServerEngine& se, std::vector<ServerJob*>* done) {
   Engine& e = *se.eng;
   cudaStream_t st = ctx->stream;
   std::vector<std::pair<int, unsigned long long>> rays;
   for (int r = 0; r < e.rows; ++r) {
-    if (!se.row_job[r] || e.mirror[r].nsamples > 0) continue;
+    if (!se.row_job[r] || e.mirror[r].sample_base < e.mirror[r].sample_end) continue;
     ServerJob* j = jobs[se.row_job[r]].get();
     const illume_render_params& p = j->params;
     const int npix = p.width * p.height;
@@ -259,10 +314,8 @@ int Server::retire(ServerEngine& se, std::vector<ServerJob*>* done) {
 int Server::apply_candidate(ServerEngine& se, int idx) {
   Engine& e = *se.eng;
   const int cap = se.candidates[idx].first;
-  long long min_paths = 0;
   for (int r = 0; r < e.rows; ++r)
-    if (se.row_job[r]) min_paths += e.mirror[r].npix;
-  if (min_paths > cap) return ILLUME_ERR_INVALID;
+    if (se.row_job[r] && e.mirror[r].npix > cap) return ILLUME_ERR_INVALID;
   std::string err;
   int st = e.resize(cap, &err);
   if (st != ILLUME_OK) { set_error(err); return st; }
@@ -274,9 +327,10 @@ int Server::apply_candidate(ServerEngine& se, int idx) {
 void Server::tune(ServerEngine& se, double rays, double ms) {
   static constexpr int kWindow = 3;
   if (se.tune_state == 0) {
-    for (int cap : {1 << 21, 1 << 22, 1 << 23}) {
+    for (int cap : {1 << 22, 1 << 23, 1 << 24}) {
       if (budget && reserved + engines_bytes() - se.eng->device_bytes() + (size_t)cap * kBytesPerPath > budget) continue;
-      for (int v = 0; v < 2; ++v) se.candidates.push_back({cap, v});
+      const int variants = se.eng->knobs.bvh_kind == BVH_BINARY ? 3 : 2;
+      for (int v = 0; v < variants; ++v) se.candidates.push_back({cap, v});
     }
     se.rate.assign(se.candidates.size(), 0.0);
     se.tune_state = 1;
@@ -314,11 +368,13 @@ int Server::step(int* running_out) {
     ServerEngine& se = kv.second;
     Engine& e = *se.eng;
     if ((st = retire(se, &done)) != ILLUME_OK) return st;   // jobs with no samples
-    rebalance(se);
+    compose(se);
     int depth = 0, k = passes_per_step;
+    std::vector<int> active;
     for (int r = 0; r < e.rows; ++r) {
       const JobDesc& J = e.mirror[r];
       if (!se.row_job[r] || J.nsamples <= 0) continue;
+      active.push_back(r);
       depth = std::max(depth, J.max_depth);
       k = std::min(k, (J.sample_end - J.sample_base + J.per_pass - 1) / J.per_pass);
     }
@@ -327,8 +383,7 @@ int Server::step(int* running_out) {
     ILLUME_CUDA_TRY(cudaEventRecord(ev0, ctx->stream));
     if ((st = e.run(k, depth)) != ILLUME_OK) return st;
     ILLUME_CUDA_TRY(cudaEventRecord(ev1, ctx->stream));
-    for (int r = 0; r < e.rows; ++r)
-      if (se.row_job[r]) jobs[se.row_job[r]]->stats.kernel_launches += (int64_t)k * Engine::launches_per_pass(depth);
+    for (int r : active) jobs[se.row_job[r]]->stats.kernel_launches += (int64_t)k * Engine::launches_per_pass(depth);
     unsigned long long total = 0;
     ILLUME_CUDA_TRY(cudaMemcpyAsync(&total, e.w.rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
     ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -406,7 +461,7 @@ int Server::set_option(int option, int64_t value) {
       autotune = value != 0;
       return ILLUME_OK;
     case ILLUME_SERVER_TRACE_VARIANT:
-      if (value < -1 || value > 1) { set_error("unknown trace kernel variant"); return ILLUME_ERR_INVALID; }
+      if (value < -1 || value > 2) { set_error("unknown trace kernel variant"); return ILLUME_ERR_INVALID; }
       trace_variant = (int)value;
       return ILLUME_OK;
     default:

@@ -1,12 +1,14 @@
 // Render server with continuous batching.
 //
-// Jobs share one wavefront job table per trace-kernel setting (intersector, BVH layout):
-// every pass renders the next sample range of every running job together, so a small
-// job's paths fill the slots a large job leaves free and late bounces stay full. A
-// queued job is admitted as soon as a table row, its minimum path share (one sample of
-// every pixel) and its device footprint fit; running jobs split the path slots between
-// them (water-filling), and a job that finishes frees its row and slots for the next
-// pass. Scenes, BVHs and accumulators stay resident on the device between passes.
+// Jobs share one wavefront job table per trace-kernel setting (intersector, BVH layout).
+// A queued job is admitted as soon as a table row and its device footprint fit. Before
+// every step the server composes the next passes: jobs grouped by scene (one scene's
+// BVH per pass stays in L2), groups taken smallest remaining job first while the slots
+// and an L2 budget allow (or the pass is under half full), the chosen jobs sharing the
+// path slots by water-filling, the others paused. Small jobs thus run together in one
+// full pass instead of one under-filled pass each, and a finished job frees its row
+// and slots for the next pass. Scenes, BVHs and accumulators stay resident on the
+// device between passes.
 //
 // A job's image depends only on its own scene and parameters: random numbers are keyed
 // by (pixel, sample, bounce) and (seed, job), and each pixel's samples are summed in
@@ -60,7 +62,7 @@ struct Server {
   Context* ctx = nullptr;
   size_t budget = 0;          // device bytes for engines and job buffers (0 = unlimited)
   int rows = 64;              // job-table rows per engine
-  int path_capacity = 1 << 22;
+  int path_capacity = 1 << 23;
   int passes_per_step = 1;
   int autotune = 0;
   int trace_variant = -1;     // -1 = per-layout default
@@ -84,7 +86,7 @@ struct Server {
  private:
   size_t engines_bytes() const;
   int admit();
-  void rebalance(ServerEngine& se);
+  void compose(ServerEngine& se);
   int retire(ServerEngine& se, std::vector<ServerJob*>* done);
   void tune(ServerEngine& se, double rays, double ms);
   int apply_candidate(ServerEngine& se, int idx);

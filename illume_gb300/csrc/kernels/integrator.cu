@@ -95,6 +95,8 @@ __global__ void __launch_bounds__(1024) k_plan(WaveBuffers w) {
     w.counters[kCounterPixels] = pixels;
     w.counters[0] = paths;
     w.counters[1] = 0;
+    w.counters[44] = 0;   // trace ray-fetch counters by bounce parity
+    w.counters[45] = 0;
     if (over) w.counters[42] = 1;
     for (int c = 0; c < EV_COUNT; ++c) ev_counts2(w, 0)[c] = 0;
   }

@@ -26,6 +26,7 @@ static constexpr int kMaxNodeVisits = 1 << 22;
 struct TraceRay {
   V3 o, d;        // object-space origin / direction (direction as given, not normalised)
   V3 idir;        // clamped reciprocal direction for box tests
+  V3 oi;          // o * idir (box tests in fused multiply-add form)
   int oct;        // bit 2: d.x < 0, bit 1: d.y < 0, bit 0: d.z < 0
   // watertight setup
   int kx, ky, kz;
@@ -40,6 +41,7 @@ __device__ __forceinline__ void setup_ray(TraceRay& r, V3 o, V3 d, int isect) {
   r.o = o;
   r.d = d;
   r.idir = v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+  r.oi = v3(o.x * r.idir.x, o.y * r.idir.y, o.z * r.idir.z);
   r.oct = (d.x < 0.0f ? 4 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 1 : 0);
   if (isect == ISECT_WATERTIGHT) {
     const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
@@ -129,8 +131,25 @@ __device__ __forceinline__ bool box_hit(float lox, float loy, float loz, float h
   return t0 <= t1 && t0 <= tbest * kExitSlack;
 }
 
+// The same slab test with one fused multiply-add per plane, t = plane * idir - o * idir.
+// It differs from box_hit by the rounding of o * idir, a relative 2^-24 of |o| / |d|,
+// far inside the boxes' build padding (2^-16 of extent plus magnitude) for origins
+// within ~100x the mesh extent, so it culls no box that contains a hit either.
+__device__ __forceinline__ bool box_hit_fma(float lox, float loy, float loz, float hix, float hiy, float hiz,
+                                            const TraceRay& r, float tbest, float& tentry) {
+  const float nx = r.idir.x >= 0.0f ? lox : hix, fx = r.idir.x >= 0.0f ? hix : lox;
+  const float ny = r.idir.y >= 0.0f ? loy : hiy, fy = r.idir.y >= 0.0f ? hiy : loy;
+  const float nz = r.idir.z >= 0.0f ? loz : hiz, fz = r.idir.z >= 0.0f ? hiz : loz;
+  const float t0 = fmaxf(fmaxf(__fmaf_rn(nx, r.idir.x, -r.oi.x), __fmaf_rn(ny, r.idir.y, -r.oi.y)),
+                         fmaxf(__fmaf_rn(nz, r.idir.z, -r.oi.z), 0.0f));
+  const float t1 = fminf(fminf(__fmaf_rn(fx, r.idir.x, -r.oi.x), __fmaf_rn(fy, r.idir.y, -r.oi.y)),
+                         __fmaf_rn(fz, r.idir.z, -r.oi.z)) * kExitSlack;
+  tentry = t0;
+  return t0 <= t1 && t0 <= tbest * kExitSlack;
+}
+
 // ---- binary BVH ----
-template <bool COUNT>
+template <bool COUNT, bool FMA = false>
 __device__ __forceinline__ void traverse_bvh2(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
                                               int* stack, VisitCount& vc) {
   int sp = 0;
@@ -141,8 +160,10 @@ __device__ __forceinline__ void traverse_bvh2(const DevMesh& m, const TraceRay& 
     const float4 a = __ldg(&n->a), b = __ldg(&n->b), c = __ldg(&n->c);
     const int4 d = __ldg(&n->d);
     float te0, te1;
-    const bool h0 = box_hit(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0);
-    const bool h1 = box_hit(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1);
+    const bool h0 = FMA ? box_hit_fma(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0)
+                        : box_hit(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0);
+    const bool h1 = FMA ? box_hit_fma(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1)
+                        : box_hit(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1);
     // leaves are tested at once; inner children are visited near first
     int inner0 = -1, inner1 = -1;
     if (h0) {
@@ -353,7 +374,7 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 }
 
 // Full closest-hit query for a world-space ray (direction used as given).
-template <int KIND, bool COUNT = false>
+template <int KIND, bool COUNT = false, bool FMA = false>
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
                                                  VisitCount* vcp = nullptr) {
   VisitCount vc;
@@ -386,7 +407,7 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     MeshBest b{h.t, -1, 0.0f, 0.0f};
     const DevMesh& m = sc.meshes[in.mesh];
     if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);
-    else traverse_bvh2<COUNT>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
+    else traverse_bvh2<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }
   }
   if (COUNT && vcp) *vcp = vc;

@@ -40,16 +40,32 @@ __device__ __forceinline__ int event_class(const WaveBuffers& w, const JobDesc& 
 
 // Trace stage of one bounce: closest hit of every queued ray in its job's scene, then
 // an append of the ray's queue position to its event class's queue.
-template <int KIND, bool COUNT, int MINB = 1>
+// OPT: box tests in fused multiply-add form, and warps take their next 32 rays from a
+// shared counter (counters[44 + parity]) instead of a fixed grid stride, so that warps
+// whose rays finish early take over the remaining work.
+template <int KIND, bool COUNT, int MINB = 1, bool OPT = false>
 __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
   const int parity = bounce & 1;
   const int n = w.counters[parity];
-  if (blockIdx.x == 0 && threadIdx.x == 0) w.counters[parity ^ 1] = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    w.counters[parity ^ 1] = 0;
+    w.counters[44 + (parity ^ 1)] = 0;
+  }
   int* counts = ev_counts(w, parity);
+  int* fetch = w.counters + 44 + parity;
+  const int lane = threadIdx.x & 31;
   typename std::conditional<KIND == BVH_WIDE8, uint2, int>::type stack[kStack];
   unsigned long long my_nodes = 0, my_tris = 0;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-    const int i = base + threadIdx.x;
+  int base = OPT ? 0 : blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+  for (;;) {
+    if (OPT) {
+      int b0 = 0;
+      if (lane == 0) b0 = atomicAdd(fetch, 32);
+      base = __shfl_sync(0xffffffffu, b0, 0);
+    }
+    if (base >= n) break;
+    const int i = base + lane;
+    if (!OPT) base += gridDim.x * blockDim.x;
     const bool valid = i < n;
     const unsigned mask = __ballot_sync(0xffffffffu, valid);
     if (!valid) continue;
@@ -59,7 +75,8 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
     const JobDesc& J = w.jobs[packed >> kMediumBits];
     const SceneView& sc = J.sc;
     VisitCount vc;
-    const HitRecord h = closest_hit<KIND, COUNT>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack, &vc);
+    const HitRecord h =
+        closest_hit<KIND, COUNT, OPT>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack, &vc);
     if (COUNT) { my_nodes += vc.nodes; my_tris += vc.tris; }
     const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
     w.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
@@ -229,7 +246,8 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
   typename std::conditional<KIND == BVH_WIDE8, uint2, int>::type stack[kStack];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 a = rays[2 * i], b = rays[2 * i + 1];
-    const HitRecord h = closest_hit<KIND>(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), isect, stack);
+    // the binary layout is tested with the box arithmetic of the default trace kernel
+    const HitRecord h = closest_hit<KIND, false, KIND == BVH_BINARY>(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), isect, stack);
     illume_hit o;
     o.t = h.t;
     o.u = h.geom >= 0 ? h.u : 0.0f;
@@ -243,12 +261,16 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 }
 
 // Trace kernel variants (RenderKnobs::trace_variant):
-//   binary BVH: 0 = at most 64 registers (8 blocks of 128 per SM), 1 = compiler's register choice;
+//   binary BVH: 0 = at most 64 registers (8 blocks of 128 per SM), fused box tests, dynamic
+//   ray fetch (the default); 1 = compiler's register choice, grid-stride rays, plain box
+//   tests; 2 = variant 1 held to 64 registers;
 //   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine.
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (bvh_kind == BVH_WIDE8)
     return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
-  return variant == 1 ? (const void*)k_trace<BVH_BINARY, false> : (const void*)k_trace<BVH_BINARY, false, 8>;
+  if (variant == 1) return (const void*)k_trace<BVH_BINARY, false>;
+  if (variant == 2) return (const void*)k_trace<BVH_BINARY, false, 8>;
+  return (const void*)k_trace<BVH_BINARY, false, 8, true>;
 }
 
 void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st,
@@ -268,8 +290,13 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
     else k_trace<BVH_BINARY, false><<<grid, 128, 0, st>>>(w, k, bounce);
     return;
   }
-  if (count_visits) k_trace<BVH_BINARY, true, 8><<<grid, 128, 0, st>>>(w, k, bounce);
-  else k_trace<BVH_BINARY, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+  if (k.trace_variant == 2) {
+    if (count_visits) k_trace<BVH_BINARY, true, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+    else k_trace<BVH_BINARY, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+    return;
+  }
+  if (count_visits) k_trace<BVH_BINARY, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+  else k_trace<BVH_BINARY, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
 }
 
 void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float* rays8, int n, int isect,

@@ -152,7 +152,9 @@ typedef struct {
    * floats of the camera-to-world rows (3x4, the layout of illume_scene_desc's
    * camera_transform), then fov (degrees), dof and aperture. NULL = the scene's camera. */
   const float* camera;
-  int32_t reserved[4];        /* reserved[0]: binary-BVH trace kernel variant (0 default, 1 other) */
+  int32_t reserved[4];        /* reserved[0]: binary-BVH trace kernel variant: 0 = 64 registers, fused box
+                               * tests, dynamic ray fetch (default); 1 = compiler's register choice,
+                               * grid-stride rays; 2 = variant 1 held to 64 registers */
 } illume_render_params;
 
 typedef struct {
@@ -303,7 +305,8 @@ int illume_server_destroy(illume_server* s);
 /* Queue a job (ILLUME_ERR_BUDGET if its footprint can never fit the budget). The
  * server ignores params->samples_per_pass and the binary-kernel variant word. */
 int illume_job_submit(illume_server* s, illume_scene* scene, const illume_render_params* params, illume_job_id* out);
-/* One scheduling round: admit what fits, rebalance path slots, run up to
+/* One scheduling round: admit what fits, compose the passes (jobs grouped by scene,
+ * smallest remaining job first, slots shared by water-filling), run up to
  * ILLUME_SERVER_PASSES_PER_STEP wavefront passes (fewer if a job finishes sooner),
  * retire finished jobs. *jobs_running = running + queued jobs afterwards. */
 int illume_server_step(illume_server* s, int* jobs_running);
@@ -317,7 +320,7 @@ int illume_job_poll(illume_server* s, illume_job_id id, float* out_mean, uint8_t
 int illume_job_cancel(illume_server* s, illume_job_id id);
 
 typedef enum {
-  ILLUME_SERVER_PATH_CAPACITY = 0,    /* path slots of each job table (default 4194304) */
+  ILLUME_SERVER_PATH_CAPACITY = 0,    /* path slots of each job table (default 8388608) */
   ILLUME_SERVER_PASSES_PER_STEP = 1,  /* passes per illume_server_step (default 1) */
   ILLUME_SERVER_AUTOTUNE = 2,         /* 1 = choose path slots and trace kernel from measured throughput */
   ILLUME_SERVER_TRACE_VARIANT = 3     /* trace kernel variant (-1 = default) */
