@@ -327,10 +327,12 @@ int Server::apply_candidate(ServerEngine& se, int idx) {
 void Server::tune(ServerEngine& se, double rays, double ms) {
   static constexpr int kWindow = 3;
   if (se.tune_state == 0) {
-    for (int cap : {1 << 22, 1 << 23, 1 << 24}) {
+    // binary BVH: the default kernel and its while-while form; 8-wide: both kernels
+    const std::vector<int> variants = se.eng->knobs.bvh_kind == BVH_BINARY ? std::vector<int>{0, 3}
+                                                                           : std::vector<int>{0, 1};
+    for (int cap : {1 << 23, 1 << 24}) {
       if (budget && reserved + engines_bytes() - se.eng->device_bytes() + (size_t)cap * kBytesPerPath > budget) continue;
-      const int variants = se.eng->knobs.bvh_kind == BVH_BINARY ? 3 : 2;
-      for (int v = 0; v < variants; ++v) se.candidates.push_back({cap, v});
+      for (int v : variants) se.candidates.push_back({cap, v});
     }
     se.rate.assign(se.candidates.size(), 0.0);
     se.tune_state = 1;
@@ -461,7 +463,7 @@ int Server::set_option(int option, int64_t value) {
       autotune = value != 0;
       return ILLUME_OK;
     case ILLUME_SERVER_TRACE_VARIANT:
-      if (value < -1 || value > 2) { set_error("unknown trace kernel variant"); return ILLUME_ERR_INVALID; }
+      if (value < -1 || value > 3) { set_error("unknown trace kernel variant"); return ILLUME_ERR_INVALID; }
       trace_variant = (int)value;
       return ILLUME_OK;
     default:

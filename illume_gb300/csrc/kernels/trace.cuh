@@ -193,6 +193,60 @@ __device__ __forceinline__ void traverse_bvh2(const DevMesh& m, const TraceRay& 
   }
 }
 
+// Binary BVH, "while-while" order (after Aila and Laine, "Understanding the efficiency
+// of ray traversal on GPUs", HPG 2009): a lane keeps visiting inner nodes and sets aside
+// the first leaf it meets; the warp leaves the node loop once every lane still in it
+// holds a leaf, and then tests those leaves together. Stack entries are inner node
+// indices (>= 0) or leaf codes ~(first << 3 | count) (<= -2); -1 is empty.
+template <bool COUNT, bool FMA>
+__device__ __forceinline__ void traverse_bvh2_ww(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
+                                                 int* stack, VisitCount& vc) {
+  constexpr int kEmpty = -1;
+  int sp = 0;
+  int cur = 0;          // next entry: inner node, leaf code or kEmpty
+  int leaf = kEmpty;    // leaf set aside
+  for (int guard = 0; guard < kMaxNodeVisits; ++guard) {
+    while (cur >= 0) {
+      if (COUNT) vc.nodes++;
+      const Bvh2Node* n = m.bvh2 + cur;
+      const float4 a = __ldg(&n->a), b = __ldg(&n->b), c = __ldg(&n->c);
+      const int4 d = __ldg(&n->d);
+      float te0, te1;
+      const bool h0 = FMA ? box_hit_fma(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0)
+                          : box_hit(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0);
+      const bool h1 = FMA ? box_hit_fma(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1)
+                          : box_hit(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1);
+      int c0 = !h0 ? kEmpty : (d.x >= 0 ? d.x : (d.z > 0 ? ~((~d.x << 3) | d.z) : kEmpty));
+      int c1 = !h1 ? kEmpty : (d.y >= 0 ? d.y : (d.w > 0 ? ~((~d.y << 3) | d.w) : kEmpty));
+      if (c0 != kEmpty && c1 != kEmpty && te1 < te0) { const int t = c0; c0 = c1; c1 = t; }
+      if (c0 == kEmpty) { c0 = c1; c1 = kEmpty; }
+      if (c0 != kEmpty) {
+        cur = c0;
+        if (c1 != kEmpty && sp < kStack) stack[sp++] = c1;
+      } else {
+        cur = sp > 0 ? stack[--sp] : kEmpty;
+      }
+      if (cur < kEmpty && leaf == kEmpty) {
+        leaf = cur;
+        cur = sp > 0 ? stack[--sp] : kEmpty;
+      }
+      if (__all_sync(__activemask(), leaf != kEmpty)) break;
+    }
+    while (leaf != kEmpty) {
+      const int code = ~leaf;
+      const int first = code >> 3, count = code & 7;
+      if (COUNT) vc.tris += count;
+      for (int i = first; i < first + count; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
+      leaf = kEmpty;
+      if (cur < kEmpty) {
+        leaf = cur;
+        cur = sp > 0 ? stack[--sp] : kEmpty;
+      }
+    }
+    if (cur == kEmpty) break;
+  }
+}
+
 // ---- 8-wide quantised BVH ----
 __device__ __forceinline__ float exp2i(uint8_t biased) { return __int_as_float((int)biased << 23); }
 
@@ -374,7 +428,7 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 }
 
 // Full closest-hit query for a world-space ray (direction used as given).
-template <int KIND, bool COUNT = false, bool FMA = false>
+template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false>
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
                                                  VisitCount* vcp = nullptr) {
   VisitCount vc;
@@ -407,6 +461,7 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     MeshBest b{h.t, -1, 0.0f, 0.0f};
     const DevMesh& m = sc.meshes[in.mesh];
     if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);
+    else if (WW) traverse_bvh2_ww<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else traverse_bvh2<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }
   }

@@ -43,7 +43,7 @@ __device__ __forceinline__ int event_class(const WaveBuffers& w, const JobDesc& 
 // OPT: box tests in fused multiply-add form, and warps take their next 32 rays from a
 // shared counter (counters[44 + parity]) instead of a fixed grid stride, so that warps
 // whose rays finish early take over the remaining work.
-template <int KIND, bool COUNT, int MINB = 1, bool OPT = false>
+template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false>
 __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
   const int parity = bounce & 1;
   const int n = w.counters[parity];
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
     const SceneView& sc = J.sc;
     VisitCount vc;
     const HitRecord h =
-        closest_hit<KIND, COUNT, OPT>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack, &vc);
+        closest_hit<KIND, COUNT, OPT, WW>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack, &vc);
     if (COUNT) { my_nodes += vc.nodes; my_tris += vc.tris; }
     const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
     w.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
@@ -263,13 +263,15 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 // Trace kernel variants (RenderKnobs::trace_variant):
 //   binary BVH: 0 = at most 64 registers (8 blocks of 128 per SM), fused box tests, dynamic
 //   ray fetch (the default); 1 = compiler's register choice, grid-stride rays, plain box
-//   tests; 2 = variant 1 held to 64 registers;
+//   tests; 2 = variant 1 held to 64 registers; 3 = variant 0 with while-while traversal
+//   (leaves set aside and tested warp-together, traverse_bvh2_ww);
 //   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine.
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (bvh_kind == BVH_WIDE8)
     return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
   if (variant == 1) return (const void*)k_trace<BVH_BINARY, false>;
   if (variant == 2) return (const void*)k_trace<BVH_BINARY, false, 8>;
+  if (variant == 3) return (const void*)k_trace<BVH_BINARY, false, 8, true, true>;
   return (const void*)k_trace<BVH_BINARY, false, 8, true>;
 }
 
@@ -293,6 +295,11 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
   if (k.trace_variant == 2) {
     if (count_visits) k_trace<BVH_BINARY, true, 8><<<grid, 128, 0, st>>>(w, k, bounce);
     else k_trace<BVH_BINARY, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+    return;
+  }
+  if (k.trace_variant == 3) {
+    if (count_visits) k_trace<BVH_BINARY, true, 8, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    else k_trace<BVH_BINARY, false, 8, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
     return;
   }
   if (count_visits) k_trace<BVH_BINARY, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
