@@ -281,12 +281,15 @@ def run_ours(args):
     achieved_gbs = trace_bytes / (prof_t.trace_ms * 1e-3) / 1e9
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
+    # DRAM traffic of the trace kernel per launch: bytes per ray from the committed ncu
+    # summary, times this workload's rays per trace launch
     traffic = None
     tf = os.path.join(ROOT, "profiles", "trace_traffic.txt")
     if os.path.exists(tf):
         for line in open(tf):
-            if line.startswith("dram_bytes_per_launch_full_workload:"):
-                traffic = float(line.split(":")[1])
+            if line.startswith("dram_bytes_per_ray:"):
+                traffic = round(float(line.split(":")[1]) * prof_t.rays / max(prof_t.trace_launches, 1))
+    algo_per_launch = round(trace_bytes / max(prof_t.trace_launches, 1))
 
     # end to end through the C-ABI with host buffers
     npix = args.res * args.res
@@ -329,6 +332,8 @@ def run_ours(args):
                          "frac": round(achieved_gbs / peak, 4), "traffic": traffic,
                          "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
                          "kernel": "k_trace", "bytes_per_ray": round(bytes_per_ray, 1),
+                         "algorithmic_bytes_per_launch": algo_per_launch,
+                         "traffic_source": "profiles/trace_traffic.txt (ncu DRAM bytes per ray x rays per launch)",
                          "node_fetches_per_ray": round(prof_c.node_fetches / max(prof_c.rays, 1), 2),
                          "tri_tests_per_ray": round(prof_c.tri_tests / max(prof_c.rays, 1), 2),
                          "trace_ms_per_pass": round(prof_t.trace_ms, 3), "shade_ms_per_pass": round(prof_t.shade_ms, 3)},

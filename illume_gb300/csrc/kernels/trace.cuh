@@ -135,14 +135,26 @@ __device__ __forceinline__ bool box_hit(float lox, float loy, float loz, float h
 // It differs from box_hit by the rounding of o * idir, a relative 2^-24 of |o| / |d|,
 // far inside the boxes' build padding (2^-16 of extent plus magnitude) for origins
 // within ~100x the mesh extent, so it culls no box that contains a hit either.
+// Three-input minimum / maximum (sm_100 and later), as fminf / fmaxf of the three.
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 __device__ __forceinline__ bool box_hit_fma(float lox, float loy, float loz, float hix, float hiy, float hiz,
                                             const TraceRay& r, float tbest, float& tentry) {
   const float nx = r.idir.x >= 0.0f ? lox : hix, fx = r.idir.x >= 0.0f ? hix : lox;
   const float ny = r.idir.y >= 0.0f ? loy : hiy, fy = r.idir.y >= 0.0f ? hiy : loy;
   const float nz = r.idir.z >= 0.0f ? loz : hiz, fz = r.idir.z >= 0.0f ? hiz : loz;
-  const float t0 = fmaxf(fmaxf(__fmaf_rn(nx, r.idir.x, -r.oi.x), __fmaf_rn(ny, r.idir.y, -r.oi.y)),
+  const float t0 = max3f(__fmaf_rn(nx, r.idir.x, -r.oi.x), __fmaf_rn(ny, r.idir.y, -r.oi.y),
                          fmaxf(__fmaf_rn(nz, r.idir.z, -r.oi.z), 0.0f));
-  const float t1 = fminf(fminf(__fmaf_rn(fx, r.idir.x, -r.oi.x), __fmaf_rn(fy, r.idir.y, -r.oi.y)),
+  const float t1 = min3f(__fmaf_rn(fx, r.idir.x, -r.oi.x), __fmaf_rn(fy, r.idir.y, -r.oi.y),
                          __fmaf_rn(fz, r.idir.z, -r.oi.z)) * kExitSlack;
   tentry = t0;
   return t0 <= t1 && t0 <= tbest * kExitSlack;
