@@ -51,8 +51,11 @@ def parse():
     ap.add_argument("--bvh", default="binary", choices=["binary", "wide", "wide-persistent"])
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--trace-variant", type=int, default=0,
-                    help="binary traversal: 0 64 registers + fused box tests + dynamic ray fetch (default), "
-                         "1 compiler register choice, 2 variant 1 held to 64 registers")
+                    help="binary traversal: 0 64 registers + fused box tests + dynamic ray fetch + while-while "
+                         "(default), 1 compiler register choice, 2 variant 1 held to 64 registers, 3 variant 0 with "
+                         "leaves tested where met")
+    ap.add_argument("--shade-variant", type=int, default=0,
+                    help="shade kernel: 0 at most 64 registers (default), 1 compiler register choice")
     ap.add_argument("--tris", type=int, default=100_000)
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--depth", type=int, default=25)
@@ -231,6 +234,7 @@ def run_ours(args):
     p.accum_mode = C.ACCUM_FP32
     p.sample_begin = rank * 1_000_000
     p.reserved[0] = args.trace_variant
+    p.reserved[1] = args.shade_variant
     r = Renderer(ctx, scene, params=p)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")   # > 129 MB L2
 

@@ -76,7 +76,7 @@ int Engine::init(Context* c, int nrows, int ncap, const RenderKnobs& k, std::str
   ILLUME_CUDA_TRY(cudaMemsetAsync(jobs.get(), 0, jobs.size(), ctx->stream));
   point();
   grid_trace = kernel_grid_blocks(trace_kernel_ptr(knobs.bvh_kind, knobs.trace_variant), 128, ctx->device);
-  grid_shade = kernel_grid_blocks(shade_kernel_ptr(), 128, ctx->device);
+  grid_shade = kernel_grid_blocks(shade_kernel_ptr(knobs.shade_variant), 128, ctx->device);
   return ILLUME_OK;
 }
 
@@ -149,7 +149,7 @@ void Engine::launch_pass(cudaStream_t st, int depth) {
   launch_raygen(w, grid_raygen, st);
   for (int b = 0; b < depth; ++b) {
     launch_trace(w, knobs, b, grid_trace, st);
-    launch_shade(w, b, grid_shade, st);
+    launch_shade(w, knobs, b, grid_shade, st);
   }
   launch_accumulate(w, grid_acc, st);
   launch_advance(w, st);
@@ -203,7 +203,7 @@ int Engine::run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>&
   for (int b = 0; b < depth; ++b) {
     launch_trace(w, knobs, b, grid_trace, st, count_visits);
     cudaEventRecord(ev[k++], st);
-    launch_shade(w, b, grid_shade, st);
+    launch_shade(w, knobs, b, grid_shade, st);
     cudaEventRecord(ev[k++], st);
   }
   launch_accumulate(w, grid_acc, st);

@@ -39,6 +39,7 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if (p.bvh_kind == BVH_BINARY && (p.reserved[0] < 0 || p.reserved[0] > 3)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.accum_mode < ACCUM_FP32 || p.accum_mode > ACCUM_FP64) { *err = "unknown accumulation mode"; return ILLUME_ERR_INVALID; }
   if (p.samples_per_pass < 0) { *err = "negative samples per pass"; return ILLUME_ERR_INVALID; }
+  if (p.reserved[1] < 0 || p.reserved[1] > 1) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
   if ((int)scene.t_mediums.size() > kMaxMediums) { *err = "too many mediums"; return ILLUME_ERR_UNSUPPORTED; }
   if (!scene.ctx || !scene.view_dev) { *err = "scene has not been uploaded to a device"; return ILLUME_ERR_INVALID; }
   return ILLUME_OK;
@@ -49,6 +50,7 @@ RenderKnobs render_knobs(const illume_render_params& p) {
   k.isect = p.intersector;
   k.bvh_kind = p.bvh_kind == 2 ? BVH_WIDE8 : p.bvh_kind;
   k.trace_variant = p.bvh_kind == 2 ? 1 : (p.bvh_kind == BVH_BINARY ? p.reserved[0] : 0);
+  k.shade_variant = p.reserved[1];
   return k;
 }
 

@@ -97,6 +97,7 @@ int Server::admit() {
       se.eng.reset(new Engine);
       RenderKnobs k = render_knobs(p);
       k.trace_variant = trace_variant >= 0 ? trace_variant : (p.bvh_kind == 2 ? 1 : 0);
+      k.shade_variant = 0;
       std::string err;
       const int st = se.eng->init(ctx, rows, (int)cap, k, &err);
       if (st != ILLUME_OK) { set_error(err); return st; }

@@ -141,8 +141,10 @@ struct BounceRng {
   __device__ __forceinline__ float operator()() { return s.next(); }
 };
 
-// Shading of one bounce over the material-sorted event queues.
-__global__ void __launch_bounds__(128) k_shade(WaveBuffers w, int bounce) {
+// Shading of one bounce over the material-sorted event queues. MINB = blocks of 128
+// threads per SM the register allocation must allow (1 = the compiler's choice).
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) {
   const int parity = bounce & 1;
   const int* counts = ev_counts2(w, parity);
   __shared__ int prefix[EV_COUNT + 1];
@@ -460,15 +462,21 @@ __global__ void k_bsdf_batch(int type, int dist, const float* in, int n, float* 
   }
 }
 
-const void* shade_kernel_ptr() { return (const void*)k_shade; }
+// Shade kernel variants (RenderKnobs::shade_variant): 0 = at most 64 registers (8 blocks of
+// 128 per SM, more loads in flight for this gather-latency-bound stage), 1 = compiler's
+// register choice.
+const void* shade_kernel_ptr(int variant) {
+  return variant == 1 ? (const void*)k_shade<1> : (const void*)k_shade<8>;
+}
 
 void launch_plan(const WaveBuffers& w, cudaStream_t st) {
   const int threads = w.njobs >= 1024 ? 1024 : ((w.njobs + 31) / 32) * 32;
   k_plan<<<1, threads > 32 ? threads : 32, 0, st>>>(w);
 }
 void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st) { k_raygen<<<grid, 256, 0, st>>>(w); }
-void launch_shade(const WaveBuffers& w, int bounce, int grid, cudaStream_t st) {
-  k_shade<<<grid, 128, 0, st>>>(w, bounce);
+void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st) {
+  if (k.shade_variant == 1) k_shade<1><<<grid, 128, 0, st>>>(w, bounce);
+  else k_shade<8><<<grid, 128, 0, st>>>(w, bounce);
 }
 void launch_accumulate(const WaveBuffers& w, int grid, cudaStream_t st) { k_accumulate<<<grid, 256, 0, st>>>(w); }
 void launch_advance(const WaveBuffers& w, cudaStream_t st) {

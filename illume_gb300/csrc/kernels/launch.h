@@ -76,6 +76,7 @@ struct RenderKnobs {
   int isect;           // illume_intersector
   int bvh_kind;        // BVH_BINARY or BVH_WIDE8
   int trace_variant;   // see trace_kernel_ptr
+  int shade_variant;   // see shade_kernel_ptr
 };
 
 int kernel_grid_blocks(const void* fn, int block, int device);
@@ -84,7 +85,7 @@ void launch_plan(const WaveBuffers& w, cudaStream_t st);
 void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st);
 void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st,
                   bool count_visits = false);
-void launch_shade(const WaveBuffers& w, int bounce, int grid, cudaStream_t st);
+void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st);
 void launch_accumulate(const WaveBuffers& w, int grid, cudaStream_t st);
 void launch_advance(const WaveBuffers& w, cudaStream_t st);
 void launch_tonemap(const Accumulators& acc, int accum_mode, int npix, float samples, int op, uint8_t* rgb8,
@@ -98,6 +99,6 @@ void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float
 void launch_bsdf_batch(int type, int distribution, const float* in, int n, float* out, cudaStream_t st);
 
 const void* trace_kernel_ptr(int bvh_kind, int variant = 0);
-const void* shade_kernel_ptr();
+const void* shade_kernel_ptr(int variant = 0);
 
 }  // namespace illume

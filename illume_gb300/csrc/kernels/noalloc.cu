@@ -133,7 +133,7 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
   cudaStream_t st = ctx->c.stream;
   const int sms = ctx->c.sm_count > 0 ? ctx->c.sm_count : 1;
   const int grid_trace = kernel_grid_blocks(trace_kernel_ptr(p.bvh_kind, 0), 128, dev);
-  const int grid_shade = kernel_grid_blocks(shade_kernel_ptr(), 128, dev);
+  const int grid_shade = kernel_grid_blocks(shade_kernel_ptr(0), 128, dev);
   const int grid_small = std::max(1, std::min((cap + 255) / 256, sms * 8));
   k_noalloc_begin<<<grid_small, 256, 0, st>>>(w.counters, w.rays, w.visits, w.jobs, row, d_sum, cap);
   for (int s = 0; s < p.spp; ++s) {
@@ -141,7 +141,7 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
     launch_raygen(w, grid_small, st);
     for (int b = 0; b < p.max_depth; ++b) {
       launch_trace(w, k, b, grid_trace, st);
-      launch_shade(w, b, grid_shade, st);
+      launch_shade(w, k, b, grid_shade, st);
     }
     launch_accumulate(w, grid_small, st);
     launch_advance(w, st);

@@ -246,8 +246,10 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
   typename std::conditional<KIND == BVH_WIDE8, uint2, int>::type stack[kStack];
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 a = rays[2 * i], b = rays[2 * i + 1];
-    // the binary layout is tested with the box arithmetic of the default trace kernel
-    const HitRecord h = closest_hit<KIND, false, KIND == BVH_BINARY>(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), isect, stack);
+    // the binary layout is tested with the box arithmetic and traversal order of the
+    // default trace kernel
+    const HitRecord h =
+        closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY>(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), isect, stack);
     illume_hit o;
     o.t = h.t;
     o.u = h.geom >= 0 ? h.u : 0.0f;
@@ -262,17 +264,17 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 
 // Trace kernel variants (RenderKnobs::trace_variant):
 //   binary BVH: 0 = at most 64 registers (8 blocks of 128 per SM), fused box tests, dynamic
-//   ray fetch (the default); 1 = compiler's register choice, grid-stride rays, plain box
-//   tests; 2 = variant 1 held to 64 registers; 3 = variant 0 with while-while traversal
-//   (leaves set aside and tested warp-together, traverse_bvh2_ww);
+//   ray fetch, while-while traversal (traverse_bvh2_ww; the default); 1 = compiler's
+//   register choice, grid-stride rays, plain box tests, leaves tested where met; 2 =
+//   variant 1 held to 64 registers; 3 = variant 0 with leaves tested where met;
 //   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine.
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (bvh_kind == BVH_WIDE8)
     return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
   if (variant == 1) return (const void*)k_trace<BVH_BINARY, false>;
   if (variant == 2) return (const void*)k_trace<BVH_BINARY, false, 8>;
-  if (variant == 3) return (const void*)k_trace<BVH_BINARY, false, 8, true, true>;
-  return (const void*)k_trace<BVH_BINARY, false, 8, true>;
+  if (variant == 3) return (const void*)k_trace<BVH_BINARY, false, 8, true>;
+  return (const void*)k_trace<BVH_BINARY, false, 8, true, true>;
 }
 
 void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st,
@@ -298,12 +300,12 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
     return;
   }
   if (k.trace_variant == 3) {
-    if (count_visits) k_trace<BVH_BINARY, true, 8, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
-    else k_trace<BVH_BINARY, false, 8, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    if (count_visits) k_trace<BVH_BINARY, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    else k_trace<BVH_BINARY, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
     return;
   }
-  if (count_visits) k_trace<BVH_BINARY, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
-  else k_trace<BVH_BINARY, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+  if (count_visits) k_trace<BVH_BINARY, true, 8, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
+  else k_trace<BVH_BINARY, false, 8, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
 }
 
 void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float* rays8, int n, int isect,

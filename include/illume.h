@@ -153,8 +153,11 @@ typedef struct {
    * camera_transform), then fov (degrees), dof and aperture. NULL = the scene's camera. */
   const float* camera;
   int32_t reserved[4];        /* reserved[0]: binary-BVH trace kernel variant: 0 = 64 registers, fused box
-                               * tests, dynamic ray fetch (default); 1 = compiler's register choice,
-                               * grid-stride rays; 2 = variant 1 held to 64 registers */
+                               * tests, dynamic ray fetch, while-while traversal (default); 1 = compiler's
+                               * register choice, grid-stride rays, leaves tested where met; 2 = variant 1
+                               * held to 64 registers; 3 = variant 0 with leaves tested where met.
+                               * reserved[1]: shade kernel variant: 0 = at most 64 registers (default),
+                               * 1 = compiler's register choice. */
 } illume_render_params;
 
 typedef struct {
