@@ -1,4 +1,5 @@
 #include "image_io.h"
+#include "png_decode.h"
 
 #include <math.h>
 #include <stdio.h>
@@ -179,6 +180,7 @@ bool load_image(const std::string& path, Image* out, std::string* err) {
   if (e == "pfm") return load_pfm(d, out, err);
   if (e == "ppm") return load_ppm(d, out, err);
   if (e == "hdr") return load_hdr(d, out, err);
+  if (e == "png") return decode_png(d, out, err);
   *err = "unsupported image format ." + e + " (" + path + ")";
   return false;
 }

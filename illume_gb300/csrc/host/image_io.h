@@ -1,4 +1,4 @@
-// Image files: texture input (Radiance .hdr, .pfm, binary .ppm) and render output
+// Image files: texture input (Radiance .hdr, .pfm, binary .ppm, .png) and render output
 // (8-bit RGB .png and .ppm, float .pfm). The PNG writer stores deflate blocks without
 // compression, so it needs no zlib.
 #pragma once
