@@ -55,7 +55,7 @@ def parse():
                          "(default), 1 compiler register choice, 2 variant 1 held to 64 registers, 3 variant 0 with "
                          "leaves tested where met")
     ap.add_argument("--shade-variant", type=int, default=0,
-                    help="shade kernel: 0 at most 64 registers (default), 1 compiler register choice")
+                    help="shade kernel: 0 compiler register choice (default), 1 at most 64 registers")
     ap.add_argument("--tris", type=int, default=100_000)
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--depth", type=int, default=25)

@@ -462,11 +462,11 @@ __global__ void k_bsdf_batch(int type, int dist, const float* in, int n, float* 
   }
 }
 
-// Shade kernel variants (RenderKnobs::shade_variant): 0 = at most 64 registers (8 blocks of
-// 128 per SM, more loads in flight for this gather-latency-bound stage), 1 = compiler's
-// register choice.
+// Shade kernel variants (RenderKnobs::shade_variant): 0 = compiler's register choice (72,
+// the default), 1 = at most 64 registers (8 blocks of 128 per SM: more loads in flight,
+// but the spills it needs cost more; measured slower on the traversal workload).
 const void* shade_kernel_ptr(int variant) {
-  return variant == 1 ? (const void*)k_shade<1> : (const void*)k_shade<8>;
+  return variant == 1 ? (const void*)k_shade<8> : (const void*)k_shade<1>;
 }
 
 void launch_plan(const WaveBuffers& w, cudaStream_t st) {
@@ -475,8 +475,8 @@ void launch_plan(const WaveBuffers& w, cudaStream_t st) {
 }
 void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st) { k_raygen<<<grid, 256, 0, st>>>(w); }
 void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st) {
-  if (k.shade_variant == 1) k_shade<1><<<grid, 128, 0, st>>>(w, bounce);
-  else k_shade<8><<<grid, 128, 0, st>>>(w, bounce);
+  if (k.shade_variant == 1) k_shade<8><<<grid, 128, 0, st>>>(w, bounce);
+  else k_shade<1><<<grid, 128, 0, st>>>(w, bounce);
 }
 void launch_accumulate(const WaveBuffers& w, int grid, cudaStream_t st) { k_accumulate<<<grid, 256, 0, st>>>(w); }
 void launch_advance(const WaveBuffers& w, cudaStream_t st) {

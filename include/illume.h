@@ -156,8 +156,8 @@ typedef struct {
                                * tests, dynamic ray fetch, while-while traversal (default); 1 = compiler's
                                * register choice, grid-stride rays, leaves tested where met; 2 = variant 1
                                * held to 64 registers; 3 = variant 0 with leaves tested where met.
-                               * reserved[1]: shade kernel variant: 0 = at most 64 registers (default),
-                               * 1 = compiler's register choice. */
+                               * reserved[1]: shade kernel variant: 0 = compiler's register choice
+                               * (default), 1 = at most 64 registers. */
 } illume_render_params;
 
 typedef struct {
