@@ -39,7 +39,8 @@ struct Bvh2Node {
   float4 a;   // c0.lo.x c0.lo.y c0.lo.z c0.hi.x
   float4 b;   // c0.hi.y c0.hi.z c1.lo.x c1.lo.y
   float4 c;   // c1.lo.z c1.hi.x c1.hi.y c1.hi.z
-  int4 d;     // child0, child1, count0, count1
+  int4 d;     // child0, child1: inner node index (>= 0), leaf ~(first << 3 | count), empty
+              // slot -1; count0, count1: triangles of leaf children (0 otherwise)
 };
 
 // 8-wide BVH node with child boxes quantised to 8 bits per axis (80 B), after Ylitie,

@@ -237,7 +237,7 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
         Box empty;
         empty.reset();
         n.b.z = inf; n.b.w = inf; n.c = float4{inf, -inf, -inf, -inf};
-        n.d = int4{~bn[0].first, ~0, bn[0].count, 0};
+        n.d = int4{~((bn[0].first << 3) | bn[0].count), ~0, bn[0].count, 0};
         out->bvh2.push_back(n);
       } else {
         while (!st.empty()) {
@@ -256,8 +256,8 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
           const BNode& R = bn[b.right];
           encode_box(n, 0, L.box);
           encode_box(n, 1, R.box);
-          n.d.x = L.left >= 0 ? idx[b.left] : ~L.first;
-          n.d.y = R.left >= 0 ? idx[b.right] : ~R.first;
+          n.d.x = L.left >= 0 ? idx[b.left] : ~((L.first << 3) | L.count);
+          n.d.y = R.left >= 0 ? idx[b.right] : ~((R.first << 3) | R.count);
           n.d.z = L.left >= 0 ? 0 : L.count;
           n.d.w = R.left >= 0 ? 0 : R.count;
           out->bvh2[k] = n;
@@ -455,7 +455,8 @@ bool check_mesh_bvh(const float* P, const int* tris, int T, const MeshBvh& b, st
         if (child[s] < 0) {
           if (count[s] == 0) continue;
           if (!parent.contains(*cb[s]) && ni != 0) { *msg = "binary: child box outside parent"; return false; }
-          for (int i = ~child[s]; i < ~child[s] + count[s]; ++i) {
+          if ((~child[s] & 7) != count[s]) { *msg = "binary: leaf code and count disagree"; return false; }
+          for (int i = ~child[s] >> 3; i < (~child[s] >> 3) + count[s]; ++i) {
             if (i < 0 || i >= T) { *msg = "binary: triangle index out of range"; return false; }
             const int p = prim_of(b.bvh2_tris[3 * i]);
             if (p < 0 || p >= T || seen[p]++) { *msg = "binary: triangle referenced twice or invalid"; return false; }

@@ -357,6 +357,11 @@ int Scene::build_host(std::string* err) {
   auto t0 = std::chrono::steady_clock::now();
   const SceneHost& h = host;
   const int nm = h.num_meshes();
+  for (int i = 0; i < nm; ++i)
+    if (h.mesh_num_tris[i] >= (1 << 28)) {   // leaf codes hold the first triangle in 28 bits
+      *err = "mesh " + std::to_string(i) + " has 2^28 or more triangles";
+      return ILLUME_ERR_UNSUPPORTED;
+    }
   bvhs.assign(nm, MeshBvh{});
   const int nthreads = std::max(1, std::min<int>(nm, (int)std::thread::hardware_concurrency()));
   std::vector<std::thread> pool;

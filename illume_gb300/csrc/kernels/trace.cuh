@@ -181,14 +181,14 @@ __device__ __forceinline__ void traverse_bvh2(const DevMesh& m, const TraceRay& 
     if (h0) {
       if (d.x < 0) {
         if (COUNT) vc.tris += d.z;
-        for (int i = ~d.x; i < ~d.x + d.z; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
+        for (int i = ~d.x >> 3; i < (~d.x >> 3) + d.z; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
       }
       else inner0 = d.x;
     }
     if (h1) {
       if (d.y < 0) {
         if (COUNT) vc.tris += d.w;
-        for (int i = ~d.y; i < ~d.y + d.w; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
+        for (int i = ~d.y >> 3; i < (~d.y >> 3) + d.w; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
       }
       else inner1 = d.y;
     }
@@ -228,8 +228,9 @@ __device__ __forceinline__ void traverse_bvh2_ww(const DevMesh& m, const TraceRa
                           : box_hit(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0);
       const bool h1 = FMA ? box_hit_fma(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1)
                           : box_hit(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1);
-      int c0 = !h0 ? kEmpty : (d.x >= 0 ? d.x : (d.z > 0 ? ~((~d.x << 3) | d.z) : kEmpty));
-      int c1 = !h1 ? kEmpty : (d.y >= 0 ? d.y : (d.w > 0 ? ~((~d.y << 3) | d.w) : kEmpty));
+      // children are stored as visited: inner index, leaf code, or -1 for an empty slot
+      int c0 = h0 ? d.x : kEmpty;
+      int c1 = h1 ? d.y : kEmpty;
       if (c0 != kEmpty && c1 != kEmpty && te1 < te0) { const int t = c0; c0 = c1; c1 = t; }
       if (c0 == kEmpty) { c0 = c1; c1 = kEmpty; }
       if (c0 != kEmpty) {
