@@ -233,8 +233,8 @@ def run_ours(args):
     p.intersector = C.ISECT_WATERTIGHT
     p.accum_mode = C.ACCUM_FP32
     p.sample_begin = rank * 1_000_000
-    p.reserved[0] = args.trace_variant
-    p.reserved[1] = args.shade_variant
+    p.trace_variant = args.trace_variant
+    p.shade_variant = args.shade_variant
     r = Renderer(ctx, scene, params=p)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")   # > 129 MB L2
 

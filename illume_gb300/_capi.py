@@ -34,6 +34,7 @@ TONE_LINEAR, TONE_REINHARD, TONE_FILMIC, TONE_UNCHARTED = range(4)
 ISECT_MT, ISECT_WATERTIGHT = range(2)
 BVH_BINARY, BVH_WIDE8, BVH_WIDE8_PERSISTENT = range(3)
 ACCUM_FP32, ACCUM_KAHAN, ACCUM_FP64 = range(3)
+ESTIMATOR_REFERENCE, ESTIMATOR_NEE = range(2)
 SERVER_PATH_CAPACITY, SERVER_PASSES_PER_STEP, SERVER_AUTOTUNE, SERVER_TRACE_VARIANT = range(4)
 
 _pi32 = POINTER(c_int32)
@@ -76,7 +77,8 @@ class RenderParams(ctypes.Structure):
         ("sample_begin", c_int32), ("ray_bias", c_float), ("tonemapper", c_int32),
         ("seed", c_uint32), ("job", c_uint32), ("accum_mode", c_int32), ("intersector", c_int32),
         ("bvh_kind", c_int32), ("exact_hg", c_int32), ("samples_per_pass", c_int32),
-        ("camera", _pf), ("reserved", c_int32 * 4),
+        ("camera", _pf), ("trace_variant", c_int32), ("shade_variant", c_int32), ("estimator", c_int32),
+        ("reserved", c_int32),
     ]
 
 

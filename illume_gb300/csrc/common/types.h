@@ -33,8 +33,8 @@ enum EventClass : int {
 };
 
 // Binary BVH node (64 B): the boxes of both children are stored in the parent, so one
-// node fetch decides both children. child >= 0: inner node index; child < 0: leaf with
-// triangles [~child, ~child + count).
+// node fetch decides both children. child >= 0: inner node index; child <= -2: leaf
+// ~(first << 3 | count) with triangles [first, first + count); child == -1: empty slot.
 struct Bvh2Node {
   float4 a;   // c0.lo.x c0.lo.y c0.lo.z c0.hi.x
   float4 b;   // c0.hi.y c0.hi.z c1.lo.x c1.lo.y
@@ -101,6 +101,25 @@ struct DevTexture {
 
 struct DevMedium { float absorption[3]; float scattering, g; int active; int pad[2]; };
 
+// Light sampling data of a scene (the opt-in next-event estimator; the reference
+// estimator never reads it).
+struct LightView {
+  // environment: piecewise-constant density over the map's texels, proportional to
+  // luminance x cos(elevation); env_w == 0 when the environment is not sampled
+  int env_w, env_h;
+  const float* env_func;        // env_h x env_w texel weights
+  const float* env_marginal;    // env_h + 1 cumulative row weights (last = 1)
+  const float* env_cond;        // env_h x (env_w + 1) cumulative weights within each row
+  float env_integral;           // mean texel weight (density normaliser)
+  float env_prob;               // probability of sampling the environment rather than a triangle
+  // emissive triangles of mesh instances, world space, chosen by area x luminance
+  int num_tri;
+  const float4* tri;            // 3 float4 per light: (v0, area), (e1, select prob), (e2, instance / prim bits)
+  const float* tri_cdf;         // num_tri + 1 cumulative select probabilities
+  const int* inst_light_base;   // per instance: index of its first light (-1: not emissive)
+  int pad[2];
+};
+
 // Everything a kernel needs about a scene, passed by value as a kernel parameter.
 struct SceneView {
   const DevMesh* meshes;
@@ -111,7 +130,8 @@ struct SceneView {
   const DevMedium* mediums;
   int num_meshes, num_instances, num_spheres, num_materials;
   int env_tex;
-  int pad[3];
+  int pad;
+  const LightView* lights;      // device copy, read only by the next-event estimator
 };
 
 struct CameraView {

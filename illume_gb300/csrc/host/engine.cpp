@@ -13,6 +13,23 @@ void Engine::drop_graphs() {
   graphs.clear();
 }
 
+int Engine::ensure_shadow(std::string* err) {
+  if (s_orig.get() && s_orig.size() >= sizeof(float4) * (size_t)cap) return ILLUME_OK;
+  int st;
+  if ((st = s_orig.alloc(ctx, sizeof(float4) * (size_t)cap)) != ILLUME_OK) { *err = last_error(); return st; }
+  if ((st = s_dir.alloc(ctx, sizeof(float4) * (size_t)cap)) != ILLUME_OK) { *err = last_error(); return st; }
+  if ((st = s_val.alloc(ctx, sizeof(float4) * (size_t)cap)) != ILLUME_OK) { *err = last_error(); return st; }
+  drop_graphs();
+  point();
+  return ILLUME_OK;
+}
+
+bool Engine::any_nee() const {
+  for (const JobDesc& J : mirror)
+    if (J.nsamples > 0 && (J.flags & JOB_NEE)) return true;
+  return false;
+}
+
 int Engine::alloc_paths(std::string* err) {
   int st;
 #define ALLOC(buf, bytes) if ((st = (buf).alloc(ctx, (bytes))) != ILLUME_OK) { *err = last_error(); return st; }
@@ -40,6 +57,9 @@ void Engine::point() {
   w.evq = evq.as<int>();
   w.counters = counters.as<int>();
   w.contrib = contrib.as<float4>();
+  w.s_orig = s_orig.as<float4>();
+  w.s_dir = s_dir.as<float4>();
+  w.s_val = s_val.as<float4>();
   w.rays = rays.as<unsigned long long>();
   w.visits = visits.as<unsigned long long>();
   w.jobs = jobs.as<JobDesc>();
@@ -77,6 +97,8 @@ int Engine::init(Context* c, int nrows, int ncap, const RenderKnobs& k, std::str
   point();
   grid_trace = kernel_grid_blocks(trace_kernel_ptr(knobs.bvh_kind, knobs.trace_variant), 128, ctx->device);
   grid_shade = kernel_grid_blocks(shade_kernel_ptr(knobs.shade_variant), 128, ctx->device);
+  grid_shadow = kernel_grid_blocks(shadow_kernel_ptr(knobs.bvh_kind), 128, ctx->device);
+  grid_shade_nee = kernel_grid_blocks(shade_kernel_ptr(knobs.shade_variant, true), 128, ctx->device);
   return ILLUME_OK;
 }
 
@@ -87,7 +109,7 @@ int Engine::resize(int new_cap, std::string* err) {
   drop_graphs();
   const int old = cap;
   cap = new_cap;
-  const int st = alloc_paths(err);
+  int st = alloc_paths(err);
   if (st != ILLUME_OK) {
     cap = old;
     std::string e2;
@@ -95,6 +117,7 @@ int Engine::resize(int new_cap, std::string* err) {
     point();
     return st;
   }
+  if (s_orig.get() && (st = ensure_shadow(err)) != ILLUME_OK) return st;
   point();
   return ILLUME_OK;
 }
@@ -144,12 +167,13 @@ int Engine::free_rows() const {
   return n;
 }
 
-void Engine::launch_pass(cudaStream_t st, int depth) {
+void Engine::launch_pass(cudaStream_t st, int depth, bool nee) {
   launch_plan(w, st);
   launch_raygen(w, grid_raygen, st);
   for (int b = 0; b < depth; ++b) {
     launch_trace(w, knobs, b, grid_trace, st);
-    launch_shade(w, knobs, b, grid_shade, st);
+    launch_shade(w, knobs, b, nee ? grid_shade_nee : grid_shade, st, nee);
+    if (nee) launch_shadow(w, knobs, b, grid_shadow, st);
   }
   launch_accumulate(w, grid_acc, st);
   launch_advance(w, st);
@@ -162,11 +186,18 @@ int Engine::run(int npasses, int depth) {
     return ILLUME_ERR_INVALID;
   }
   cudaStream_t st = ctx->stream;
-  auto it = graphs.find(depth);
+  const bool nee = any_nee();
+  if (nee) {
+    std::string err;
+    const int s = ensure_shadow(&err);
+    if (s != ILLUME_OK) { set_error(err); return s; }
+  }
+  const int key = 2 * depth + (nee ? 1 : 0);
+  auto it = graphs.find(key);
   if (it == graphs.end()) {
     cudaGraph_t g;
     ILLUME_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    launch_pass(st, depth);
+    launch_pass(st, depth, nee);
     ILLUME_CUDA_TRY(cudaStreamEndCapture(st, &g));
     cudaGraphExec_t exec = nullptr;
     const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
@@ -175,15 +206,15 @@ int Engine::run(int npasses, int depth) {
       set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
       return ILLUME_ERR_CUDA;
     }
-    it = graphs.emplace(depth, exec).first;
+    it = graphs.emplace(key, exec).first;
   }
   for (int i = 0; i < npasses; ++i) {
     ILLUME_CUDA_TRY(cudaGraphLaunch(it->second, st));
     advance_mirror();
   }
   passes += npasses;
-  launches += (long long)npasses * launches_per_pass(depth);
-  ctx->launches += (long long)npasses * launches_per_pass(depth);
+  launches += (long long)npasses * launches_per_pass(depth, nee);
+  ctx->launches += (long long)npasses * launches_per_pass(depth, nee);
   return ILLUME_OK;
 }
 
@@ -193,6 +224,12 @@ int Engine::run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>&
     return ILLUME_ERR_INVALID;
   }
   cudaStream_t st = ctx->stream;
+  const bool nee = any_nee();
+  if (nee) {
+    std::string err;
+    const int s = ensure_shadow(&err);
+    if (s != ILLUME_OK) { set_error(err); return s; }
+  }
   ev.resize(3 + 2 * depth);
   for (auto& e : ev) ILLUME_CUDA_TRY(cudaEventCreate(&e));
   int k = 0;
@@ -203,7 +240,8 @@ int Engine::run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>&
   for (int b = 0; b < depth; ++b) {
     launch_trace(w, knobs, b, grid_trace, st, count_visits);
     cudaEventRecord(ev[k++], st);
-    launch_shade(w, knobs, b, grid_shade, st);
+    launch_shade(w, knobs, b, nee ? grid_shade_nee : grid_shade, st, nee);
+    if (nee) launch_shadow(w, knobs, b, grid_shadow, st);
     cudaEventRecord(ev[k++], st);
   }
   launch_accumulate(w, grid_acc, st);
@@ -212,8 +250,8 @@ int Engine::run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>&
   ILLUME_CUDA_TRY(cudaGetLastError());
   advance_mirror();
   passes += 1;
-  launches += launches_per_pass(depth);
-  ctx->launches += launches_per_pass(depth);
+  launches += launches_per_pass(depth, nee);
+  ctx->launches += launches_per_pass(depth, nee);
   return ILLUME_OK;
 }
 
@@ -227,7 +265,8 @@ int Engine::read_row_rays(int r, unsigned long long* out) {
 size_t Engine::device_bytes() const {
   size_t b = 0;
   const DevBuffer* all[] = {&q_orig[0], &q_orig[1], &q_dir[0], &q_dir[1], &q_thr[0], &q_thr[1], &hit, &hit_geom,
-                            &evq, &counters, &contrib, &rays, &visits, &jobs, &path_base, &pixel_base};
+                            &evq, &counters, &contrib, &rays, &visits, &jobs, &path_base, &pixel_base,
+                            &s_orig, &s_dir, &s_val};
   for (const DevBuffer* d : all) b += d->size();
   return b;
 }

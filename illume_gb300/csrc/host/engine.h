@@ -24,10 +24,11 @@ struct Engine {
   RenderKnobs knobs{};
   DevBuffer q_orig[2], q_dir[2], q_thr[2], hit, hit_geom, evq, counters, contrib, rays, visits;
   DevBuffer jobs, path_base, pixel_base;
+  DevBuffer s_orig, s_dir, s_val;   // shadow rays (allocated when a job uses next-event estimation)
   WaveBuffers w{};
   std::vector<JobDesc> mirror;   // the table as the device has it after the launched passes
-  int grid_trace = 0, grid_shade = 0, grid_raygen = 0, grid_acc = 0;
-  std::map<int, cudaGraphExec_t> graphs;   // captured pass by depth
+  int grid_trace = 0, grid_shade = 0, grid_raygen = 0, grid_acc = 0, grid_shadow = 0, grid_shade_nee = 0;
+  std::map<int, cudaGraphExec_t> graphs;   // captured pass by (depth, shadow stage)
   long long passes = 0, launches = 0;
 
   Engine() = default;
@@ -51,14 +52,16 @@ struct Engine {
   int read_row_rays(int r, unsigned long long* out);   // synchronous
   int free_rows() const;
   long long paths_in_pass() const;                      // of the next pass, from the mirror
-  static int launches_per_pass(int depth) { return 5 + 2 * depth; }
+  static int launches_per_pass(int depth, bool nee = false) { return 5 + (nee ? 3 : 2) * depth; }
+  bool any_nee() const;   // a job of the next pass uses next-event estimation
   size_t device_bytes() const;
 
  private:
   int alloc_paths(std::string* err);
   void point();
   void advance_mirror();
-  void launch_pass(cudaStream_t st, int depth);
+  void launch_pass(cudaStream_t st, int depth, bool nee);
+  int ensure_shadow(std::string* err);
   void drop_graphs();
 };
 

@@ -36,10 +36,11 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if ((long long)p.width * p.height > (1LL << 28)) { *err = "image too large"; return ILLUME_ERR_INVALID; }
   if (p.intersector != ISECT_MT && p.intersector != ISECT_WATERTIGHT) { *err = "unknown intersector"; return ILLUME_ERR_INVALID; }
   if (p.bvh_kind < BVH_BINARY || p.bvh_kind > 2) { *err = "unknown BVH kind"; return ILLUME_ERR_INVALID; }
-  if (p.bvh_kind == BVH_BINARY && (p.reserved[0] < 0 || p.reserved[0] > 3)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
+  if (p.bvh_kind == BVH_BINARY && (p.trace_variant < 0 || p.trace_variant > 3)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.accum_mode < ACCUM_FP32 || p.accum_mode > ACCUM_FP64) { *err = "unknown accumulation mode"; return ILLUME_ERR_INVALID; }
   if (p.samples_per_pass < 0) { *err = "negative samples per pass"; return ILLUME_ERR_INVALID; }
-  if (p.reserved[1] < 0 || p.reserved[1] > 1) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
+  if (p.shade_variant < 0 || p.shade_variant > 1) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
+  if (p.estimator < ILLUME_ESTIMATOR_REFERENCE || p.estimator > ILLUME_ESTIMATOR_NEE) { *err = "unknown estimator"; return ILLUME_ERR_INVALID; }
   if ((int)scene.t_mediums.size() > kMaxMediums) { *err = "too many mediums"; return ILLUME_ERR_UNSUPPORTED; }
   if (!scene.ctx || !scene.view_dev) { *err = "scene has not been uploaded to a device"; return ILLUME_ERR_INVALID; }
   return ILLUME_OK;
@@ -49,8 +50,8 @@ RenderKnobs render_knobs(const illume_render_params& p) {
   RenderKnobs k{};
   k.isect = p.intersector;
   k.bvh_kind = p.bvh_kind == 2 ? BVH_WIDE8 : p.bvh_kind;
-  k.trace_variant = p.bvh_kind == 2 ? 1 : (p.bvh_kind == BVH_BINARY ? p.reserved[0] : 0);
-  k.shade_variant = p.reserved[1];
+  k.trace_variant = p.bvh_kind == 2 ? 1 : (p.bvh_kind == BVH_BINARY ? p.trace_variant : 0);
+  k.shade_variant = p.shade_variant;
   return k;
 }
 
@@ -64,7 +65,7 @@ JobDesc job_row(const Scene& scene, const illume_render_params& p, const Accumul
   J.job = p.job;
   J.max_depth = p.max_depth;
   J.ray_bias = p.ray_bias;
-  J.exact_hg = p.exact_hg;
+  J.flags = (p.exact_hg ? JOB_EXACT_HG : 0) | (p.estimator == ILLUME_ESTIMATOR_NEE ? JOB_NEE : 0);
   J.accum_mode = p.accum_mode;
   J.npix = p.width * p.height;
   J.width = p.width;
@@ -151,7 +152,7 @@ int Renderer::render_device(bool accumulate, illume_render_stats* stats) {
     stats->rays = (int64_t)(rays_after - rays_before);
     stats->paths = (int64_t)spp * npix;
     stats->render_ms = ms;
-    stats->kernel_launches = (int64_t)npasses * Engine::launches_per_pass(p.max_depth);
+    stats->kernel_launches = (int64_t)npasses * Engine::launches_per_pass(p.max_depth, p.estimator == ILLUME_ESTIMATOR_NEE);
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
     stats->h2d_bytes = 4 * sizeof(int);
     stats->d2h_bytes = 16;

@@ -523,12 +523,35 @@ int Scene::build_and_upload(std::string* err) {
   UP(mats.data(), mats.size() * sizeof(DevMaterial), v.materials);
   UP(texs.data(), texs.size() * sizeof(DevTexture), v.textures);
   UP(meds.data(), meds.size() * sizeof(DevMedium), v.mediums);
-#undef UP
   v.num_meshes = nm;
   v.num_instances = ni;
   v.num_spheres = ns;
   v.num_materials = nmat;
   v.env_tex = h.env_tex;
+  // light sampling tables of the next-event estimator
+  build_lights(h, &lights_host);
+  {
+    const HostLights& L = lights_host;
+    LightView lv{};
+    lv.env_w = L.env_w;
+    lv.env_h = L.env_h;
+    lv.env_integral = L.env_integral;
+    lv.env_prob = L.env_prob;
+    if (L.env_w > 0) {
+      UP(L.env_func.data(), L.env_func.size() * sizeof(float), lv.env_func);
+      UP(L.env_marginal.data(), L.env_marginal.size() * sizeof(float), lv.env_marginal);
+      UP(L.env_cond.data(), L.env_cond.size() * sizeof(float), lv.env_cond);
+    }
+    lv.num_tri = (int)L.tri_cdf.size() > 0 ? (int)L.tri_cdf.size() - 1 : 0;
+    if (lv.num_tri > 0) {
+      UP(L.tri.data(), L.tri.size() * sizeof(float4), lv.tri);
+      UP(L.tri_cdf.data(), L.tri_cdf.size() * sizeof(float), lv.tri_cdf);
+    }
+    if (!L.inst_light_base.empty()) UP(L.inst_light_base.data(), L.inst_light_base.size() * sizeof(int), lv.inst_light_base);
+    lights_view = lv;
+    UP(&lights_view, sizeof(LightView), v.lights);
+  }
+#undef UP
   view = v;
   {
     void* p_ = nullptr;

@@ -11,6 +11,7 @@
 
 #include "../common/types.h"
 #include "bvh_build.h"
+#include "lights.h"
 #include "../../../include/illume.h"
 
 namespace illume {
@@ -100,6 +101,8 @@ struct Scene {
   std::vector<std::unique_ptr<DevBuffer>> buffers;
   SceneView view{};
   SceneView* view_dev = nullptr;   // device copy of `view`
+  HostLights lights_host;           // light sampling tables (host copies)
+  LightView lights_view{};          // host source of the device light view
   size_t device_bytes = 0;
   size_t trace_bytes[2] = {0, 0};   // node + triangle bytes a traversal reads: binary, 8-wide
   // device tables (kept for re-uploads) and the host source of every device buffer

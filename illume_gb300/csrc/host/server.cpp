@@ -383,10 +383,11 @@ int Server::step(int* running_out) {
     }
     if (depth == 0 && e.paths_in_pass() == 0) continue;
     k = std::max(k, 1);
+    const int per_pass_launches = Engine::launches_per_pass(depth, e.any_nee());
     ILLUME_CUDA_TRY(cudaEventRecord(ev0, ctx->stream));
     if ((st = e.run(k, depth)) != ILLUME_OK) return st;
     ILLUME_CUDA_TRY(cudaEventRecord(ev1, ctx->stream));
-    for (int r : active) jobs[se.row_job[r]]->stats.kernel_launches += (int64_t)k * Engine::launches_per_pass(depth);
+    for (int r : active) jobs[se.row_job[r]]->stats.kernel_launches += (int64_t)k * per_pass_launches;
     unsigned long long total = 0;
     ILLUME_CUDA_TRY(cudaMemcpyAsync(&total, e.w.rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
     ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
@@ -396,7 +397,7 @@ int Server::step(int* running_out) {
     se.rays_seen = total;
     totals.rays += (int64_t)rays;
     totals.passes += k;
-    totals.kernel_launches += (int64_t)k * Engine::launches_per_pass(depth);
+    totals.kernel_launches += (int64_t)k * per_pass_launches;
     totals.device_ms += ms;
     if ((st = retire(se, &done)) != ILLUME_OK) return st;
     if (autotune && se.tune_state != 2) tune(se, rays, ms);

@@ -10,6 +10,7 @@
 // depends only on its own job row (scene, camera, Philox key, sample index), never on
 // which other jobs share the pass.
 #include "launch.h"
+#include "nee.cuh"
 #include "shading.cuh"
 #include "../common/philox.cuh"
 
@@ -97,6 +98,8 @@ __global__ void __launch_bounds__(1024) k_plan(WaveBuffers w) {
     w.counters[1] = 0;
     w.counters[44] = 0;   // trace ray-fetch counters by bounce parity
     w.counters[45] = 0;
+    w.counters[46] = 0;   // shadow-ray counts by bounce parity
+    w.counters[47] = 0;
     if (over) w.counters[42] = 1;
     for (int c = 0; c < EV_COUNT; ++c) ev_counts2(w, 0)[c] = 0;
   }
@@ -136,6 +139,18 @@ __global__ void __launch_bounds__(256) k_raygen(WaveBuffers w) {
   }
 }
 
+// A path's radiance: the reference estimator ends a path at its one contribution, so
+// the slot is written once; with next-event estimation contributions add up.
+template <bool NEE>
+__device__ __forceinline__ void add_radiance(float4* c, V3 L) {
+  if (NEE) {
+    const float4 v = *c;
+    *c = make_float4(v.x + L.x, v.y + L.y, v.z + L.z, 0.0f);
+  } else {
+    *c = make_float4(L.x, L.y, L.z, 0.0f);
+  }
+}
+
 struct BounceRng {
   RngStream s;
   __device__ __forceinline__ float operator()() { return s.next(); }
@@ -143,7 +158,9 @@ struct BounceRng {
 
 // Shading of one bounce over the material-sorted event queues. MINB = blocks of 128
 // threads per SM the register allocation must allow (1 = the compiler's choice).
-template <int MINB>
+// NEE: the instance with the next-event estimator compiled in (launched only when a job
+// of the pass uses it; its extra registers stay out of the reference path).
+template <int MINB, bool NEE>
 __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) {
   const int parity = bounce & 1;
   const int* counts = ev_counts2(w, parity);
@@ -163,9 +180,10 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) 
   int* next_count = w.counters + (parity ^ 1);
   for (int base = blockIdx.x * blockDim.x; base < total; base += gridDim.x * blockDim.x) {
     const int gi = base + threadIdx.x;
-    bool cont = false;
+    bool cont = false, shadow = false;
     int myjob = -1;
     float4 no = make_float4(0, 0, 0, 0), nd = no, nt = no;
+    float4 so = no, sd = no, sv = no;
     const unsigned live = __ballot_sync(0xffffffffu, gi < total);
     if (gi < total) {
       int cls = 0;
@@ -193,13 +211,15 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) 
                  J.job);
       float4* contrib = w.contrib + g;
       const bool last = bounce + 1 >= J.max_depth;
+      const bool nee = NEE && (J.flags & JOB_NEE) != 0;
+      const float pdf_prev = qt.w;   // density of the BSDF sample that led here (next-event paths)
       if (medium >= 0 && sc.mediums[medium].active) {
         const DevMedium md = sc.mediums[medium];
         const float u = rng();
         const float dist = -logf(u) / md.scattering;
         if (cls == EV_MEDIUM) {
           const float u1 = rng(), u2 = rng();
-          const V3 dir = to_basis(sample_hg(md.g, u1, u2, J.exact_hg != 0), d);
+          const V3 dir = to_basis(sample_hg(md.g, u1, u2, (J.flags & JOB_EXACT_HG) != 0), d);
           const V3 no3 = add(o, mul(d, dist));
           const V3 nd3 = normalize(dir);
           thr = mulv(thr, v3(expf(-1.0f * dist * md.absorption[0]), expf(-1.0f * dist * md.absorption[1]),
@@ -216,8 +236,9 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) 
                            expf(-1.0f * t * md.absorption[2])));
       }
       if (cls == EV_MISS) {
-        const V3 L = mulv(thr, env_eval(sc, d));
-        *contrib = make_float4(L.x, L.y, L.z, 0.0f);
+        V3 L = mulv(thr, env_eval(sc, d));
+        if (nee && pdf_prev > 0.0f) L = mul(L, power_heuristic(pdf_prev, env_light_pdf(*sc.lights, d)));
+        add_radiance<NEE>(contrib, L);
         goto done;
       }
       {
@@ -266,11 +287,49 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) 
         const V3 albedo = tex_eval(sc, mat.albedo_tex, uv0, uv1);
         const float roughness = tex_eval(sc, mat.roughness_tex, uv0, uv1).x;
         if (mat.type == MAT_EMISSIVE) {
-          const V3 L = mulv(thr, albedo);
-          *contrib = make_float4(L.x, L.y, L.z, 0.0f);
+          V3 L = mulv(thr, albedo);
+          if (nee && pdf_prev > 0.0f && geom >= 0) {
+            const LightView& LV = *sc.lights;
+            const int base = LV.num_tri > 0 ? __ldg(LV.inst_light_base + geom) : -1;
+            if (base >= 0) {
+              const int l = base + __float_as_int(hv.w);
+              const float4 e1 = __ldg(&LV.tri[3 * l + 1]), e2 = __ldg(&LV.tri[3 * l + 2]);
+              const V3 ln = cross(v3(e1.x, e1.y, e1.z), v3(e2.x, e2.y, e2.z));
+              const float lnl = sqrtf(dot(ln, ln));
+              const float cos_l = lnl > 0.0f ? dot(ln, d) / lnl : 0.0f;
+              L = mul(L, power_heuristic(pdf_prev, tri_light_pdf(LV, l, t, cos_l)));
+            }
+          }
+          add_radiance<NEE>(contrib, L);
           goto done;
         }
         if (last) goto done;   // the path has used all its closest-hit queries
+        // next-event estimation: one light sample at a non-delta reflection vertex in air
+        if (nee && (medium < 0 || !sc.mediums[medium].active) &&
+            (mat.type == MAT_LAMBERT || mat.type == MAT_ROUGHCONDUCTOR || mat.type == MAT_ROUGHREFLECTIVE)) {
+          RngStream nr;
+          nr.init((uint32_t)(pid % npix), (uint32_t)(J.sample_base + pid / npix), 0x40000000u | (uint32_t)(bounce + 1),
+                  J.seed, J.job);
+          const float u0 = nr.next(), u1 = nr.next(), u2 = nr.next();
+          const V3 ph = add(o, mul(d, t));
+          const LightSample ls = sample_light(sc, *sc.lights, ph, u0, u1, u2);
+          V3 fcos;
+          float pdf_b = 0.0f;
+          if (ls.ok && bsdf_eval_cos(mat, d, N, albedo, roughness, ls.dir, fcos, pdf_b)) {
+            const V3 Cn = mul(mulv(mulv(thr, fcos), ls.Le), power_heuristic(ls.pdf, pdf_b) / ls.pdf);
+            if (isfinite(Cn.x + Cn.y + Cn.z) && (Cn.x > 0.0f || Cn.y > 0.0f || Cn.z > 0.0f)) {
+              const V3 norm_o = mul(N, dot(N, d) > 0.0f ? -1.0f : 1.0f);
+              const V3 org = add(ph, mul(norm_o, J.ray_bias));
+              const float tmax = ls.dist == FLT_MAX ? FLT_MAX : ls.dist * (1.0f - 1e-4f) - J.ray_bias;
+              if (tmax > 0.0f) {
+                shadow = true;
+                so = make_float4(org.x, org.y, org.z, __int_as_float(job));
+                sd = make_float4(ls.dir.x, ls.dir.y, ls.dir.z, tmax);
+                sv = make_float4(Cn.x, Cn.y, Cn.z, __int_as_float(g));
+              }
+            }
+          }
+        }
         const ScatterResult s = scatter(mat, d, N, albedo, roughness, rng);
         if (s.status == SCATTER_KILLED) goto done;
         if (s.medium != kMediumUnchanged) medium = s.medium;
@@ -280,12 +339,27 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) 
         cont = true;
         no = make_float4(p.x, p.y, p.z, qo.w);
         nd = make_float4(dir.x, dir.y, dir.z, pack_job_medium(job, medium));
-        nt = make_float4(thr.x, thr.y, thr.z, 0.0f);
+        nt = make_float4(thr.x, thr.y, thr.z, nee ? bsdf_sampled_pdf(mat, s, d, N) : 0.0f);
       }
     done:;
       // closest-hit queries of this bounce, per job
       const unsigned peers = __match_any_sync(live, myjob);
       if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&w.jobs[myjob].rays, (unsigned long long)__popc(peers));
+    }
+    // compacted append of the shadow rays of this bounce
+    const unsigned sballot = NEE ? __ballot_sync(0xffffffffu, shadow) : 0u;
+    if (NEE && sballot) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(sballot) - 1;
+      int slot = 0;
+      if (lane == leader) slot = atomicAdd(w.counters + 46 + parity, __popc(sballot));
+      slot = __shfl_sync(0xffffffffu, slot, leader);
+      if (shadow) {
+        const int j = slot + __popc(sballot & ((1u << lane) - 1));
+        w.s_orig[j] = so;
+        w.s_dir[j] = sd;
+        w.s_val[j] = sv;
+      }
     }
     // compacted append of the continuing paths into the next bounce's queue
     const unsigned ballot = __ballot_sync(0xffffffffu, cont);
@@ -465,8 +539,9 @@ __global__ void k_bsdf_batch(int type, int dist, const float* in, int n, float* 
 // Shade kernel variants (RenderKnobs::shade_variant): 0 = compiler's register choice (72,
 // the default), 1 = at most 64 registers (8 blocks of 128 per SM: more loads in flight,
 // but the spills it needs cost more; measured slower on the traversal workload).
-const void* shade_kernel_ptr(int variant) {
-  return variant == 1 ? (const void*)k_shade<8> : (const void*)k_shade<1>;
+const void* shade_kernel_ptr(int variant, bool nee) {
+  if (nee) return variant == 1 ? (const void*)k_shade<8, true> : (const void*)k_shade<1, true>;
+  return variant == 1 ? (const void*)k_shade<8, false> : (const void*)k_shade<1, false>;
 }
 
 void launch_plan(const WaveBuffers& w, cudaStream_t st) {
@@ -474,9 +549,14 @@ void launch_plan(const WaveBuffers& w, cudaStream_t st) {
   k_plan<<<1, threads > 32 ? threads : 32, 0, st>>>(w);
 }
 void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st) { k_raygen<<<grid, 256, 0, st>>>(w); }
-void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st) {
-  if (k.shade_variant == 1) k_shade<8><<<grid, 128, 0, st>>>(w, bounce);
-  else k_shade<1><<<grid, 128, 0, st>>>(w, bounce);
+void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st, bool nee) {
+  if (nee) {
+    if (k.shade_variant == 1) k_shade<8, true><<<grid, 128, 0, st>>>(w, bounce);
+    else k_shade<1, true><<<grid, 128, 0, st>>>(w, bounce);
+  } else {
+    if (k.shade_variant == 1) k_shade<8, false><<<grid, 128, 0, st>>>(w, bounce);
+    else k_shade<1, false><<<grid, 128, 0, st>>>(w, bounce);
+  }
 }
 void launch_accumulate(const WaveBuffers& w, int grid, cudaStream_t st) { k_accumulate<<<grid, 256, 0, st>>>(w); }
 void launch_advance(const WaveBuffers& w, cudaStream_t st) {

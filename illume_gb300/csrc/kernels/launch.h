@@ -28,7 +28,7 @@ struct JobDesc {
   uint32_t seed, job;        // Philox key
   int max_depth;             // closest-hit queries per path
   float ray_bias;
-  int exact_hg, accum_mode;
+  int flags, accum_mode;      // flags: JOB_EXACT_HG, JOB_NEE
   int npix, width;
   // pass state: samples [sample_base, sample_base + nsamples) of every pixel are in the
   // current pass; advanced by k_advance after every pass; nsamples == 0 = idle row
@@ -38,6 +38,7 @@ struct JobDesc {
   unsigned long long rays;   // closest-hit queries traced for this job (running total)
 };
 static_assert(sizeof(JobDesc) == 256, "JobDesc layout");
+enum JobFlags : int { JOB_EXACT_HG = 1, JOB_NEE = 2 };
 
 // A queued ray's fourth direction word packs its job row and medium:
 // (job << kMediumBits) | (medium + 1), medium -1 = air.
@@ -56,6 +57,9 @@ struct WaveBuffers {
   int* evq;              // EV_COUNT queues of `cap` slot indices each
   int* counters;         // see kCounter* below
   float4* contrib;       // per path radiance of the current pass
+  float4* s_orig;        // shadow rays of the next-event estimator: origin, job row (int bits)
+  float4* s_dir;         //   direction, maximum distance
+  float4* s_val;         //   contribution if unoccluded, path slot (int bits)
   unsigned long long* rays;   // closest-hit queries traced (running total)
   unsigned long long* visits; // [node fetches, triangle tests] of the instrumented trace kernel
   JobDesc* jobs;
@@ -66,7 +70,8 @@ struct WaveBuffers {
 };
 
 // counters[]: [0..1] queue sizes by parity, [2 + 16 * parity + class] event counts,
-// [kCounterPaths] paths of the pass, [kCounterPixels] pixels of the pass.
+// [kCounterPaths] paths of the pass, [kCounterPixels] pixels of the pass, [42] slot
+// overflow flag, [44 + parity] trace ray-fetch counters, [46 + parity] shadow-ray counts.
 static constexpr int kCounterPaths = 40;
 static constexpr int kCounterPixels = 41;
 static constexpr int kCounterWords = 64;
@@ -85,7 +90,8 @@ void launch_plan(const WaveBuffers& w, cudaStream_t st);
 void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st);
 void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st,
                   bool count_visits = false);
-void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st);
+void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st, bool nee = false);
+void launch_shadow(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st);
 void launch_accumulate(const WaveBuffers& w, int grid, cudaStream_t st);
 void launch_advance(const WaveBuffers& w, cudaStream_t st);
 void launch_tonemap(const Accumulators& acc, int accum_mode, int npix, float samples, int op, uint8_t* rgb8,
@@ -99,6 +105,7 @@ void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float
 void launch_bsdf_batch(int type, int distribution, const float* in, int n, float* out, cudaStream_t st);
 
 const void* trace_kernel_ptr(int bvh_kind, int variant = 0);
-const void* shade_kernel_ptr(int variant = 0);
+const void* shade_kernel_ptr(int variant = 0, bool nee = false);
+const void* shadow_kernel_ptr(int bvh_kind);
 
 }  // namespace illume

@@ -76,6 +76,10 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
   }
   if (p.spp < 0 || p.max_depth < 0) { set_error("negative spp or depth"); return ILLUME_ERR_INVALID; }
   if (p.accum_mode != ILLUME_ACCUM_FP32) { set_error("illume_render_noalloc accumulates in FP32 only"); return ILLUME_ERR_INVALID; }
+  if (p.estimator != ILLUME_ESTIMATOR_REFERENCE) {
+    set_error("illume_render_noalloc runs the reference estimator only (no shadow-ray scratch)");
+    return ILLUME_ERR_UNSUPPORTED;
+  }
   if (p.intersector != ILLUME_ISECT_MT && p.intersector != ILLUME_ISECT_WATERTIGHT) { set_error("unknown intersector"); return ILLUME_ERR_INVALID; }
   if (p.bvh_kind != ILLUME_BVH_BINARY && p.bvh_kind != ILLUME_BVH_WIDE8) { set_error("unknown BVH kind"); return ILLUME_ERR_INVALID; }
   const int dev = ctx->c.device;

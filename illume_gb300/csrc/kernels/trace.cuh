@@ -442,11 +442,12 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 
 // Full closest-hit query for a world-space ray (direction used as given).
 template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false>
+// tmax: only hits closer than tmax count (shadow rays).
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
-                                                 VisitCount* vcp = nullptr) {
+                                                 VisitCount* vcp = nullptr, float tmax = FLT_MAX) {
   VisitCount vc;
   HitRecord h;
-  h.t = FLT_MAX; h.u = 0.0f; h.v = 0.0f; h.prim = -1; h.geom = -1;
+  h.t = tmax; h.u = 0.0f; h.v = 0.0f; h.prim = -1; h.geom = -1;
   // spheres (src/primitives/sphere.cu:43-77)
   for (int s = 0; s < sc.num_spheres; ++s) {
     const DevSphere sp = sc.spheres[s];

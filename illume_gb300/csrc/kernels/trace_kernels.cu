@@ -96,6 +96,37 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
   }
 }
 
+// Shadow rays of the next-event estimator: a contribution is added to its path's
+// radiance when nothing lies within the ray's maximum distance.
+template <int KIND>
+__global__ void __launch_bounds__(128, 8) k_shadow(WaveBuffers w, RenderKnobs k, int bounce) {
+  const int parity = bounce & 1;
+  const int n = w.counters[46 + parity];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    w.counters[46 + (parity ^ 1)] = 0;
+    atomicAdd(w.rays, (unsigned long long)n);
+  }
+  typename std::conditional<KIND == BVH_WIDE8, uint2, int>::type stack[kStack];
+  for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const int i = base + threadIdx.x;
+    const bool valid = i < n;
+    const unsigned mask = __ballot_sync(0xffffffffu, valid);
+    if (!valid) continue;
+    const float4 so = w.s_orig[i], sd = w.s_dir[i], sv = w.s_val[i];
+    const int job = __float_as_int(so.w);
+    const SceneView& sc = w.jobs[job].sc;
+    const HitRecord h = closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY>(
+        sc, v3(so.x, so.y, so.z), v3(sd.x, sd.y, sd.z), k.isect, stack, nullptr, sd.w);
+    if (h.geom == -1) {
+      float4* c = w.contrib + __float_as_int(sv.w);
+      const float4 v = *c;
+      *c = make_float4(v.x + sv.x, v.y + sv.y, v.z + sv.z, v.w);
+    }
+    const unsigned peers = __match_any_sync(mask, job);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&w.jobs[job].rays, (unsigned long long)__popc(peers));
+  }
+}
+
 // Persistent trace kernel for the 8-wide BVH. Each lane owns one ray at a time and walks
 // it through a small state machine (spheres at load, then per instance: box cull, object
 // ray set-up, traversal steps); every loop iteration runs one traversal step per lane,
@@ -306,6 +337,15 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
   }
   if (count_visits) k_trace<BVH_BINARY, true, 8, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
   else k_trace<BVH_BINARY, false, 8, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
+}
+
+const void* shadow_kernel_ptr(int bvh_kind) {
+  return bvh_kind == BVH_WIDE8 ? (const void*)k_shadow<BVH_WIDE8> : (const void*)k_shadow<BVH_BINARY>;
+}
+
+void launch_shadow(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st) {
+  if (k.bvh_kind == BVH_WIDE8) k_shadow<BVH_WIDE8><<<grid, 128, 0, st>>>(w, k, bounce);
+  else k_shadow<BVH_BINARY><<<grid, 128, 0, st>>>(w, k, bounce);
 }
 
 void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float* rays8, int n, int isect,

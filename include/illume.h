@@ -58,6 +58,11 @@ enum illume_intersector { ILLUME_ISECT_MT = 0, ILLUME_ISECT_WATERTIGHT = 1 };
  * persistent kernel that schedules node and triangle steps per warp. */
 enum illume_bvh_kind { ILLUME_BVH_BINARY = 0, ILLUME_BVH_WIDE8 = 1, ILLUME_BVH_WIDE8_PERSISTENT = 2 };
 enum illume_accum_mode { ILLUME_ACCUM_FP32 = 0, ILLUME_ACCUM_KAHAN = 1, ILLUME_ACCUM_FP64 = 2 };
+/* REFERENCE: paths find light only by BSDF sampling, as src/renderer.cu:183-386 (the
+ * default; every parity test runs it). NEE: adds next-event estimation with multiple
+ * importance sampling at lambert, rough conductor and rough dielectric reflection
+ * vertices (environment map and emissive mesh triangles); same expectation, less noise. */
+enum illume_estimator { ILLUME_ESTIMATOR_REFERENCE = 0, ILLUME_ESTIMATOR_NEE = 1 };
 
 /* ---- reference output types: same layout as src/bitmap.h:6-20 ---- */
 typedef struct { size_t red, green, blue; } illume_pixel;
@@ -152,12 +157,13 @@ typedef struct {
    * floats of the camera-to-world rows (3x4, the layout of illume_scene_desc's
    * camera_transform), then fov (degrees), dof and aperture. NULL = the scene's camera. */
   const float* camera;
-  int32_t reserved[4];        /* reserved[0]: binary-BVH trace kernel variant: 0 = 64 registers, fused box
-                               * tests, dynamic ray fetch, while-while traversal (default); 1 = compiler's
-                               * register choice, grid-stride rays, leaves tested where met; 2 = variant 1
-                               * held to 64 registers; 3 = variant 0 with leaves tested where met.
-                               * reserved[1]: shade kernel variant: 0 = compiler's register choice
-                               * (default), 1 = at most 64 registers. */
+  int32_t trace_variant;      /* binary BVH: 0 = 64 registers, fused box tests, dynamic ray fetch,
+                               * while-while traversal (default); 1 = compiler's register choice,
+                               * grid-stride rays, leaves tested where met; 2 = variant 1 held to 64
+                               * registers; 3 = variant 0 with leaves tested where met */
+  int32_t shade_variant;      /* 0 = compiler's register choice (default), 1 = at most 64 registers */
+  int32_t estimator;          /* illume_estimator */
+  int32_t reserved;
 } illume_render_params;
 
 typedef struct {
