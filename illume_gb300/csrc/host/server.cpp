@@ -465,7 +465,7 @@ int Server::set_option(int option, int64_t value) {
       autotune = value != 0;
       return ILLUME_OK;
     case ILLUME_SERVER_TRACE_VARIANT:
-      if (value < -1 || value > 3) { set_error("unknown trace kernel variant"); return ILLUME_ERR_INVALID; }
+      if (value < -1 || value > 4) { set_error("unknown trace kernel variant"); return ILLUME_ERR_INVALID; }
       trace_variant = (int)value;
       return ILLUME_OK;
     default:

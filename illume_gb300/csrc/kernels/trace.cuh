@@ -210,54 +210,63 @@ __device__ __forceinline__ void traverse_bvh2(const DevMesh& m, const TraceRay& 
 // the first leaf it meets; the warp leaves the node loop once every lane still in it
 // holds a leaf, and then tests those leaves together. Stack entries are inner node
 // indices (>= 0) or leaf codes ~(first << 3 | count) (<= -2); -1 is empty.
+static constexpr int kEmptyEntry = -1;
+
+// One while-while round: inner nodes until every lane still in the loop holds a leaf (or
+// this lane has nothing left), then the set-aside leaves. cur / leaf / sp carry the
+// traversal between rounds; visits bounds the node fetches of one ray.
+template <bool COUNT, bool FMA>
+__device__ __forceinline__ void ww_round(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best, int* stack,
+                                         int& cur, int& leaf, int& sp, int& visits, VisitCount& vc) {
+  constexpr int kEmpty = kEmptyEntry;
+  while (cur >= 0) {
+    if (COUNT) vc.nodes++;
+    if (++visits > kMaxNodeVisits) { cur = kEmpty; leaf = kEmpty; sp = 0; break; }
+    const Bvh2Node* n = m.bvh2 + cur;
+    const float4 a = __ldg(&n->a), b = __ldg(&n->b), c = __ldg(&n->c);
+    const int4 d = __ldg(&n->d);
+    float te0, te1;
+    const bool h0 = FMA ? box_hit_fma(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0)
+                        : box_hit(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0);
+    const bool h1 = FMA ? box_hit_fma(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1)
+                        : box_hit(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1);
+    // children are stored as visited: inner index, leaf code, or -1 for an empty slot
+    int c0 = h0 ? d.x : kEmpty;
+    int c1 = h1 ? d.y : kEmpty;
+    if (c0 != kEmpty && c1 != kEmpty && te1 < te0) { const int t = c0; c0 = c1; c1 = t; }
+    if (c0 == kEmpty) { c0 = c1; c1 = kEmpty; }
+    if (c0 != kEmpty) {
+      cur = c0;
+      if (c1 != kEmpty && sp < kStack) stack[sp++] = c1;
+    } else {
+      cur = sp > 0 ? stack[--sp] : kEmpty;
+    }
+    if (cur < kEmpty && leaf == kEmpty) {
+      leaf = cur;
+      cur = sp > 0 ? stack[--sp] : kEmpty;
+    }
+    if (__all_sync(__activemask(), leaf != kEmpty)) break;
+  }
+  while (leaf != kEmpty) {
+    const int code = ~leaf;
+    const int first = code >> 3, count = code & 7;
+    if (COUNT) vc.tris += count;
+    for (int i = first; i < first + count; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
+    leaf = kEmpty;
+    if (cur < kEmpty) {
+      leaf = cur;
+      cur = sp > 0 ? stack[--sp] : kEmpty;
+    }
+  }
+}
+
 template <bool COUNT, bool FMA>
 __device__ __forceinline__ void traverse_bvh2_ww(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
                                                  int* stack, VisitCount& vc) {
-  constexpr int kEmpty = -1;
-  int sp = 0;
-  int cur = 0;          // next entry: inner node, leaf code or kEmpty
-  int leaf = kEmpty;    // leaf set aside
-  for (int guard = 0; guard < kMaxNodeVisits; ++guard) {
-    while (cur >= 0) {
-      if (COUNT) vc.nodes++;
-      const Bvh2Node* n = m.bvh2 + cur;
-      const float4 a = __ldg(&n->a), b = __ldg(&n->b), c = __ldg(&n->c);
-      const int4 d = __ldg(&n->d);
-      float te0, te1;
-      const bool h0 = FMA ? box_hit_fma(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0)
-                          : box_hit(a.x, a.y, a.z, a.w, b.x, b.y, r, best.t, te0);
-      const bool h1 = FMA ? box_hit_fma(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1)
-                          : box_hit(b.z, b.w, c.x, c.y, c.z, c.w, r, best.t, te1);
-      // children are stored as visited: inner index, leaf code, or -1 for an empty slot
-      int c0 = h0 ? d.x : kEmpty;
-      int c1 = h1 ? d.y : kEmpty;
-      if (c0 != kEmpty && c1 != kEmpty && te1 < te0) { const int t = c0; c0 = c1; c1 = t; }
-      if (c0 == kEmpty) { c0 = c1; c1 = kEmpty; }
-      if (c0 != kEmpty) {
-        cur = c0;
-        if (c1 != kEmpty && sp < kStack) stack[sp++] = c1;
-      } else {
-        cur = sp > 0 ? stack[--sp] : kEmpty;
-      }
-      if (cur < kEmpty && leaf == kEmpty) {
-        leaf = cur;
-        cur = sp > 0 ? stack[--sp] : kEmpty;
-      }
-      if (__all_sync(__activemask(), leaf != kEmpty)) break;
-    }
-    while (leaf != kEmpty) {
-      const int code = ~leaf;
-      const int first = code >> 3, count = code & 7;
-      if (COUNT) vc.tris += count;
-      for (int i = first; i < first + count; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
-      leaf = kEmpty;
-      if (cur < kEmpty) {
-        leaf = cur;
-        cur = sp > 0 ? stack[--sp] : kEmpty;
-      }
-    }
-    if (cur == kEmpty) break;
-  }
+  int sp = 0, cur = 0, leaf = kEmptyEntry, visits = 0;
+  do {
+    ww_round<COUNT, FMA>(m, r, isect, best, stack, cur, leaf, sp, visits, vc);
+  } while (cur != kEmptyEntry);
 }
 
 // ---- 8-wide quantised BVH ----

@@ -96,6 +96,133 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
   }
 }
 
+// Binary-BVH trace kernel with lane refill. Each lane holds one ray at a time through a
+// small state machine (idle -> next instance -> traversing -> finished); every loop
+// iteration runs one while-while round for the traversing lanes, and lanes whose rays
+// are finished take new rays at once (one counter fetch per warp for all idle lanes),
+// so a warp no longer waits for its longest ray before taking new work.
+enum { RF_IDLE = 0, RF_INSTANCE = 1, RF_TRAVERSE = 2, RF_FINISH = 3 };
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128, 8) k_trace_refill(WaveBuffers w, RenderKnobs k, int bounce) {
+  const unsigned FULL = 0xffffffffu;
+  const int parity = bounce & 1;
+  const int n = w.counters[parity];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    w.counters[parity ^ 1] = 0;
+    w.counters[44 + (parity ^ 1)] = 0;
+  }
+  int* counts = ev_counts(w, parity);
+  int* fetch = w.counters + 44 + parity;
+  const int lane = threadIdx.x & 31;
+  int stack[kStack];
+  int slot = -1, phase = RF_IDLE, inst = 0, cur = kEmptyEntry, leaf = kEmptyEntry, sp = 0, visits = 0;
+  int job = 0;
+  TraceRay r;
+  MeshBest b{FLT_MAX, -1, 0.0f, 0.0f};
+  HitRecord h;
+  h.t = FLT_MAX; h.u = h.v = 0.0f; h.prim = -1; h.geom = -1;
+  VisitCount vc;
+  bool more = true;   // warp-uniform: rays may remain in the queue
+  for (;;) {
+    if (more) {
+      const unsigned idle = __ballot_sync(FULL, phase == RF_IDLE);
+      if (idle) {
+        const int leader = __ffs(idle) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(fetch, __popc(idle));
+        base = __shfl_sync(FULL, base, leader);
+        if (base + __popc(idle) >= n) more = false;
+        if (phase == RF_IDLE) {
+          const int i = base + __popc(idle & ((1u << lane) - 1));
+          if (i < n) {
+            slot = i;
+            const float4 qo = w.q_orig[parity][i], qd = w.q_dir[parity][i];
+            job = __float_as_int(qd.w) >> kMediumBits;
+            const SceneView& sc = w.jobs[job].sc;
+            const V3 o = v3(qo.x, qo.y, qo.z), d = v3(qd.x, qd.y, qd.z);
+            h.t = FLT_MAX; h.u = h.v = 0.0f; h.prim = -1; h.geom = -1;
+            for (int s = 0; s < sc.num_spheres; ++s) {   // spheres (src/primitives/sphere.cu:43-77)
+              const DevSphere spr = sc.spheres[s];
+              const V3 l = sub(v3(spr.cx, spr.cy, spr.cz), o);
+              const float sd = dot(l, d), ls = dot(l, l), rs = spr.r * spr.r;
+              if (sd < 0.0f && ls > rs) continue;
+              const float ms = ls - sd * sd;
+              if (ms > rs) continue;
+              const float q = sqrtf(rs - ms);
+              const float t = ls > rs ? sd - q : sd + q;
+              if (t < h.t) { h.t = t; h.geom = -2 - s; h.prim = -1; }
+            }
+            inst = 0;
+            phase = RF_INSTANCE;
+          }
+        }
+      }
+    }
+    if (__ballot_sync(FULL, phase != RF_IDLE) == 0) break;
+    if (phase == RF_INSTANCE) {
+      // next instance whose world box the ray enters before its best hit
+      const SceneView& sc = w.jobs[job].sc;
+      const float4 qo = w.q_orig[parity][slot], qd = w.q_dir[parity][slot];
+      const V3 o = v3(qo.x, qo.y, qo.z), d = v3(qd.x, qd.y, qd.z);
+      TraceRay wr;
+      wr.o = o;
+      wr.d = d;
+      wr.idir = v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+      while (inst < sc.num_instances) {
+        const DevInstance& in = sc.instances[inst];
+        float te;
+        if (box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) {
+          setup_ray(r, xform(in.inv, o, 1.0f), xform(in.inv, d, 0.0f), k.isect);
+          b = MeshBest{h.t, -1, 0.0f, 0.0f};
+          cur = 0;
+          leaf = kEmptyEntry;
+          sp = 0;
+          visits = 0;
+          phase = RF_TRAVERSE;
+          break;
+        }
+        ++inst;
+      }
+      if (phase == RF_INSTANCE) phase = RF_FINISH;
+    }
+    if (phase == RF_TRAVERSE) {
+      const SceneView& sc = w.jobs[job].sc;
+      const DevMesh& m = sc.meshes[sc.instances[inst].mesh];
+      ww_round<COUNT, true>(m, r, k.isect, b, stack, cur, leaf, sp, visits, vc);
+      if (cur == kEmptyEntry) {
+        if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = inst; }
+        ++inst;
+        phase = RF_INSTANCE;
+      }
+    }
+    const unsigned fin = __ballot_sync(FULL, phase == RF_FINISH);
+    if (phase == RF_FINISH) {
+      const JobDesc& J = w.jobs[job];
+      const float4 qo = w.q_orig[parity][slot], qd = w.q_dir[parity][slot];
+      const int packed = __float_as_int(qd.w);
+      const int cls = event_class(w, J, J.sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
+      w.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
+      w.hit_geom[slot] = h.geom;
+      const int pos = warp_append_keyed(fin, cls, counts);
+      w.evq[(size_t)cls * w.cap + pos] = slot;
+      phase = RF_IDLE;
+      slot = -1;
+    }
+  }
+  if (COUNT) {
+    unsigned long long my_nodes = vc.nodes, my_tris = vc.tris;
+    for (int off = 16; off > 0; off >>= 1) {
+      my_nodes += __shfl_down_sync(FULL, my_nodes, off);
+      my_tris += __shfl_down_sync(FULL, my_tris, off);
+    }
+    if (lane == 0) {
+      atomicAdd(w.visits, my_nodes);
+      atomicAdd(w.visits + 1, my_tris);
+    }
+  }
+}
+
 // Shadow rays of the next-event estimator: a contribution is added to its path's
 // radiance when nothing lies within the ray's maximum distance.
 template <int KIND>
@@ -297,7 +424,8 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 //   binary BVH: 0 = at most 64 registers (8 blocks of 128 per SM), fused box tests, dynamic
 //   ray fetch, while-while traversal (traverse_bvh2_ww; the default); 1 = compiler's
 //   register choice, grid-stride rays, plain box tests, leaves tested where met; 2 =
-//   variant 1 held to 64 registers; 3 = variant 0 with leaves tested where met;
+//   variant 1 held to 64 registers; 3 = variant 0 with leaves tested where met; 4 =
+//   variant 0 with lane refill (k_trace_refill);
 //   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine.
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (bvh_kind == BVH_WIDE8)
@@ -305,6 +433,7 @@ const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (variant == 1) return (const void*)k_trace<BVH_BINARY, false>;
   if (variant == 2) return (const void*)k_trace<BVH_BINARY, false, 8>;
   if (variant == 3) return (const void*)k_trace<BVH_BINARY, false, 8, true>;
+  if (variant == 4) return (const void*)k_trace_refill<false>;
   return (const void*)k_trace<BVH_BINARY, false, 8, true, true>;
 }
 
@@ -333,6 +462,11 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
   if (k.trace_variant == 3) {
     if (count_visits) k_trace<BVH_BINARY, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
     else k_trace<BVH_BINARY, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    return;
+  }
+  if (k.trace_variant == 4) {
+    if (count_visits) k_trace_refill<true><<<grid, 128, 0, st>>>(w, k, bounce);
+    else k_trace_refill<false><<<grid, 128, 0, st>>>(w, k, bounce);
     return;
   }
   if (count_visits) k_trace<BVH_BINARY, true, 8, true, true><<<grid, 128, 0, st>>>(w, k, bounce);

@@ -47,7 +47,7 @@ def test_same_alone_and_in_the_mix(ctx, scenes):
     jobs = job_list(scenes)
     ref = [alone(ctx, sc, p) for sc, p in jobs]
     for opts in ({}, {"path_capacity": 40000}, {"passes_per_step": 4}, {"trace_variant": 1},
-                 {"trace_variant": 2}, {"trace_variant": 3}):
+                 {"trace_variant": 2}, {"trace_variant": 3}, {"trace_variant": 4}):
         srv = Server(ctx, **opts)
         ids = [srv.submit(sc, p) for sc, p in jobs]
         srv.run()
