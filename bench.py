@@ -54,6 +54,9 @@ def parse():
                     help="binary traversal: 0 64 registers + fused box tests + dynamic ray fetch + while-while "
                          "(default), 1 compiler register choice, 2 variant 1 held to 64 registers, 3 variant 0 with "
                          "leaves tested where met")
+    ap.add_argument("--estimator", default="reference", choices=["reference", "nee"],
+                    help="reference: BSDF sampling only (the reference's estimator); nee: next-event estimation "
+                         "with MIS (shadow rays count as rays)")
     ap.add_argument("--shade-variant", type=int, default=0,
                     help="shade kernel: 0 compiler register choice (default), 1 at most 64 registers")
     ap.add_argument("--tris", type=int, default=100_000)
@@ -233,6 +236,7 @@ def run_ours(args):
     p.intersector = C.ISECT_WATERTIGHT
     p.accum_mode = C.ACCUM_FP32
     p.sample_begin = rank * 1_000_000
+    p.estimator = C.ESTIMATOR_NEE if args.estimator == "nee" else C.ESTIMATOR_REFERENCE
     p.trace_variant = args.trace_variant
     p.shade_variant = args.shade_variant
     r = Renderer(ctx, scene, params=p)
@@ -328,6 +332,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "mode": "plain wavefront", "bvh": args.bvh, "intersector": "watertight",
+                       "estimator": args.estimator, "trace_variant": args.trace_variant,
                        "spp_per_step": args.spp_per_step, "paths_per_step": npix * args.spp_per_step,
                        "triangles": sd.num_triangles(), "resolution": [args.res, args.res], "max_depth": args.depth,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",

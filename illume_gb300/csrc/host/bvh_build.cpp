@@ -4,7 +4,9 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
+#include <thread>
 
 namespace illume {
 
@@ -45,7 +47,97 @@ float up(double d) {
   return f;
 }
 
-// Binned SAH build; returns nodes (root at 0) and fills order.
+struct Work { int node, first, count; };
+
+// One step of the top-down binned SAH build (16 bins per axis on centroids): the node
+// of `w` becomes a leaf, or is split and its two children are pushed.
+void build_step(const Work& w, const std::vector<Box>& boxes, const std::vector<double>& ctr, std::vector<int>& order,
+                int max_leaf, std::vector<BNode>& nodes, std::vector<Work>& stack) {
+  const int kBins = 16;
+  BNode nd;
+  nd.box.reset();
+  Box cb;
+  cb.reset();
+  for (int i = w.first; i < w.first + w.count; ++i) {
+    nd.box.grow(boxes[order[i]]);
+    cb.grow_pt(&ctr[3 * (size_t)order[i]]);
+  }
+  nd.first = w.first;
+  nd.count = w.count;
+  const double parent_area = nd.box.area();
+  const double leaf_cost = (double)w.count;
+  double best_cost = INFINITY;
+  int best_axis = -1, best_bin = -1;
+  if (w.count > 1) {
+    for (int a = 0; a < 3; ++a) {
+      const double ext = cb.hi[a] - cb.lo[a];
+      if (!(ext > 0)) continue;
+      Box bb[kBins];
+      int bc[kBins] = {0};
+      for (int b = 0; b < kBins; ++b) bb[b].reset();
+      const double k = kBins / ext;
+      for (int i = w.first; i < w.first + w.count; ++i) {
+        const int p = order[i];
+        int b = (int)((ctr[3 * (size_t)p + a] - cb.lo[a]) * k);
+        b = std::min(std::max(b, 0), kBins - 1);
+        bb[b].grow(boxes[p]);
+        bc[b]++;
+      }
+      double rarea[kBins];
+      int rcount[kBins];
+      Box acc;
+      acc.reset();
+      int cnt = 0;
+      for (int b = kBins - 1; b > 0; --b) {
+        acc.grow(bb[b]);
+        cnt += bc[b];
+        rarea[b] = acc.area();
+        rcount[b] = cnt;
+      }
+      acc.reset();
+      cnt = 0;
+      for (int b = 0; b < kBins - 1; ++b) {
+        acc.grow(bb[b]);
+        cnt += bc[b];
+        if (cnt == 0 || rcount[b + 1] == 0) continue;
+        const double cost = 1.0 + (acc.area() * cnt + rarea[b + 1] * rcount[b + 1]) / std::max(parent_area, 1e-300);
+        if (cost < best_cost) { best_cost = cost; best_axis = a; best_bin = b; }
+      }
+    }
+  }
+  const bool make_leaf = w.count == 1 || (w.count <= max_leaf && leaf_cost <= best_cost);
+  if (make_leaf) {
+    nodes[w.node] = nd;
+    return;
+  }
+  int mid;
+  if (best_axis < 0) {
+    // all centroids coincide (or no valid split): object median
+    mid = w.first + w.count / 2;
+  } else {
+    const double ext = cb.hi[best_axis] - cb.lo[best_axis];
+    const double k = kBins / ext;
+    auto it = std::partition(order.begin() + w.first, order.begin() + w.first + w.count, [&](int p) {
+      int b = (int)((ctr[3 * (size_t)p + best_axis] - cb.lo[best_axis]) * k);
+      b = std::min(std::max(b, 0), kBins - 1);
+      return b <= best_bin;
+    });
+    mid = (int)(it - order.begin());
+    if (mid == w.first || mid == w.first + w.count) mid = w.first + w.count / 2;
+  }
+  nd.left = (int)nodes.size();
+  nd.right = nd.left + 1;
+  nodes.emplace_back();
+  nodes.emplace_back();
+  nodes[w.node] = nd;
+  stack.push_back({nd.right, mid, w.first + w.count - mid});
+  stack.push_back({nd.left, w.first, mid - w.first});
+}
+
+// Binned SAH build; returns nodes (root at 0) and fills order. The top of the tree is
+// split on one thread until the pending subtrees are small; those are built on the host
+// cores (each into its own node list, on a disjoint range of `order`) and stitched in.
+// The splits do not depend on the scheduling, so the tree is the same on any core count.
 std::vector<BNode> build_binary(const std::vector<Box>& boxes, std::vector<int>& order, int max_leaf) {
   const int N = (int)boxes.size();
   order.resize(N);
@@ -56,90 +148,45 @@ std::vector<BNode> build_binary(const std::vector<Box>& boxes, std::vector<int>&
   std::vector<BNode> nodes;
   nodes.reserve(2 * (size_t)N + 1);
   nodes.emplace_back();
-  struct Work { int node, first, count; };
-  std::vector<Work> stack{{0, 0, N}};
-  const int kBins = 16;
+  const int threads = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+  const int grain = threads > 1 && N > 20000 ? std::max(4096, N / (8 * threads)) : N + 1;
+  std::vector<Work> stack{{0, 0, N}}, deferred;
   while (!stack.empty()) {
     const Work w = stack.back();
     stack.pop_back();
-    BNode nd;
-    nd.box.reset();
-    Box cb;
-    cb.reset();
-    for (int i = w.first; i < w.first + w.count; ++i) {
-      nd.box.grow(boxes[order[i]]);
-      cb.grow_pt(&ctr[3 * (size_t)order[i]]);
-    }
-    nd.first = w.first;
-    nd.count = w.count;
-    const double parent_area = nd.box.area();
-    const double leaf_cost = (double)w.count;
-    double best_cost = INFINITY;
-    int best_axis = -1, best_bin = -1;
-    if (w.count > 1) {
-      for (int a = 0; a < 3; ++a) {
-        const double ext = cb.hi[a] - cb.lo[a];
-        if (!(ext > 0)) continue;
-        Box bb[kBins];
-        int bc[kBins] = {0};
-        for (int b = 0; b < kBins; ++b) bb[b].reset();
-        const double k = kBins / ext;
-        for (int i = w.first; i < w.first + w.count; ++i) {
-          const int p = order[i];
-          int b = (int)((ctr[3 * (size_t)p + a] - cb.lo[a]) * k);
-          b = std::min(std::max(b, 0), kBins - 1);
-          bb[b].grow(boxes[p]);
-          bc[b]++;
-        }
-        double rarea[kBins];
-        int rcount[kBins];
-        Box acc;
-        acc.reset();
-        int cnt = 0;
-        for (int b = kBins - 1; b > 0; --b) {
-          acc.grow(bb[b]);
-          cnt += bc[b];
-          rarea[b] = acc.area();
-          rcount[b] = cnt;
-        }
-        acc.reset();
-        cnt = 0;
-        for (int b = 0; b < kBins - 1; ++b) {
-          acc.grow(bb[b]);
-          cnt += bc[b];
-          if (cnt == 0 || rcount[b + 1] == 0) continue;
-          const double cost = 1.0 + (acc.area() * cnt + rarea[b + 1] * rcount[b + 1]) / std::max(parent_area, 1e-300);
-          if (cost < best_cost) { best_cost = cost; best_axis = a; best_bin = b; }
-        }
+    if (w.count <= grain && w.count > max_leaf) { deferred.push_back(w); continue; }
+    build_step(w, boxes, ctr, order, max_leaf, nodes, stack);
+  }
+  if (deferred.empty()) return nodes;
+  std::vector<std::vector<BNode>> sub(deferred.size());
+  std::atomic<size_t> next{0};
+  auto worker = [&]() {
+    for (size_t k = next++; k < deferred.size(); k = next++) {
+      std::vector<BNode>& sn = sub[k];
+      sn.reserve(2 * (size_t)deferred[k].count + 1);
+      sn.emplace_back();
+      std::vector<Work> st{{0, deferred[k].first, deferred[k].count}};
+      while (!st.empty()) {
+        const Work w = st.back();
+        st.pop_back();
+        build_step(w, boxes, ctr, order, max_leaf, sn, st);
       }
     }
-    const bool make_leaf = w.count == 1 || (w.count <= max_leaf && leaf_cost <= best_cost);
-    if (make_leaf) {
-      nodes[w.node] = nd;
-      continue;
-    }
-    int mid;
-    if (best_axis < 0) {
-      // all centroids coincide (or no valid split): object median
-      mid = w.first + w.count / 2;
-    } else {
-      const double ext = cb.hi[best_axis] - cb.lo[best_axis];
-      const double k = kBins / ext;
-      auto it = std::partition(order.begin() + w.first, order.begin() + w.first + w.count, [&](int p) {
-        int b = (int)((ctr[3 * (size_t)p + best_axis] - cb.lo[best_axis]) * k);
-        b = std::min(std::max(b, 0), kBins - 1);
-        return b <= best_bin;
-      });
-      mid = (int)(it - order.begin());
-      if (mid == w.first || mid == w.first + w.count) mid = w.first + w.count / 2;
-    }
-    nd.left = (int)nodes.size();
-    nd.right = nd.left + 1;
-    nodes.emplace_back();
-    nodes.emplace_back();
-    nodes[w.node] = nd;
-    stack.push_back({nd.right, mid, w.first + w.count - mid});
-    stack.push_back({nd.left, w.first, mid - w.first});
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) pool.emplace_back(worker);
+  worker();
+  for (auto& th : pool) th.join();
+  // stitch: a subtree's root replaces its placeholder, the rest is appended
+  for (size_t k = 0; k < deferred.size(); ++k) {
+    const std::vector<BNode>& sn = sub[k];
+    const int base = (int)nodes.size() - 1;   // sub index j >= 1 -> base + j
+    auto remap = [&](BNode n) {
+      if (n.left >= 0) { n.left += base; n.right += base; }
+      return n;
+    };
+    nodes[deferred[k].node] = remap(sn[0]);
+    for (size_t j = 1; j < sn.size(); ++j) nodes.push_back(remap(sn[j]));
   }
   return nodes;
 }
@@ -200,7 +247,7 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
   }
 
   // ---------------- binary layout ----------------
-  {
+  auto build_binary_layout = [&]() {
     std::vector<int> order;
     std::vector<BNode> bn = T ? build_binary(boxes, order, 4) : std::vector<BNode>();
     out->bvh2.clear();
@@ -267,10 +314,10 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
       out->stats.bvh2_nodes = (int)out->bvh2.size();
       out->stats.bvh2_depth = tree_depth(bn, 0);
     }
-  }
+  };
 
   // ---------------- 8-wide quantised layout ----------------
-  {
+  auto build_wide_layout = [&]() {
     std::vector<int> order;
     std::vector<BNode> bn = T ? build_binary(boxes, order, 3) : std::vector<BNode>();
     out->wide.clear();
@@ -393,7 +440,11 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
       out->stats.wide_nodes = (int)out->wide.size();
       out->stats.wide_depth = max_depth;
     }
-  }
+  };
+  // the two layouts are independent: build them concurrently
+  std::thread wide_thread(build_wide_layout);
+  build_binary_layout();
+  wide_thread.join();
 }
 
 }  // namespace illume
