@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=64)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--bvh", default="binary", choices=["binary", "wide", "wide-persistent"])
+    ap.add_argument("--bvh", default="binary", choices=["binary", "wide4", "wide", "wide-persistent"])
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--trace-variant", type=int, default=0,
                     help="binary traversal: 0 64 registers + fused box tests + dynamic ray fetch + while-while "
@@ -232,7 +232,8 @@ def run_ours(args):
     p = scene.default_params(args.spp_per_step, args.depth)
     p.width = p.height = args.res
     p.samples_per_pass = args.spp_per_step
-    p.bvh_kind = {"binary": C.BVH_BINARY, "wide": C.BVH_WIDE8, "wide-persistent": C.BVH_WIDE8_PERSISTENT}[args.bvh]
+    p.bvh_kind = {"binary": C.BVH_BINARY, "wide": C.BVH_WIDE8, "wide-persistent": C.BVH_WIDE8_PERSISTENT,
+                  "wide4": C.BVH_WIDE4}[args.bvh]
     p.intersector = C.ISECT_WATERTIGHT
     p.accum_mode = C.ACCUM_FP32
     p.sample_begin = rank * 1_000_000

@@ -32,7 +32,7 @@ TEX_CONSTANT, TEX_CHECKERBOARD, TEX_BITMAP = range(3)
 DIST_BECKMANN, DIST_GGX = range(2)
 TONE_LINEAR, TONE_REINHARD, TONE_FILMIC, TONE_UNCHARTED = range(4)
 ISECT_MT, ISECT_WATERTIGHT = range(2)
-BVH_BINARY, BVH_WIDE8, BVH_WIDE8_PERSISTENT = range(3)
+BVH_BINARY, BVH_WIDE8, BVH_WIDE8_PERSISTENT, BVH_WIDE4 = range(4)
 ACCUM_FP32, ACCUM_KAHAN, ACCUM_FP64 = range(3)
 ESTIMATOR_REFERENCE, ESTIMATOR_NEE = range(2)
 SERVER_PATH_CAPACITY, SERVER_PASSES_PER_STEP, SERVER_AUTOTUNE, SERVER_TRACE_VARIANT = range(4)

@@ -21,7 +21,7 @@ enum MaterialType : int {
 enum TextureType : int { TEX_CONSTANT = 0, TEX_CHECKER = 1, TEX_BITMAP = 2 };
 enum Distribution : int { DIST_BECKMANN = 0, DIST_GGX = 1 };
 enum Intersector : int { ISECT_MT = 0, ISECT_WATERTIGHT = 1 };
-enum BvhKind : int { BVH_BINARY = 0, BVH_WIDE8 = 1 };
+enum BvhKind : int { BVH_BINARY = 0, BVH_WIDE8 = 1, BVH_WIDE4 = 2 };
 enum AccumMode : int { ACCUM_FP32 = 0, ACCUM_KAHAN = 1, ACCUM_FP64 = 2 };
 
 // Event classes of one bounce, the keys of the material-sorted shading queues.
@@ -60,7 +60,19 @@ struct WideNode {
 };
 static_assert(sizeof(WideNode) == 80, "wide node must be 80 bytes");
 
+// 4-wide BVH node (128 B, one cache line): the four child boxes as rows of x / y / z
+// bounds, then the four children encoded as the binary node's (inner node index, leaf
+// ~(first << 3 | count) into the binary layout's triangle order, or -1 for an empty slot
+// whose box is empty).
+struct Bvh4Node {
+  float4 lox, loy, loz, hix, hiy, hiz;
+  int4 child;
+  int4 pad;
+};
+static_assert(sizeof(Bvh4Node) == 128, "4-wide node must be 128 bytes");
+
 struct DevMesh {
+  const Bvh4Node* bvh4;         // 4-wide BVH over the binary layout's triangles
   const Bvh2Node* bvh2;         // binary BVH
   const WideNode* wide;         // 8-wide quantised BVH
   const float4* bvh2_tris;      // 3 float4 per triangle in BVH2 leaf order; .w of the first = prim id

@@ -4,6 +4,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cfloat>
 #include <thread>
@@ -314,6 +315,78 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
       out->stats.bvh2_nodes = (int)out->bvh2.size();
       out->stats.bvh2_depth = tree_depth(bn, 0);
     }
+    // ---- 4-wide collapse of the same tree (shares bvh2_tris) ----
+    out->bvh4.clear();
+    auto set_slot = [](Bvh4Node& n, int k, const float lo[3], const float hi[3], int entry) {
+      float* lx = &n.lox.x; float* ly = &n.loy.x; float* lz = &n.loz.x;
+      float* hx = &n.hix.x; float* hy = &n.hiy.x; float* hz = &n.hiz.x;
+      lx[k] = lo[0]; ly[k] = lo[1]; lz[k] = lo[2];
+      hx[k] = hi[0]; hy[k] = hi[1]; hz[k] = hi[2];
+      (&n.child.x)[k] = entry;
+    };
+    auto empty_node = [&]() {
+      Bvh4Node n{};
+      const float lo[3] = {inf, inf, inf}, hi[3] = {-inf, -inf, -inf};
+      for (int k = 0; k < 4; ++k) set_slot(n, k, lo, hi, -1);
+      return n;
+    };
+    auto box_of = [](const Box& b, float lo[3], float hi[3]) {
+      for (int a = 0; a < 3; ++a) { lo[a] = (float)b.lo[a]; hi[a] = (float)b.hi[a]; }
+    };
+    if (T == 0) {
+      out->bvh4.push_back(empty_node());
+      out->stats.bvh4_depth = 1;
+    } else if (bn[0].left < 0) {
+      Bvh4Node n = empty_node();
+      float lo[3], hi[3];
+      box_of(bn[0].box, lo, hi);
+      set_slot(n, 0, lo, hi, ~((bn[0].first << 3) | bn[0].count));
+      out->bvh4.push_back(n);
+      out->stats.bvh4_depth = 1;
+    } else {
+      // children of each 4-wide node: start from the binary node's two children and pull
+      // up the largest-area inner child until there are four (or only leaves)
+      std::vector<std::array<int, 4>> kids;
+      std::vector<int> nkids, depth4, map4(bn.size(), -1);
+      std::vector<std::pair<int, int>> st4{{0, 1}};
+      while (!st4.empty()) {
+        const int i = st4.back().first, dpt = st4.back().second;
+        st4.pop_back();
+        map4[i] = (int)kids.size();
+        std::array<int, 4> ch{bn[i].left, bn[i].right, -1, -1};
+        int nc = 2;
+        while (nc < 4) {
+          int best = -1;
+          double ba = -1.0;
+          for (int k = 0; k < nc; ++k)
+            if (bn[ch[k]].left >= 0 && bn[ch[k]].box.area() > ba) { ba = bn[ch[k]].box.area(); best = k; }
+          if (best < 0) break;
+          const int c = ch[best];
+          ch[best] = bn[c].left;
+          ch[nc++] = bn[c].right;
+        }
+        kids.push_back(ch);
+        nkids.push_back(nc);
+        depth4.push_back(dpt);
+        for (int k = nc - 1; k >= 0; --k)
+          if (bn[ch[k]].left >= 0) st4.push_back({ch[k], dpt + 1});
+      }
+      out->bvh4.resize(kids.size());
+      int maxd = 0;
+      for (size_t q = 0; q < kids.size(); ++q) {
+        Bvh4Node n = empty_node();
+        for (int k = 0; k < nkids[q]; ++k) {
+          const BNode& c = bn[kids[q][k]];
+          float lo[3], hi[3];
+          box_of(c.box, lo, hi);
+          set_slot(n, k, lo, hi, c.left >= 0 ? map4[kids[q][k]] : ~((c.first << 3) | c.count));
+        }
+        out->bvh4[q] = n;
+        maxd = std::max(maxd, depth4[q]);
+      }
+      out->stats.bvh4_depth = maxd;
+    }
+    out->stats.bvh4_nodes = (int)out->bvh4.size();
   };
 
   // ---------------- 8-wide quantised layout ----------------
@@ -521,6 +594,37 @@ bool check_mesh_bvh(const float* P, const int* tris, int T, const MeshBvh& b, st
     }
     for (int p = 0; p < T; ++p)
       if (seen[p] != 1) { *msg = "binary: triangle " + std::to_string(p) + " not referenced exactly once"; return false; }
+  }
+  // ---- 4-wide ----
+  {
+    std::vector<int> seen(T, 0);
+    std::vector<std::pair<int, DBox>> st;
+    DBox all{{-INFINITY, -INFINITY, -INFINITY}, {INFINITY, INFINITY, INFINITY}};
+    st.push_back({0, all});
+    size_t visited = 0;
+    while (!st.empty()) {
+      const int ni = st.back().first;
+      const DBox parent = st.back().second;
+      st.pop_back();
+      if (ni < 0 || ni >= (int)b.bvh4.size() || ++visited > b.bvh4.size()) { *msg = "4-wide: bad node index"; return false; }
+      const Bvh4Node& n = b.bvh4[ni];
+      for (int k = 0; k < 4; ++k) {
+        const int e = (&n.child.x)[k];
+        if (e == -1) continue;
+        const DBox cb{{(&n.lox.x)[k], (&n.loy.x)[k], (&n.loz.x)[k]}, {(&n.hix.x)[k], (&n.hiy.x)[k], (&n.hiz.x)[k]}};
+        if (ni != 0 && !parent.contains(cb)) { *msg = "4-wide: child box outside parent"; return false; }
+        if (e >= 0) { st.push_back({e, cb}); continue; }
+        const int first = ~e >> 3, count = ~e & 7;
+        for (int i = first; i < first + count; ++i) {
+          if (i < 0 || i >= T) { *msg = "4-wide: triangle index out of range"; return false; }
+          const int p = prim_of(b.bvh2_tris[3 * i]);
+          if (p < 0 || p >= T || seen[p]++) { *msg = "4-wide: triangle referenced twice or invalid"; return false; }
+          if (!tri_inside(&b.bvh2_tris[3 * i], cb)) { *msg = "4-wide: triangle outside its leaf box"; return false; }
+        }
+      }
+    }
+    for (int p = 0; p < T; ++p)
+      if (seen[p] != 1) { *msg = "4-wide: triangle " + std::to_string(p) + " not referenced exactly once"; return false; }
   }
   // ---- wide ----
   {

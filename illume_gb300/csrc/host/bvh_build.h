@@ -2,6 +2,9 @@
 //
 // * Binned SAH binary build (16 bins per axis on centroids).
 // * Binary layout (Bvh2Node, 64 B): both child boxes live in the parent node.
+// * 4-wide layout (Bvh4Node, 128 B): the binary tree (leaves of up to 4 triangles)
+//   collapsed by pulling up the largest-area inner child until a node has 4 children;
+//   it shares the binary layout's triangle records.
 // * 8-wide layout (WideNode, 80 B): the binary tree collapsed greedily into nodes of up
 //   to 8 children, child slots ordered by ray octant, child boxes quantised to 8 bits per
 //   axis with outward rounding.
@@ -21,10 +24,12 @@ namespace illume {
 struct BuildStats {
   int bvh2_nodes = 0, bvh2_leaves = 0, bvh2_depth = 0;
   int wide_nodes = 0, wide_leaves = 0, wide_depth = 0;
+  int bvh4_nodes = 0, bvh4_depth = 0;
   double sah_cost = 0.0;
 };
 
 struct MeshBvh {
+  std::vector<Bvh4Node> bvh4;      // 4-wide layout over bvh2_tris
   std::vector<Bvh2Node> bvh2;
   std::vector<float4> bvh2_tris;   // 3 float4 per triangle in leaf order, .w of the first = prim id
   std::vector<WideNode> wide;

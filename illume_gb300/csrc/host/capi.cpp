@@ -160,9 +160,10 @@ int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t repor
       return ILLUME_ERR_INVALID;
     }
     char line[256];
-    snprintf(line, sizeof(line), "mesh %d: %d tris, binary %d nodes depth %d, wide %d nodes %d leaves depth %d\n", i,
-             h.mesh_num_tris[i], b.stats.bvh2_nodes, b.stats.bvh2_depth, b.stats.wide_nodes, b.stats.wide_leaves,
-             b.stats.wide_depth);
+    snprintf(line, sizeof(line),
+             "mesh %d: %d tris, binary %d nodes depth %d, 4-wide %d nodes depth %d, wide %d nodes %d leaves depth %d\n",
+             i, h.mesh_num_tris[i], b.stats.bvh2_nodes, b.stats.bvh2_depth, b.stats.bvh4_nodes, b.stats.bvh4_depth,
+             b.stats.wide_nodes, b.stats.wide_leaves, b.stats.wide_depth);
     rep += line;
   }
   if (report && report_len) {
@@ -323,7 +324,8 @@ int illume_trace_closest_device(illume_context* ctx, illume_scene* scene, const 
                                 int bvh_kind, illume_hit* d_hits) {
   CHECK_ARG(ctx && scene && (n == 0 || (d_rays && d_hits)) && n >= 0, "bad argument");
   CHECK_ARG(intersector == ILLUME_ISECT_MT || intersector == ILLUME_ISECT_WATERTIGHT, "unknown intersector");
-  CHECK_ARG(bvh_kind == ILLUME_BVH_BINARY || bvh_kind == ILLUME_BVH_WIDE8 || bvh_kind == ILLUME_BVH_WIDE8_PERSISTENT,
+  CHECK_ARG(bvh_kind == ILLUME_BVH_BINARY || bvh_kind == ILLUME_BVH_WIDE8 || bvh_kind == ILLUME_BVH_WIDE8_PERSISTENT ||
+                bvh_kind == ILLUME_BVH_WIDE4,
             "unknown BVH kind");
   CHECK_ARG(((uintptr_t)d_rays & 15) == 0, "rays must be 16-byte aligned");
   CHECK_ARG(scene->s.ctx == &ctx->c, "scene was not uploaded with this context");

@@ -35,7 +35,7 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if (p.width <= 0 || p.height <= 0 || p.spp < 0 || p.max_depth < 0) { *err = "invalid render size, spp or depth"; return ILLUME_ERR_INVALID; }
   if ((long long)p.width * p.height > (1LL << 28)) { *err = "image too large"; return ILLUME_ERR_INVALID; }
   if (p.intersector != ISECT_MT && p.intersector != ISECT_WATERTIGHT) { *err = "unknown intersector"; return ILLUME_ERR_INVALID; }
-  if (p.bvh_kind < BVH_BINARY || p.bvh_kind > 2) { *err = "unknown BVH kind"; return ILLUME_ERR_INVALID; }
+  if (p.bvh_kind < 0 || p.bvh_kind > 3) { *err = "unknown BVH kind"; return ILLUME_ERR_INVALID; }
   if (p.bvh_kind == BVH_BINARY && (p.trace_variant < 0 || p.trace_variant > 4)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.accum_mode < ACCUM_FP32 || p.accum_mode > ACCUM_FP64) { *err = "unknown accumulation mode"; return ILLUME_ERR_INVALID; }
   if (p.samples_per_pass < 0) { *err = "negative samples per pass"; return ILLUME_ERR_INVALID; }
@@ -49,7 +49,7 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
 RenderKnobs render_knobs(const illume_render_params& p) {
   RenderKnobs k{};
   k.isect = p.intersector;
-  k.bvh_kind = p.bvh_kind == 2 ? BVH_WIDE8 : p.bvh_kind;
+  k.bvh_kind = p.bvh_kind == 2 ? BVH_WIDE8 : (p.bvh_kind == 3 ? BVH_WIDE4 : p.bvh_kind);
   k.trace_variant = p.bvh_kind == 2 ? 1 : (p.bvh_kind == BVH_BINARY ? p.trace_variant : 0);
   k.shade_variant = p.shade_variant;
   return k;
@@ -197,7 +197,8 @@ int Renderer::profile(bool count_visits, illume_profile* out) {
   out->rays = (int64_t)(rays_after - rays_before);
   out->node_fetches = (int64_t)vis[0];
   out->tri_tests = (int64_t)vis[1];
-  out->node_bytes = eng.knobs.bvh_kind == BVH_WIDE8 ? (int64_t)sizeof(WideNode) : (int64_t)sizeof(Bvh2Node);
+  out->node_bytes = eng.knobs.bvh_kind == BVH_WIDE8 ? (int64_t)sizeof(WideNode)
+                    : eng.knobs.bvh_kind == BVH_WIDE4 ? (int64_t)sizeof(Bvh4Node) : (int64_t)sizeof(Bvh2Node);
   out->tri_bytes = 3 * (int64_t)sizeof(float4);
   for (auto& e : ev) cudaEventDestroy(e);
   samples_done += per_pass;

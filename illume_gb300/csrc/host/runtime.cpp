@@ -309,7 +309,7 @@ long long g_bvh_hits = 0, g_bvh_misses = 0;
 constexpr size_t kBvhCacheMaxBytes = size_t(4) << 30;
 
 size_t bvh_bytes(const MeshBvh& b) {
-  return b.bvh2.size() * sizeof(Bvh2Node) + b.bvh2_tris.size() * sizeof(float4) + b.wide.size() * sizeof(WideNode) +
+  return b.bvh4.size() * sizeof(Bvh4Node) + b.bvh2.size() * sizeof(Bvh2Node) + b.bvh2_tris.size() * sizeof(float4) + b.wide.size() * sizeof(WideNode) +
          b.wide_tris.size() * sizeof(float4);
 }
 
@@ -381,10 +381,15 @@ int Scene::build_host(std::string* err) {
       *err = "binary BVH deeper than the traversal stack (mesh " + std::to_string(i) + ")";
       return ILLUME_ERR_UNSUPPORTED;
     }
+    if (3 * bvhs[i].stats.bvh4_depth > 60) {   // up to 3 entries pushed per 4-wide level
+      *err = "4-wide BVH deeper than the traversal stack (mesh " + std::to_string(i) + ")";
+      return ILLUME_ERR_UNSUPPORTED;
+    }
   }
-  trace_bytes[0] = trace_bytes[1] = 0;
+  trace_bytes[0] = trace_bytes[1] = trace_bytes[2] = 0;
   for (const MeshBvh& b : bvhs) {
     trace_bytes[0] += b.bvh2.size() * sizeof(Bvh2Node) + b.bvh2_tris.size() * sizeof(float4);
+    trace_bytes[2] += b.bvh4.size() * sizeof(Bvh4Node) + b.bvh2_tris.size() * sizeof(float4);
     trace_bytes[1] += b.wide.size() * sizeof(WideNode) + b.wide_tris.size() * sizeof(float4);
   }
   build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -422,6 +427,7 @@ int Scene::build_and_upload(std::string* err) {
     DevMesh& m = meshes[i];
     memset(&m, 0, sizeof(m));
     UP(b.bvh2.data(), b.bvh2.size() * sizeof(Bvh2Node), m.bvh2);
+    UP(b.bvh4.data(), b.bvh4.size() * sizeof(Bvh4Node), m.bvh4);
     UP(b.wide.data(), b.wide.size() * sizeof(WideNode), m.wide);
     UP(b.bvh2_tris.data(), b.bvh2_tris.size() * sizeof(float4), m.bvh2_tris);
     UP(b.wide_tris.data(), b.wide_tris.size() * sizeof(float4), m.wide_tris);

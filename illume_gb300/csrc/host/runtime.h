@@ -104,7 +104,7 @@ struct Scene {
   HostLights lights_host;           // light sampling tables (host copies)
   LightView lights_view{};          // host source of the device light view
   size_t device_bytes = 0;
-  size_t trace_bytes[2] = {0, 0};   // node + triangle bytes a traversal reads: binary, 8-wide
+  size_t trace_bytes[3] = {0, 0, 0};   // node + triangle bytes a traversal reads: binary, 8-wide, 4-wide
   // device tables (kept for re-uploads) and the host source of every device buffer
   std::vector<DevMesh> t_meshes;
   std::vector<DevInstance> t_instances;

@@ -218,7 +218,7 @@ void Server::compose(ServerEngine& se) {
   }
   std::stable_sort(groups.begin(), groups.end(), [](const Group& a, const Group& b) { return a.key < b.key; });
   const size_t l2_target = ctx->l2_bytes > 0 ? (size_t)ctx->l2_bytes * 3 / 4 : ((size_t)96 << 20);
-  const int kind = e.knobs.bvh_kind == BVH_WIDE8 ? 1 : 0;
+  const int kind = e.knobs.bvh_kind == BVH_WIDE8 ? 1 : (e.knobs.bvh_kind == BVH_WIDE4 ? 2 : 0);
   std::vector<char> chosen(e.rows, 0);
   long long paths = 0;
   size_t bytes = 0;

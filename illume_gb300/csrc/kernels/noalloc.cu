@@ -81,7 +81,10 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
     return ILLUME_ERR_UNSUPPORTED;
   }
   if (p.intersector != ILLUME_ISECT_MT && p.intersector != ILLUME_ISECT_WATERTIGHT) { set_error("unknown intersector"); return ILLUME_ERR_INVALID; }
-  if (p.bvh_kind != ILLUME_BVH_BINARY && p.bvh_kind != ILLUME_BVH_WIDE8) { set_error("unknown BVH kind"); return ILLUME_ERR_INVALID; }
+  if (p.bvh_kind != ILLUME_BVH_BINARY && p.bvh_kind != ILLUME_BVH_WIDE8 && p.bvh_kind != ILLUME_BVH_WIDE4) {
+    set_error("unknown BVH kind");
+    return ILLUME_ERR_INVALID;
+  }
   const int dev = ctx->c.device;
   if (dev < 0 || dev >= 256) { set_error("device index out of range"); return ILLUME_ERR_INVALID; }
   ILLUME_CUDA_TRY(cudaSetDevice(dev));
@@ -132,11 +135,11 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
   row.nsamples = p.spp > 0 ? 1 : 0;
   RenderKnobs k{};
   k.isect = p.intersector;
-  k.bvh_kind = p.bvh_kind;
+  k.bvh_kind = p.bvh_kind == ILLUME_BVH_WIDE4 ? BVH_WIDE4 : p.bvh_kind;
   k.trace_variant = 0;
   cudaStream_t st = ctx->c.stream;
   const int sms = ctx->c.sm_count > 0 ? ctx->c.sm_count : 1;
-  const int grid_trace = kernel_grid_blocks(trace_kernel_ptr(p.bvh_kind, 0), 128, dev);
+  const int grid_trace = kernel_grid_blocks(trace_kernel_ptr(k.bvh_kind, 0), 128, dev);
   const int grid_shade = kernel_grid_blocks(shade_kernel_ptr(0), 128, dev);
   const int grid_small = std::max(1, std::min((cap + 255) / 256, sms * 8));
   k_noalloc_begin<<<grid_small, 256, 0, st>>>(w.counters, w.rays, w.visits, w.jobs, row, d_sum, cap);

@@ -269,6 +269,77 @@ __device__ __forceinline__ void traverse_bvh2_ww(const DevMesh& m, const TraceRa
   } while (cur != kEmptyEntry);
 }
 
+// ---- 4-wide BVH ----
+__device__ __forceinline__ void bvh4_slot(float lox, float loy, float loz, float hix, float hiy, float hiz, int child,
+                                          const TraceRay& r, float tbest, float& key, int& entry) {
+  float te;
+  const bool h = box_hit_fma(lox, loy, loz, hix, hiy, hiz, r, tbest, te);
+  key = h ? te : FLT_MAX;
+  entry = h ? child : kEmptyEntry;
+}
+
+__device__ __forceinline__ void sort_pair(float& ka, int& ea, float& kb, int& eb) {
+  const bool s = kb < ka;
+  const float k = s ? kb : ka;
+  kb = s ? ka : kb;
+  ka = k;
+  const int e = s ? eb : ea;
+  eb = s ? ea : eb;
+  ea = e;
+}
+
+// 4-wide BVH in while-while order: per node the four child boxes are tested, the hit
+// children (inner or leaf) ordered by entry distance with a 5-comparator network; the
+// nearest becomes the next entry and the others are pushed farthest first. Leaves are
+// set aside and tested warp-together as in ww_round; triangles are the binary layout's.
+template <bool COUNT>
+__device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
+                                                 int* stack, VisitCount& vc) {
+  constexpr int kEmpty = kEmptyEntry;
+  int sp = 0, cur = 0, leaf = kEmpty, visits = 0;
+  do {
+    while (cur >= 0) {
+      if (COUNT) vc.nodes++;
+      if (++visits > kMaxNodeVisits) { cur = kEmpty; leaf = kEmpty; sp = 0; break; }
+      const Bvh4Node* n = m.bvh4 + cur;
+      const float4 lx = __ldg(&n->lox), ly = __ldg(&n->loy), lz = __ldg(&n->loz);
+      const float4 hx = __ldg(&n->hix), hy = __ldg(&n->hiy), hz = __ldg(&n->hiz);
+      const int4 ch = __ldg(&n->child);
+      float k0, k1, k2, k3;
+      int e0, e1, e2, e3;
+      bvh4_slot(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, ch.x, r, best.t, k0, e0);
+      bvh4_slot(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, ch.y, r, best.t, k1, e1);
+      bvh4_slot(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, ch.z, r, best.t, k2, e2);
+      bvh4_slot(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, ch.w, r, best.t, k3, e3);
+      sort_pair(k0, e0, k1, e1);
+      sort_pair(k2, e2, k3, e3);
+      sort_pair(k0, e0, k2, e2);
+      sort_pair(k1, e1, k3, e3);
+      sort_pair(k1, e1, k2, e2);
+      if (e3 != kEmpty && sp < kStack) stack[sp++] = e3;
+      if (e2 != kEmpty && sp < kStack) stack[sp++] = e2;
+      if (e1 != kEmpty && sp < kStack) stack[sp++] = e1;
+      cur = e0 != kEmpty ? e0 : (sp > 0 ? stack[--sp] : kEmpty);
+      if (cur < kEmpty && leaf == kEmpty) {
+        leaf = cur;
+        cur = sp > 0 ? stack[--sp] : kEmpty;
+      }
+      if (__all_sync(__activemask(), leaf != kEmpty)) break;
+    }
+    while (leaf != kEmpty) {
+      const int code = ~leaf;
+      const int first = code >> 3, count = code & 7;
+      if (COUNT) vc.tris += count;
+      for (int i = first; i < first + count; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
+      leaf = kEmpty;
+      if (cur < kEmpty) {
+        leaf = cur;
+        cur = sp > 0 ? stack[--sp] : kEmpty;
+      }
+    }
+  } while (cur != kEmpty);
+}
+
 // ---- 8-wide quantised BVH ----
 __device__ __forceinline__ float exp2i(uint8_t biased) { return __int_as_float((int)biased << 23); }
 
@@ -484,6 +555,7 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     MeshBest b{h.t, -1, 0.0f, 0.0f};
     const DevMesh& m = sc.meshes[in.mesh];
     if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);
+    else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else if (WW) traverse_bvh2_ww<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else traverse_bvh2<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }

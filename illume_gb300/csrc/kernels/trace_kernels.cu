@@ -428,6 +428,7 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 //   variant 0 with lane refill (k_trace_refill);
 //   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine.
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
+  if (bvh_kind == BVH_WIDE4) return (const void*)k_trace<BVH_WIDE4, false, 8, true>;
   if (bvh_kind == BVH_WIDE8)
     return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
   if (variant == 1) return (const void*)k_trace<BVH_BINARY, false>;
@@ -439,6 +440,11 @@ const void* trace_kernel_ptr(int bvh_kind, int variant) {
 
 void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st,
                   bool count_visits) {
+  if (k.bvh_kind == BVH_WIDE4) {
+    if (count_visits) k_trace<BVH_WIDE4, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    else k_trace<BVH_WIDE4, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    return;
+  }
   if (k.bvh_kind == BVH_WIDE8) {
     if (k.trace_variant == 1) {
       if (count_visits) k_trace_sm<true, false><<<grid, 128, 0, st>>>(w, nullptr, k, bounce, nullptr, 0, nullptr);
@@ -474,11 +480,13 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
 }
 
 const void* shadow_kernel_ptr(int bvh_kind) {
+  if (bvh_kind == BVH_WIDE4) return (const void*)k_shadow<BVH_WIDE4>;
   return bvh_kind == BVH_WIDE8 ? (const void*)k_shadow<BVH_WIDE8> : (const void*)k_shadow<BVH_BINARY>;
 }
 
 void launch_shadow(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st) {
-  if (k.bvh_kind == BVH_WIDE8) k_shadow<BVH_WIDE8><<<grid, 128, 0, st>>>(w, k, bounce);
+  if (k.bvh_kind == BVH_WIDE4) k_shadow<BVH_WIDE4><<<grid, 128, 0, st>>>(w, k, bounce);
+  else if (k.bvh_kind == BVH_WIDE8) k_shadow<BVH_WIDE8><<<grid, 128, 0, st>>>(w, k, bounce);
   else k_shadow<BVH_BINARY><<<grid, 128, 0, st>>>(w, k, bounce);
 }
 
@@ -498,7 +506,9 @@ void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float
     return;
   }
   const int grid = (n + 127) / 128;
-  if (bvh_kind == BVH_WIDE8)
+  if (bvh_kind == 3)   // 4-wide BVH (illume_bvh_kind ILLUME_BVH_WIDE4)
+    k_trace_hook<BVH_WIDE4><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);
+  else if (bvh_kind == BVH_WIDE8)
     k_trace_hook<BVH_WIDE8><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);
   else
     k_trace_hook<BVH_BINARY><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);

@@ -31,7 +31,7 @@ def render(ctx, sd, w, h, spp, depth, **kw):
 
 
 @pytest.mark.parametrize("name", ["box", "materials", "mesh"])
-@pytest.mark.parametrize("bvh", [C.BVH_BINARY, C.BVH_WIDE8, C.BVH_WIDE8_PERSISTENT])
+@pytest.mark.parametrize("bvh", [C.BVH_BINARY, C.BVH_WIDE8, C.BVH_WIDE8_PERSISTENT, C.BVH_WIDE4])
 def test_matches_reference_render(ctx, name, bvh):
     z = golden(f"ref_scene_{name}.npz")
     sd = golden_scene(name)

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 KINDS = [(C.BVH_BINARY, C.ISECT_MT), (C.BVH_BINARY, C.ISECT_WATERTIGHT), (C.BVH_WIDE8, C.ISECT_MT),
          (C.BVH_WIDE8, C.ISECT_WATERTIGHT), (C.BVH_WIDE8_PERSISTENT, C.ISECT_MT),
-         (C.BVH_WIDE8_PERSISTENT, C.ISECT_WATERTIGHT)]
+         (C.BVH_WIDE8_PERSISTENT, C.ISECT_WATERTIGHT), (C.BVH_WIDE4, C.ISECT_MT), (C.BVH_WIDE4, C.ISECT_WATERTIGHT)]
 
 
 def ulp(a, b):
@@ -89,7 +89,7 @@ def test_displaced_icosphere(ctx, bvh, isect):
     compare(sd, ray_set(sd, 30000, seed=2), ctx, bvh, isect)
 
 
-@pytest.mark.parametrize("bvh", [C.BVH_BINARY, C.BVH_WIDE8, C.BVH_WIDE8_PERSISTENT])
+@pytest.mark.parametrize("bvh", [C.BVH_BINARY, C.BVH_WIDE8, C.BVH_WIDE8_PERSISTENT, C.BVH_WIDE4])
 def test_camera_rays_full_size_mesh(ctx, bvh):
     """Primary rays of the 100k-triangle traversal scene (the benchmark's mesh)."""
     from illume_gb300 import synth
