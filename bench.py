@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=64)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--bvh", default="binary", choices=["binary", "wide4", "wide", "wide-persistent"])
+    ap.add_argument("--bvh", default="wide4", choices=["wide4", "binary", "wide", "wide-persistent"])
     ap.add_argument("--spp-per-step", type=int, default=16)
     ap.add_argument("--trace-variant", type=int, default=0,
                     help="binary traversal: 0 64 registers + fused box tests + dynamic ray fetch + while-while "

@@ -2,7 +2,8 @@
 //   illume <save> <scene.json> <spp> <maxdepth>  ->  <save>-<W>x<H>-<spp>spp-<maxdepth>md.png
 // Relative mesh paths in the scene resolve against the current directory, as in the
 // reference. Extra options (after the four positional arguments):
-//   --seed N   --accum fp32|kahan|fp64   --bvh binary|wide   --isect mt|watertight
+//   --seed N   --accum fp32|kahan|fp64   --bvh wide4|binary|wide   --isect mt|watertight
+//   --estimator reference|nee
 //   --pfm      also write the mean radiance as <name>.pfm
 #include <stdio.h>
 #include <stdlib.h>
@@ -26,14 +27,15 @@ int main(int argc, char** argv) {
   const int spp = (int)strtol(argv[3], nullptr, 10);
   const int max_depth = (int)strtol(argv[4], nullptr, 10);
   uint32_t seed = 0;
-  int accum = ILLUME_ACCUM_FP32, bvh = ILLUME_BVH_BINARY, isect = ILLUME_ISECT_WATERTIGHT;
+  int accum = ILLUME_ACCUM_FP32, bvh = ILLUME_BVH_WIDE4, isect = ILLUME_ISECT_WATERTIGHT, estimator = ILLUME_ESTIMATOR_REFERENCE;
   bool pfm = false;
   for (int i = 5; i < argc; ++i) {
     const std::string a = argv[i];
     const char* v = i + 1 < argc ? argv[i + 1] : "";
     if (a == "--seed") { seed = (uint32_t)strtoul(v, nullptr, 10); ++i; }
     else if (a == "--accum") { accum = !strcmp(v, "fp64") ? ILLUME_ACCUM_FP64 : !strcmp(v, "kahan") ? ILLUME_ACCUM_KAHAN : ILLUME_ACCUM_FP32; ++i; }
-    else if (a == "--bvh") { bvh = !strcmp(v, "wide") ? ILLUME_BVH_WIDE8 : ILLUME_BVH_BINARY; ++i; }
+    else if (a == "--bvh") { bvh = !strcmp(v, "wide") ? ILLUME_BVH_WIDE8 : !strcmp(v, "binary") ? ILLUME_BVH_BINARY : ILLUME_BVH_WIDE4; ++i; }
+    else if (a == "--estimator") { estimator = !strcmp(v, "nee") ? ILLUME_ESTIMATOR_NEE : ILLUME_ESTIMATOR_REFERENCE; ++i; }
     else if (a == "--isect") { isect = !strcmp(v, "mt") ? ILLUME_ISECT_MT : ILLUME_ISECT_WATERTIGHT; ++i; }
     else if (a == "--pfm") { pfm = true; }
   }
@@ -47,6 +49,7 @@ int main(int argc, char** argv) {
   p.accum_mode = accum;
   p.bvh_kind = bvh;
   p.intersector = isect;
+  p.estimator = estimator;
   illume_renderer* r = nullptr;
   if (illume_renderer_create(ctx, scene, &p, &r) != ILLUME_OK) return fail("renderer");
   const int W = illume_renderer_get_width(r), H = illume_renderer_get_height(r);

@@ -195,7 +195,7 @@ int illume_render_params_default(const illume_scene* scene, int spp, int max_dep
   out->job = 0;
   out->accum_mode = ILLUME_ACCUM_FP32;
   out->intersector = ILLUME_ISECT_WATERTIGHT;
-  out->bvh_kind = ILLUME_BVH_BINARY;
+  out->bvh_kind = ILLUME_BVH_WIDE4;
   out->exact_hg = 0;
   out->samples_per_pass = 0;
   return ILLUME_OK;

@@ -53,10 +53,11 @@ enum illume_texture_type { ILLUME_TEX_CONSTANT = 0, ILLUME_TEX_CHECKERBOARD = 1,
 enum illume_distribution { ILLUME_DIST_BECKMANN = 0, ILLUME_DIST_GGX = 1 };
 enum illume_tonemapper { ILLUME_TONE_LINEAR = 0, ILLUME_TONE_REINHARD = 1, ILLUME_TONE_FILMIC = 2, ILLUME_TONE_UNCHARTED = 3 }; /* src/tonemapper.h:10-13 */
 enum illume_intersector { ILLUME_ISECT_MT = 0, ILLUME_ISECT_WATERTIGHT = 1 };
-/* BINARY: 64-byte nodes holding both child boxes (the default). WIDE8: 80-byte 8-wide nodes
- * with 8-bit quantised child boxes. WIDE8_PERSISTENT: the same nodes traversed by a
- * persistent kernel that schedules node and triangle steps per warp. WIDE4: 128-byte
- * 4-wide nodes with FP32 child boxes, collapsed from the binary tree. */
+/* WIDE4: 128-byte 4-wide nodes with FP32 child boxes, collapsed from the binary tree (the
+ * default of illume_render_params_default). BINARY: 64-byte nodes holding both child
+ * boxes. WIDE8: 80-byte 8-wide nodes with 8-bit quantised child boxes. WIDE8_PERSISTENT:
+ * the same nodes traversed by a persistent kernel that schedules node and triangle steps
+ * per warp. All four give the same closest hits. */
 enum illume_bvh_kind { ILLUME_BVH_BINARY = 0, ILLUME_BVH_WIDE8 = 1, ILLUME_BVH_WIDE8_PERSISTENT = 2, ILLUME_BVH_WIDE4 = 3 };
 enum illume_accum_mode { ILLUME_ACCUM_FP32 = 0, ILLUME_ACCUM_KAHAN = 1, ILLUME_ACCUM_FP64 = 2 };
 /* REFERENCE: paths find light only by BSDF sampling, as src/renderer.cu:183-386 (the

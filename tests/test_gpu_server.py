@@ -10,9 +10,11 @@ from illume_gb300 import _capi as C
 pytestmark = pytest.mark.gpu
 
 
-def params(scene, w, h, spp, depth, seed=0, job=0, accum=C.ACCUM_FP32):
+def params(scene, w, h, spp, depth, seed=0, job=0, accum=C.ACCUM_FP32, bvh=None):
     p = scene.default_params(spp, depth)
     p.width, p.height, p.seed, p.job, p.accum_mode = w, h, seed, job, accum
+    if bvh is not None:
+        p.bvh_kind = bvh
     return p
 
 
@@ -25,11 +27,12 @@ def scenes(ctx):
     return a, b
 
 
-def job_list(scenes):
+def job_list(scenes, bvh=None):
     a, b = scenes
-    return [(a, params(a, 48, 48, 40, 8, seed=1, job=1)), (b, params(b, 64, 48, 24, 12, seed=2, job=2)),
-            (a, params(a, 32, 24, 64, 6, seed=3, job=3)), (b, params(b, 40, 40, 9, 20, seed=4, job=4, accum=C.ACCUM_KAHAN)),
-            (a, params(a, 24, 16, 100, 8, seed=5, job=5, accum=C.ACCUM_FP64))]
+    return [(a, params(a, 48, 48, 40, 8, seed=1, job=1, bvh=bvh)), (b, params(b, 64, 48, 24, 12, seed=2, job=2, bvh=bvh)),
+            (a, params(a, 32, 24, 64, 6, seed=3, job=3, bvh=bvh)),
+            (b, params(b, 40, 40, 9, 20, seed=4, job=4, accum=C.ACCUM_KAHAN, bvh=bvh)),
+            (a, params(a, 24, 16, 100, 8, seed=5, job=5, accum=C.ACCUM_FP64, bvh=bvh))]
 
 
 def alone(ctx, sc, p):
@@ -42,12 +45,15 @@ def alone(ctx, sc, p):
     return out
 
 
-def test_same_alone_and_in_the_mix(ctx, scenes):
+@pytest.mark.parametrize("bvh", [C.BVH_WIDE4, C.BVH_BINARY])
+def test_same_alone_and_in_the_mix(ctx, scenes, bvh):
+    """Every server setting (slots, passes per step, and for the binary layout each trace
+    kernel variant) gives each job the image it gets alone with the default settings."""
     from illume_gb300.api import Server
-    jobs = job_list(scenes)
+    jobs = job_list(scenes, bvh)
     ref = [alone(ctx, sc, p) for sc, p in jobs]
-    for opts in ({}, {"path_capacity": 40000}, {"passes_per_step": 4}, {"trace_variant": 1},
-                 {"trace_variant": 2}, {"trace_variant": 3}, {"trace_variant": 4}):
+    variants = [{"trace_variant": v} for v in (1, 2, 3, 4)] if bvh == C.BVH_BINARY else []
+    for opts in [{}, {"path_capacity": 40000}, {"passes_per_step": 4}] + variants:
         srv = Server(ctx, **opts)
         ids = [srv.submit(sc, p) for sc, p in jobs]
         srv.run()
