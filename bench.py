@@ -310,9 +310,13 @@ def run_ours(args):
     barrier()
     t0 = time.perf_counter()
     e2e_rays = 0
+    t_up = t_dev = 0.0
     for k in range(e2e_steps):
+        ta = time.perf_counter()
         C.check(C.lib().illume_scene_upload(scene.handle, ctypes.byref(up_bytes)))
+        t_up += time.perf_counter() - ta
         C.check(C.lib().illume_render(r.handle, C.fptr(mean), None, None, C.u8ptr(rgb8), ctypes.byref(st)))
+        t_dev += st.render_ms * 1e-3
         e2e_rays += st.rays
     e2e_s = time.perf_counter() - t0
     e2e_value = e2e_rays / e2e_s / 1e6
@@ -349,7 +353,10 @@ def run_ours(args):
                          "trace_ms_per_pass": round(prof_t.trace_ms, 3), "shade_ms_per_pass": round(prof_t.shade_ms, 3)},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s",
-                    "h2d_bytes_per_step": int(up_bytes.value) + 16, "d2h_bytes_per_step": npix * (12 + 3) + 8},
+                    "h2d_bytes_per_step": int(up_bytes.value) + 16, "d2h_bytes_per_step": npix * (12 + 3) + 8,
+                    "ms_per_step": round(e2e_s / e2e_steps * 1e3, 3),
+                    "upload_ms_per_step": round(t_up / e2e_steps * 1e3, 3),
+                    "device_render_ms_per_step": round(t_dev / e2e_steps * 1e3, 3)},
             "gpu_launches": int(launches),
             "clocks": clk,
         }

@@ -403,12 +403,15 @@ int Scene::build_and_upload(std::string* err) {
   if (bst != ILLUME_OK) return bst;
   auto t1 = std::chrono::steady_clock::now();
 
+  // resident: uploaded once (textures, light tables), like the reference's texture
+  // objects, which HostScene creates once; the rest is what SceneRef copies per render
+  bool resident = false;
   auto up = [&](const void* src, size_t bytes, void** out) -> int {
     buffers.emplace_back(new DevBuffer);
     int st = buffers.back()->upload(ctx, src, bytes);
     if (st != ILLUME_OK) return st;
     *out = buffers.back()->get();
-    uploads.push_back({*out, src, bytes});
+    uploads.push_back({*out, src, bytes, resident});
     device_bytes += buffers.back()->size();
     return ILLUME_OK;
   };
@@ -503,7 +506,9 @@ int Scene::build_and_upload(std::string* err) {
     meds[i].active = h.med_active[i];
   }
   float4* texels = nullptr;
+  resident = true;
   if (!h.texels.empty()) UP(h.texels.data(), h.texels.size() * sizeof(float), texels);
+  resident = false;
   const int nt = h.num_textures();
   std::vector<DevTexture>& texs = t_textures;
   texs.assign(nt, DevTexture{});
@@ -536,6 +541,7 @@ int Scene::build_and_upload(std::string* err) {
   v.env_tex = h.env_tex;
   // light sampling tables of the next-event estimator
   build_lights(h, &lights_host);
+  resident = true;
   {
     const HostLights& L = lights_host;
     LightView lv{};
@@ -557,6 +563,7 @@ int Scene::build_and_upload(std::string* err) {
     lights_view = lv;
     UP(&lights_view, sizeof(LightView), v.lights);
   }
+  resident = false;
 #undef UP
   view = v;
   {
@@ -573,6 +580,7 @@ int Scene::build_and_upload(std::string* err) {
 int Scene::upload_again(size_t* bytes) {
   size_t total = 0;
   for (const Upload& u : uploads) {
+    if (u.resident) continue;
     if (u.bytes && u.src) ILLUME_CUDA_TRY(cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, ctx->stream));
     total += u.bytes;
   }

@@ -112,7 +112,7 @@ struct Scene {
   std::vector<DevMaterial> t_materials;
   std::vector<DevTexture> t_textures;
   std::vector<DevMedium> t_mediums;
-  struct Upload { void* dst; const void* src; size_t bytes; };
+  struct Upload { void* dst; const void* src; size_t bytes; bool resident; };
   std::vector<Upload> uploads;
   int upload_again(size_t* bytes);
   double build_ms = 0.0, upload_ms = 0.0;

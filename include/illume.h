@@ -210,9 +210,12 @@ int illume_scene_create(illume_context* ctx, const illume_scene_desc* desc, illu
 int illume_scene_describe(const illume_scene* scene, illume_scene_desc* out);
 /* Device bytes held by the scene (geometry, BVHs, textures). */
 int illume_scene_device_bytes(const illume_scene* scene, size_t* out);
-/* Copies the scene's host tables to its device buffers again (what the reference's
- * SceneRef does at the start of every render_to_bitmap, src/scene/sceneref.cpp:9-122);
- * synchronous. Returns the bytes copied in *bytes (nullable). */
+/* Copies the scene's geometry to its device buffers again: triangles, vertex attributes,
+ * every BVH layout, and the mesh / instance / sphere / material tables (what the
+ * reference's SceneRef copies at the start of every render_to_bitmap,
+ * src/scene/sceneref.cpp:9-122). Textures and light tables stay resident (the
+ * reference creates its texture objects once, in HostScene). Synchronous. Returns the
+ * bytes copied in *bytes (nullable). */
 int illume_scene_upload(illume_scene* scene, size_t* bytes);
 /* Checks the BVH invariants of every mesh (each triangle referenced exactly once, child
  * boxes inside their parent's, quantised boxes containing the exact boxes) and writes a
