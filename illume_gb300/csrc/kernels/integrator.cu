@@ -100,6 +100,8 @@ __global__ void __launch_bounds__(1024) k_plan(WaveBuffers w) {
     w.counters[45] = 0;
     w.counters[46] = 0;   // shadow-ray counts by bounce parity
     w.counters[47] = 0;
+    w.counters[48] = 0;   // shadow-ray fetch counters by bounce parity
+    w.counters[49] = 0;
     if (over) w.counters[42] = 1;
     for (int c = 0; c < EV_COUNT; ++c) ev_counts2(w, 0)[c] = 0;
   }

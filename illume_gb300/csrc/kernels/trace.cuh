@@ -215,7 +215,8 @@ static constexpr int kEmptyEntry = -1;
 // One while-while round: inner nodes until every lane still in the loop holds a leaf (or
 // this lane has nothing left), then the set-aside leaves. cur / leaf / sp carry the
 // traversal between rounds; visits bounds the node fetches of one ray.
-template <bool COUNT, bool FMA>
+// ANY: stop at the first triangle hit closer than best.t (occlusion queries).
+template <bool COUNT, bool FMA, bool ANY = false>
 __device__ __forceinline__ void ww_round(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best, int* stack,
                                          int& cur, int& leaf, int& sp, int& visits, VisitCount& vc) {
   constexpr int kEmpty = kEmptyEntry;
@@ -252,6 +253,7 @@ __device__ __forceinline__ void ww_round(const DevMesh& m, const TraceRay& r, in
     const int first = code >> 3, count = code & 7;
     if (COUNT) vc.tris += count;
     for (int i = first; i < first + count; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
+    if (ANY && best.prim >= 0) { cur = kEmpty; leaf = kEmpty; sp = 0; break; }
     leaf = kEmpty;
     if (cur < kEmpty) {
       leaf = cur;
@@ -260,12 +262,12 @@ __device__ __forceinline__ void ww_round(const DevMesh& m, const TraceRay& r, in
   }
 }
 
-template <bool COUNT, bool FMA>
+template <bool COUNT, bool FMA, bool ANY = false>
 __device__ __forceinline__ void traverse_bvh2_ww(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
                                                  int* stack, VisitCount& vc) {
   int sp = 0, cur = 0, leaf = kEmptyEntry, visits = 0;
   do {
-    ww_round<COUNT, FMA>(m, r, isect, best, stack, cur, leaf, sp, visits, vc);
+    ww_round<COUNT, FMA, ANY>(m, r, isect, best, stack, cur, leaf, sp, visits, vc);
   } while (cur != kEmptyEntry);
 }
 
@@ -292,7 +294,7 @@ __device__ __forceinline__ void sort_pair(float& ka, int& ea, float& kb, int& eb
 // children (inner or leaf) ordered by entry distance with a 5-comparator network; the
 // nearest becomes the next entry and the others are pushed farthest first. Leaves are
 // set aside and tested warp-together as in ww_round; triangles are the binary layout's.
-template <bool COUNT>
+template <bool COUNT, bool ANY = false>
 __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
                                                  int* stack, VisitCount& vc) {
   constexpr int kEmpty = kEmptyEntry;
@@ -331,6 +333,7 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
       const int first = code >> 3, count = code & 7;
       if (COUNT) vc.tris += count;
       for (int i = first; i < first + count; ++i) test_triangle(m.bvh2_tris + 3 * i, isect, r, best);
+      if (ANY && best.prim >= 0) { cur = kEmpty; leaf = kEmpty; sp = 0; break; }
       leaf = kEmpty;
       if (cur < kEmpty) {
         leaf = cur;
@@ -521,8 +524,9 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 }
 
 // Full closest-hit query for a world-space ray (direction used as given).
-template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false>
-// tmax: only hits closer than tmax count (shadow rays).
+// tmax: only hits closer than tmax count (shadow rays). ANY: return at the first hit
+// found closer than tmax (occlusion; with the binary and 4-wide layouts).
+template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false, bool ANY = false>
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
                                                  VisitCount* vcp = nullptr, float tmax = FLT_MAX) {
   VisitCount vc;
@@ -542,6 +546,7 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     const float t = ls > rs ? sd - q : sd + q;
     if (t < h.t) { h.t = t; h.geom = -2 - s; h.prim = -1; }
   }
+  if (ANY && h.geom != -1) return h;
   // world-space probe for instance boxes
   TraceRay wr;
   wr.o = o; wr.d = d;
@@ -555,10 +560,11 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     MeshBest b{h.t, -1, 0.0f, 0.0f};
     const DevMesh& m = sc.meshes[in.mesh];
     if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);
-    else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
-    else if (WW) traverse_bvh2_ww<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
+    else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT, ANY>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
+    else if (WW) traverse_bvh2_ww<COUNT, FMA, ANY>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else traverse_bvh2<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }
+    if (ANY && h.geom != -1) break;
   }
   if (COUNT && vcp) *vcp = vc;
   return h;

@@ -224,25 +224,34 @@ __global__ void __launch_bounds__(128, 8) k_trace_refill(WaveBuffers w, RenderKn
 }
 
 // Shadow rays of the next-event estimator: a contribution is added to its path's
-// radiance when nothing lies within the ray's maximum distance.
+// radiance when nothing lies within the ray's maximum distance. Occlusion needs no
+// closest hit, so the traversal stops at the first hit (binary and 4-wide layouts);
+// warps take 32 rays at a time from a counter (counters[48 + parity]).
 template <int KIND>
 __global__ void __launch_bounds__(128, 8) k_shadow(WaveBuffers w, RenderKnobs k, int bounce) {
   const int parity = bounce & 1;
   const int n = w.counters[46 + parity];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     w.counters[46 + (parity ^ 1)] = 0;
+    w.counters[48 + (parity ^ 1)] = 0;
     atomicAdd(w.rays, (unsigned long long)n);
   }
+  int* fetch = w.counters + 48 + parity;
+  const int lane = threadIdx.x & 31;
   typename std::conditional<KIND == BVH_WIDE8, uint2, int>::type stack[kStack];
-  for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-    const int i = base + threadIdx.x;
+  for (;;) {
+    int b0 = 0;
+    if (lane == 0) b0 = atomicAdd(fetch, 32);
+    const int base = __shfl_sync(0xffffffffu, b0, 0);
+    if (base >= n) break;
+    const int i = base + lane;
     const bool valid = i < n;
     const unsigned mask = __ballot_sync(0xffffffffu, valid);
     if (!valid) continue;
     const float4 so = w.s_orig[i], sd = w.s_dir[i], sv = w.s_val[i];
     const int job = __float_as_int(so.w);
     const SceneView& sc = w.jobs[job].sc;
-    const HitRecord h = closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY>(
+    const HitRecord h = closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY, KIND != BVH_WIDE8>(
         sc, v3(so.x, so.y, so.z), v3(sd.x, sd.y, sd.z), k.isect, stack, nullptr, sd.w);
     if (h.geom == -1) {
       float4* c = w.contrib + __float_as_int(sv.w);
@@ -250,7 +259,7 @@ __global__ void __launch_bounds__(128, 8) k_shadow(WaveBuffers w, RenderKnobs k,
       *c = make_float4(v.x + sv.x, v.y + sv.y, v.z + sv.z, v.w);
     }
     const unsigned peers = __match_any_sync(mask, job);
-    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&w.jobs[job].rays, (unsigned long long)__popc(peers));
+    if (lane == __ffs(peers) - 1) atomicAdd(&w.jobs[job].rays, (unsigned long long)__popc(peers));
   }
 }
 
