@@ -10,8 +10,9 @@ synthetic data. One step = one wavefront pass of `--spp-per-step` samples of eve
 * value: rays traced (closest-hit queries, counted as the reference counts them) per
   second of device time, inputs resident in HBM, L2 flushed between timed steps.
 * e2e: the same metric through the reference-facing C-ABI with host buffers: every step
-  re-uploads the scene (what the reference's SceneRef does on every render) and reads
-  the mean image and the tonemapped RGB8 image back.
+  re-uploads the scene geometry (what the reference's SceneRef does on every render;
+  the library keeps a page-locked copy of it) and reads the mean image and the
+  tonemapped RGB8 image back into pinned host arrays.
 * roofline: the trace kernel's algorithmic bytes (node fetches x node size + triangle
   tests x triangle record size + ray in / hit out, counted by an instrumented pass)
   over its measured time, against the measured HBM copy bandwidth.
@@ -65,10 +66,11 @@ def parse():
     ap.add_argument("--sss-res", type=int, nargs=2, default=[96, 72],
                     help="sss: image size (the accumulation study needs the per-pixel spp, not the pixels)")
     ap.add_argument("--sss-spp", type=int, default=20000)
-    ap.add_argument("--workload", default="traversal", choices=["traversal", "batched", "served", "sss"],
+    ap.add_argument("--workload", default="traversal", choices=["traversal", "batched", "served", "sss", "cornell"],
                     help="traversal: the headline single-render workload; batched: 64 uneven jobs in one job "
                          "table vs one job at a time; served: Poisson request stream, continuous batching vs "
-                         "one request at a time")
+                         "one request at a time; sss: accumulation precision study; cornell: the small "
+                         "Cornell-box case with the oracle beside it")
     ap.add_argument("--jobs", type=int, default=64)
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--plain-1spp", action="store_true",
@@ -302,8 +304,9 @@ def run_ours(args):
 
     # end to end through the C-ABI with host buffers
     npix = args.res * args.res
-    mean = np.zeros((npix, 3), np.float32)
-    rgb8 = np.zeros((npix, 3), np.uint8)
+    # the step's results land in pinned host memory (page-locked, DMA-able)
+    mean = torch.zeros((npix, 3), dtype=torch.float32, pin_memory=True).numpy()
+    rgb8 = torch.zeros((npix, 3), dtype=torch.uint8, pin_memory=True).numpy()
     e2e_steps = max(1, min(args.steps, 4))
     up_bytes = ctypes.c_size_t()
     st = C.RenderStats()
@@ -655,6 +658,87 @@ def run_sss(args):
     print(json.dumps(out), flush=True)
 
 
+def run_cornell(args):
+    """The small plain-method case: the Cornell box (mirror and glass spheres, 256x256,
+    64 spp, depth 8, FP32 accumulation, seed 0). One step = one full render on the GPU.
+    Beside it, the same render by the oracle (the reference integrator restated) on all
+    host cores in FP32 (timed) and in FP64 (the image the GPU's is compared with: same
+    Philox streams, so the difference is arithmetic, not Monte Carlo noise)."""
+    import torch
+    import numpy as np
+    from illume_gb300 import _capi as C
+    from illume_gb300 import synth
+    from illume_gb300.api import Context, HostScene, Renderer
+    from oracle import pyoracle
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    W = H = 256
+    spp, depth = 64, 8
+    sd = synth.cornell_scene(W, H)
+    ctx = Context(local)
+    scene = HostScene.from_data(ctx, sd)
+    p = scene.default_params(spp, depth)
+    p.width, p.height, p.seed, p.job, p.accum_mode = W, H, 0, 0, C.ACCUM_FP32
+    p.estimator = C.ESTIMATOR_NEE if args.estimator == "nee" else C.ESTIMATOR_REFERENCE
+    r = Renderer(ctx, scene, params=p)
+    for _ in range(args.warmup):
+        r.render_device()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    dev_ms, rays, launches = 0.0, 0, 0
+    for _ in range(args.steps):
+        st = r.render_device()
+        dev_ms += st.render_ms
+        rays += st.rays
+        launches += st.kernel_launches
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    g = r.read(mean=False, sums=True)
+    r.close()
+    gmean = g["sum"] / spp
+    gvar = np.maximum(g["sumsq"] / spp - gmean * gmean, 0)
+    value = rays / (dev_ms * 1e-3) / 1e6
+    osc = pyoracle.OracleScene(sd)
+    t0 = time.perf_counter()
+    o32, _, crays = osc.render(W, H, spp, depth, seed=0, job=0, isect=C.ISECT_WATERTIGHT, precision=32)
+    cpu_s = time.perf_counter() - t0
+    threads = os.cpu_count() or 1
+    osum, osq, _ = osc.render(W, H, spp, depth, seed=0, job=0, isect=C.ISECT_WATERTIGHT, precision=64)
+    om = osum / spp
+    ovar = np.maximum(osq / spp - om * om, 0)
+    rmse = float(np.sqrt(np.mean((gmean - om) ** 2)))
+    rmse32 = float(np.sqrt(np.mean((gmean - o32 / spp) ** 2)))
+    sigma = np.sqrt((gvar + ovar) / spp)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dev_ms / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"Cornell box (5 wall quads, 130x105 light (17,12,4), mirror and glass spheres r=90), "
+                               f"{W}x{H}, {spp} spp, depth {depth}, FP32 accumulation, seed 0",
+                   "estimator": args.estimator, "rays_per_render": rays // args.steps,
+                   "l2": "scene and image fit in L2 (working set < 40 MB); not flushed"},
+        # the reference estimator follows the oracle's Philox streams, so these differences
+        # are arithmetic (FP32 paths that part from the FP64 ones); the next-event estimator
+        # draws other samples, so for it they are Monte Carlo noise
+        "rmse_vs_fp64_oracle": rmse,
+        "rel_rmse_vs_fp64_oracle": rmse / max(float(np.mean(np.abs(om))), 1e-12),
+        "rmse_vs_fp32_oracle": rmse32,
+        "within_3sigma_of_fp64_oracle": float(np.mean(np.abs(gmean - om) <= 3 * sigma + 1e-6)),
+        "variance_per_sample": {"gpu": float(gvar.mean()), "fp64_oracle": float(ovar.mean())},
+        "cpu_baseline": {"value": round(crays / cpu_s / 1e6, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"the full {W}x{H} {spp}-spp render, FP32 oracle, {crays} rays, {cpu_s:.1f} s, "
+                                   f"OpenMP {threads} threads"},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    scene.close()
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -665,6 +749,8 @@ def main():
         run_served(args)
     elif args.workload == "sss":
         run_sss(args)
+    elif args.workload == "cornell":
+        run_cornell(args)
     else:
         run_ours(args)
 

@@ -574,7 +574,29 @@ int Scene::build_and_upload(std::string* err) {
   }
   ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   upload_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+  pin_upload_sources();
   return ILLUME_OK;
+}
+
+void Scene::pin_upload_sources() {
+  size_t total = 0;
+  for (const Upload& u : uploads)
+    if (!u.resident && u.src && u.bytes) total += (u.bytes + 255) & ~(size_t)255;
+  if (total == 0) return;
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, total, cudaHostAllocDefault) != cudaSuccess) {
+    cudaGetLastError();   // keep the pageable sources
+    return;
+  }
+  pinned.p = p;
+  pinned.bytes = total;
+  char* at = static_cast<char*>(p);
+  for (Upload& u : uploads) {
+    if (u.resident || !u.src || !u.bytes) continue;
+    memcpy(at, u.src, u.bytes);
+    u.src = at;
+    at += (u.bytes + 255) & ~(size_t)255;
+  }
 }
 
 int Scene::upload_again(size_t* bytes) {

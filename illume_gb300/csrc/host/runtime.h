@@ -114,6 +114,18 @@ struct Scene {
   std::vector<DevMedium> t_mediums;
   struct Upload { void* dst; const void* src; size_t bytes; bool resident; };
   std::vector<Upload> uploads;
+  // Page-locked copy of the per-render (non-resident) sources, made once after the build
+  // (the host tables never change afterwards), so that re-uploads are DMA copies from
+  // pinned memory; the sources stay pageable if it cannot be allocated.
+  struct PinnedCopy {
+    void* p = nullptr;
+    size_t bytes = 0;
+    PinnedCopy() = default;
+    PinnedCopy(const PinnedCopy&) = delete;
+    PinnedCopy& operator=(const PinnedCopy&) = delete;
+    ~PinnedCopy() { if (p) cudaFreeHost(p); }
+  } pinned;
+  void pin_upload_sources();
   int upload_again(size_t* bytes);
   double build_ms = 0.0, upload_ms = 0.0;
   int build_host(std::string* err);        // BVHs only (host-only scenes)
