@@ -3,6 +3,7 @@
 #include <stddef.h>
 
 #include <algorithm>
+#include <functional>
 
 namespace illume {
 
@@ -11,6 +12,24 @@ Engine::~Engine() { drop_graphs(); }
 void Engine::drop_graphs() {
   for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
   graphs.clear();
+  for (auto& kv : head_graphs) cudaGraphExecDestroy(kv.second);
+  head_graphs.clear();
+  if (acc_graph) cudaGraphExecDestroy(acc_graph);
+  acc_graph = nullptr;
+}
+
+static int capture(cudaStream_t st, cudaGraphExec_t* out, const std::function<void()>& body) {
+  cudaGraph_t g;
+  ILLUME_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  body();
+  ILLUME_CUDA_TRY(cudaStreamEndCapture(st, &g));
+  const cudaError_t e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    return ILLUME_ERR_CUDA;
+  }
+  return ILLUME_OK;
 }
 
 int Engine::ensure_shadow(std::string* err) {
@@ -74,6 +93,7 @@ void Engine::point() {
 
 int Engine::init(Context* c, int nrows, int ncap, const RenderKnobs& k, std::string* err) {
   ctx = c;
+  if (!stream) stream = ctx->stream;
   rows = nrows;
   cap = ncap;
   knobs = k;
@@ -90,10 +110,10 @@ int Engine::init(Context* c, int nrows, int ncap, const RenderKnobs& k, std::str
   ALLOC(pixel_base, sizeof(int) * (size_t)(rows + 1));
 #undef ALLOC
   mirror.assign(rows, JobDesc{});
-  ILLUME_CUDA_TRY(cudaMemsetAsync(counters.get(), 0, counters.size(), ctx->stream));
-  ILLUME_CUDA_TRY(cudaMemsetAsync(rays.get(), 0, rays.size(), ctx->stream));
-  ILLUME_CUDA_TRY(cudaMemsetAsync(visits.get(), 0, visits.size(), ctx->stream));
-  ILLUME_CUDA_TRY(cudaMemsetAsync(jobs.get(), 0, jobs.size(), ctx->stream));
+  ILLUME_CUDA_TRY(cudaMemsetAsync(counters.get(), 0, counters.size(), stream));
+  ILLUME_CUDA_TRY(cudaMemsetAsync(rays.get(), 0, rays.size(), stream));
+  ILLUME_CUDA_TRY(cudaMemsetAsync(visits.get(), 0, visits.size(), stream));
+  ILLUME_CUDA_TRY(cudaMemsetAsync(jobs.get(), 0, jobs.size(), stream));
   point();
   grid_trace = kernel_grid_blocks(trace_kernel_ptr(knobs.bvh_kind, knobs.trace_variant), 128, ctx->device);
   grid_shade = kernel_grid_blocks(shade_kernel_ptr(knobs.shade_variant), 128, ctx->device);
@@ -105,7 +125,7 @@ int Engine::init(Context* c, int nrows, int ncap, const RenderKnobs& k, std::str
 int Engine::resize(int new_cap, std::string* err) {
   if (new_cap == cap) return ILLUME_OK;
   if (new_cap < 1 || new_cap > (1 << 30)) { *err = "path slots out of range"; return ILLUME_ERR_INVALID; }
-  ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  ILLUME_CUDA_TRY(cudaStreamSynchronize(stream));
   drop_graphs();
   const int old = cap;
   cap = new_cap;
@@ -132,7 +152,7 @@ int Engine::set_trace_variant(int variant) {
 
 int Engine::write_row(int r) {
   ILLUME_CUDA_TRY(cudaMemcpyAsync(jobs.as<JobDesc>() + r, &mirror[r], sizeof(JobDesc), cudaMemcpyHostToDevice,
-                                  ctx->stream));
+                                  stream));
   return ILLUME_OK;
 }
 
@@ -141,16 +161,14 @@ int Engine::write_pass_state(int r) {
   static_assert(offsetof(JobDesc, per_pass) == offsetof(JobDesc, sample_base) + 3 * sizeof(int), "pass state words");
   ILLUME_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(jobs.as<JobDesc>() + r) + off,
                                   reinterpret_cast<const char*>(&mirror[r]) + off, 4 * sizeof(int),
-                                  cudaMemcpyHostToDevice, ctx->stream));
+                                  cudaMemcpyHostToDevice, stream));
   return ILLUME_OK;
 }
 
 void Engine::advance_mirror() {
   for (JobDesc& J : mirror) {
     if (J.nsamples <= 0) continue;
-    J.sample_base += J.nsamples;
-    const int left = J.sample_end - J.sample_base;
-    J.nsamples = left < J.per_pass ? std::max(left, 0) : J.per_pass;
+    advance_pass_state(J.sample_base, J.nsamples, J.sample_end, J.per_pass, J.flags);
   }
 }
 
@@ -167,7 +185,7 @@ int Engine::free_rows() const {
   return n;
 }
 
-void Engine::launch_pass(cudaStream_t st, int depth, bool nee) {
+void Engine::launch_head(cudaStream_t st, int depth, bool nee) {
   launch_plan(w, st);
   launch_raygen(w, grid_raygen, st);
   for (int b = 0; b < depth; ++b) {
@@ -175,8 +193,49 @@ void Engine::launch_pass(cudaStream_t st, int depth, bool nee) {
     launch_shade(w, knobs, b, nee ? grid_shade_nee : grid_shade, st, nee);
     if (nee) launch_shadow(w, knobs, b, grid_shadow, st);
   }
+}
+
+void Engine::launch_pass(cudaStream_t st, int depth, bool nee) {
+  launch_head(st, depth, nee);
   launch_accumulate(w, grid_acc, st);
   launch_advance(w, st);
+}
+
+int Engine::run_interleaved(int depth, cudaEvent_t wait_ev, cudaEvent_t record_ev) {
+  if (paths_in_pass() > cap) {
+    set_error("job table needs more path slots than the engine has");
+    return ILLUME_ERR_INVALID;
+  }
+  const bool nee = any_nee();
+  if (nee) {
+    std::string err;
+    const int s = ensure_shadow(&err);
+    if (s != ILLUME_OK) { set_error(err); return s; }
+  }
+  const int key = 2 * depth + (nee ? 1 : 0);
+  auto it = head_graphs.find(key);
+  if (it == head_graphs.end()) {
+    cudaGraphExec_t exec = nullptr;
+    const int s = capture(stream, &exec, [&] { launch_head(stream, depth, nee); });
+    if (s != ILLUME_OK) return s;
+    it = head_graphs.emplace(key, exec).first;
+  }
+  if (!acc_graph) {
+    const int s = capture(stream, &acc_graph, [&] {
+      launch_accumulate(w, grid_acc, stream);
+      launch_advance(w, stream);
+    });
+    if (s != ILLUME_OK) return s;
+  }
+  ILLUME_CUDA_TRY(cudaGraphLaunch(it->second, stream));
+  if (wait_ev) ILLUME_CUDA_TRY(cudaStreamWaitEvent(stream, wait_ev, 0));
+  ILLUME_CUDA_TRY(cudaGraphLaunch(acc_graph, stream));
+  if (record_ev) ILLUME_CUDA_TRY(cudaEventRecord(record_ev, stream));
+  advance_mirror();
+  passes += 1;
+  launches += launches_per_pass(depth, nee);
+  ctx->launches += launches_per_pass(depth, nee);
+  return ILLUME_OK;
 }
 
 int Engine::run(int npasses, int depth) {
@@ -185,7 +244,7 @@ int Engine::run(int npasses, int depth) {
     set_error("job table needs more path slots than the engine has");
     return ILLUME_ERR_INVALID;
   }
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = stream;
   const bool nee = any_nee();
   if (nee) {
     std::string err;
@@ -195,17 +254,9 @@ int Engine::run(int npasses, int depth) {
   const int key = 2 * depth + (nee ? 1 : 0);
   auto it = graphs.find(key);
   if (it == graphs.end()) {
-    cudaGraph_t g;
-    ILLUME_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    launch_pass(st, depth, nee);
-    ILLUME_CUDA_TRY(cudaStreamEndCapture(st, &g));
     cudaGraphExec_t exec = nullptr;
-    const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) {
-      set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-      return ILLUME_ERR_CUDA;
-    }
+    const int s = capture(st, &exec, [&] { launch_pass(st, depth, nee); });
+    if (s != ILLUME_OK) return s;
     it = graphs.emplace(key, exec).first;
   }
   for (int i = 0; i < npasses; ++i) {
@@ -223,7 +274,7 @@ int Engine::run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>&
     set_error("job table needs more path slots than the engine has");
     return ILLUME_ERR_INVALID;
   }
-  cudaStream_t st = ctx->stream;
+  cudaStream_t st = stream;
   const bool nee = any_nee();
   if (nee) {
     std::string err;
@@ -257,8 +308,8 @@ int Engine::run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>&
 
 int Engine::read_row_rays(int r, unsigned long long* out) {
   ILLUME_CUDA_TRY(cudaMemcpyAsync(out, reinterpret_cast<const char*>(jobs.as<JobDesc>() + r) + offsetof(JobDesc, rays),
-                                  sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
-  ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+                                  sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
+  ILLUME_CUDA_TRY(cudaStreamSynchronize(stream));
   return ILLUME_OK;
 }
 

@@ -28,7 +28,10 @@ struct Engine {
   WaveBuffers w{};
   std::vector<JobDesc> mirror;   // the table as the device has it after the launched passes
   int grid_trace = 0, grid_shade = 0, grid_raygen = 0, grid_acc = 0, grid_shadow = 0, grid_shade_nee = 0;
+  cudaStream_t stream = nullptr;            // the engine's stream (the context's unless set before init)
   std::map<int, cudaGraphExec_t> graphs;   // captured pass by (depth, shadow stage)
+  std::map<int, cudaGraphExec_t> head_graphs;   // the same without accumulate and advance
+  cudaGraphExec_t acc_graph = nullptr;          // accumulate + advance
   long long passes = 0, launches = 0;
 
   Engine() = default;
@@ -49,6 +52,11 @@ struct Engine {
   // ev[0] before plan, ev[1] after raygen, ev[2 + 2b] after trace b, ev[3 + 2b] after
   // shade b, ev[2 + 2 depth] after accumulate. count_visits selects the instrumented trace.
   int run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>& ev);
+  // One pass whose accumulation waits for `wait_ev` (when not null) and is followed by a
+  // record of `record_ev`: two engines on two streams alternate passes over one job's
+  // samples, each pass's rendering overlapping the other's, their accumulations in
+  // sample order.
+  int run_interleaved(int depth, cudaEvent_t wait_ev, cudaEvent_t record_ev);
   int read_row_rays(int r, unsigned long long* out);   // synchronous
   int free_rows() const;
   long long paths_in_pass() const;                      // of the next pass, from the mirror
@@ -60,6 +68,7 @@ struct Engine {
   int alloc_paths(std::string* err);
   void point();
   void advance_mirror();
+  void launch_head(cudaStream_t st, int depth, bool nee);
   void launch_pass(cudaStream_t st, int depth, bool nee);
   int ensure_shadow(std::string* err);
   void drop_graphs();

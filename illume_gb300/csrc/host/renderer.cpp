@@ -37,9 +37,10 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if (p.intersector != ISECT_MT && p.intersector != ISECT_WATERTIGHT) { *err = "unknown intersector"; return ILLUME_ERR_INVALID; }
   if (p.bvh_kind < 0 || p.bvh_kind > 3) { *err = "unknown BVH kind"; return ILLUME_ERR_INVALID; }
   if (p.bvh_kind == BVH_BINARY && (p.trace_variant < 0 || p.trace_variant > 4)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
+  if (p.bvh_kind == 3 && (p.trace_variant < 0 || p.trace_variant > 3)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.accum_mode < ACCUM_FP32 || p.accum_mode > ACCUM_FP64) { *err = "unknown accumulation mode"; return ILLUME_ERR_INVALID; }
   if (p.samples_per_pass < 0) { *err = "negative samples per pass"; return ILLUME_ERR_INVALID; }
-  if (p.shade_variant < 0 || p.shade_variant > 1) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
+  if (p.shade_variant < 0 || p.shade_variant > 3) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.estimator < ILLUME_ESTIMATOR_REFERENCE || p.estimator > ILLUME_ESTIMATOR_NEE) { *err = "unknown estimator"; return ILLUME_ERR_INVALID; }
   if ((int)scene.t_mediums.size() > kMaxMediums) { *err = "too many mediums"; return ILLUME_ERR_UNSUPPORTED; }
   if (!scene.ctx || !scene.view_dev) { *err = "scene has not been uploaded to a device"; return ILLUME_ERR_INVALID; }
@@ -50,7 +51,7 @@ RenderKnobs render_knobs(const illume_render_params& p) {
   RenderKnobs k{};
   k.isect = p.intersector;
   k.bvh_kind = p.bvh_kind == 2 ? BVH_WIDE8 : (p.bvh_kind == 3 ? BVH_WIDE4 : p.bvh_kind);
-  k.trace_variant = p.bvh_kind == 2 ? 1 : (p.bvh_kind == BVH_BINARY ? p.trace_variant : 0);
+  k.trace_variant = p.bvh_kind == 2 ? 1 : (p.bvh_kind == BVH_BINARY || p.bvh_kind == 3 ? p.trace_variant : 0);
   k.shade_variant = p.shade_variant;
   return k;
 }
@@ -73,12 +74,16 @@ JobDesc job_row(const Scene& scene, const illume_render_params& p, const Accumul
 }
 
 Renderer::~Renderer() {
+  if (stream2) cudaStreamSynchronize(stream2);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
+  for (cudaEvent_t e : {acc_ev[0], acc_ev[1], join_ev})
+    if (e) cudaEventDestroy(e);
+  if (stream2) cudaStreamDestroy(stream2);
 }
 
 size_t Renderer::device_bytes() const {
-  size_t b = eng.device_bytes();
+  size_t b = eng.device_bytes() + (split ? eng2.device_bytes() : 0);
   const DevBuffer* all[] = {&sum32, &comp32, &sum64, &sumsq, &out_mean, &out_rgb8};
   for (const DevBuffer* d : all) b += d->size();
   return b;
@@ -91,6 +96,9 @@ int Renderer::init(std::string* err) {
   const long long target = 1LL << 22;  // paths in flight per pass
   per_pass = p.samples_per_pass > 0 ? p.samples_per_pass : (int)std::max(1LL, std::min<long long>(std::max(p.spp, 1), target / npix));
   if ((long long)per_pass * npix > (1LL << 30)) { *err = "too many paths per pass"; return ILLUME_ERR_INVALID; }
+  // two engines taking turns when each half still fills the GPU (2M paths)
+  split = per_pass >= 2 && (long long)per_pass * npix >= (1LL << 22);
+  if (split) per_pass = (per_pass + 1) / 2;
 #define ALLOC(buf, bytes) if ((st = (buf).alloc(ctx, (bytes))) != ILLUME_OK) { *err = last_error(); return st; }
   if (p.accum_mode == ACCUM_FP64) { ALLOC(sum64, sizeof(double) * 3 * (size_t)npix); }
   else { ALLOC(sum32, sizeof(float) * 3 * (size_t)npix); }
@@ -102,9 +110,21 @@ int Renderer::init(std::string* err) {
   acc.sum64 = sum64.as<double>();
   acc.sumsq = sumsq.as<double>();
   if ((st = eng.init(ctx, 1, per_pass * npix, render_knobs(p), err)) != ILLUME_OK) return st;
-  eng.mirror[0] = job_row(*scene, p, acc);
+  JobDesc row = job_row(*scene, p, acc);
+  if (split) row.flags |= 2 << kInterleaveShift;
+  eng.mirror[0] = row;
   p.camera = nullptr;   // read once; the caller's array need not outlive this call
   if ((st = eng.write_row(0)) != ILLUME_OK) { *err = last_error(); return st; }
+  if (split) {
+    ILLUME_CUDA_TRY(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+    eng2.stream = stream2;
+    if ((st = eng2.init(ctx, 1, per_pass * npix, render_knobs(p), err)) != ILLUME_OK) return st;
+    eng2.mirror[0] = row;
+    if ((st = eng2.write_row(0)) != ILLUME_OK) { *err = last_error(); return st; }
+    for (cudaEvent_t* e : {&acc_ev[0], &acc_ev[1], &join_ev})
+      ILLUME_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    ILLUME_CUDA_TRY(cudaStreamSynchronize(stream2));
+  }
   ILLUME_CUDA_TRY(cudaEventCreate(&ev0));
   ILLUME_CUDA_TRY(cudaEventCreate(&ev1));
   launch_clear_accumulators(acc, npix, ctx->stream);
@@ -119,6 +139,13 @@ void Renderer::set_range(int first, int count) {
   J.sample_end = first + count;
   J.per_pass = per_pass;
   J.nsamples = std::min(per_pass, count);
+  if (split) {   // the second engine starts one pass later
+    JobDesc& K = eng2.mirror[0];
+    K.sample_base = first + per_pass;
+    K.sample_end = first + count;
+    K.per_pass = per_pass;
+    K.nsamples = std::max(0, std::min(per_pass, count - per_pass));
+  }
 }
 
 int Renderer::render_device(bool accumulate, illume_render_stats* stats) {
@@ -133,23 +160,44 @@ int Renderer::render_device(bool accumulate, illume_render_stats* stats) {
   set_range(next_sample, spp);
   int s;
   if ((s = eng.write_pass_state(0)) != ILLUME_OK) return s;
-  unsigned long long rays_before = 0, rays_after = 0;
-  ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_before, reinterpret_cast<const char*>(eng.w.jobs) + offsetof(JobDesc, rays), 8,
+  if (split && (s = eng2.write_pass_state(0)) != ILLUME_OK) return s;
+  unsigned long long rays_before[2] = {0, 0}, rays_after[2] = {0, 0};
+  const size_t rays_off = offsetof(JobDesc, rays);
+  ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_before[0], reinterpret_cast<const char*>(eng.w.jobs) + rays_off, 8,
                                   cudaMemcpyDeviceToHost, st));
+  if (split)
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_before[1], reinterpret_cast<const char*>(eng2.w.jobs) + rays_off, 8,
+                                    cudaMemcpyDeviceToHost, stream2));
   const int npasses = spp > 0 ? (spp + per_pass - 1) / per_pass : 0;
   ILLUME_CUDA_TRY(cudaEventRecord(ev0, st));
-  if ((s = eng.run(npasses, p.max_depth)) != ILLUME_OK) return s;
+  if (split) {
+    // passes alternate between the engines; each accumulation waits for the previous one
+    ILLUME_CUDA_TRY(cudaStreamWaitEvent(stream2, ev0, 0));
+    for (int i = 0; i < npasses; ++i) {
+      Engine& e = (i & 1) ? eng2 : eng;
+      if ((s = e.run_interleaved(p.max_depth, i > 0 ? acc_ev[(i - 1) & 1] : nullptr, acc_ev[i & 1])) != ILLUME_OK)
+        return s;
+    }
+    ILLUME_CUDA_TRY(cudaEventRecord(join_ev, stream2));
+    ILLUME_CUDA_TRY(cudaStreamWaitEvent(st, join_ev, 0));
+  } else {
+    if ((s = eng.run(npasses, p.max_depth)) != ILLUME_OK) return s;
+  }
   ILLUME_CUDA_TRY(cudaEventRecord(ev1, st));
-  ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_after, reinterpret_cast<const char*>(eng.w.jobs) + offsetof(JobDesc, rays), 8,
+  ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_after[0], reinterpret_cast<const char*>(eng.w.jobs) + rays_off, 8,
                                   cudaMemcpyDeviceToHost, st));
+  if (split)
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_after[1], reinterpret_cast<const char*>(eng2.w.jobs) + rays_off, 8,
+                                    cudaMemcpyDeviceToHost, st));
   ILLUME_CUDA_TRY(cudaStreamSynchronize(st));
+  if (split) ILLUME_CUDA_TRY(cudaStreamSynchronize(stream2));
   ILLUME_CUDA_TRY(cudaGetLastError());
   samples_done += spp;
   next_sample += spp;
   if (stats) {
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, ev0, ev1);
-    stats->rays = (int64_t)(rays_after - rays_before);
+    stats->rays = (int64_t)(rays_after[0] - rays_before[0] + rays_after[1] - rays_before[1]);
     stats->paths = (int64_t)spp * npix;
     stats->render_ms = ms;
     stats->kernel_launches = (int64_t)npasses * Engine::launches_per_pass(p.max_depth, p.estimator == ILLUME_ESTIMATOR_NEE);

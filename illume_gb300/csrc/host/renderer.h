@@ -5,6 +5,12 @@
 // (trace, shade), accumulate, advance. The pass is captured once into a CUDA graph and
 // replayed; the sample range lives in the device's job row, so the host issues one
 // graph launch per pass and never waits inside the loop.
+//
+// Large renders split the path slots over two engines on two streams that take turns on
+// the sample ranges: while one pass is in its last bounces (few, long rays that leave
+// most of the GPU idle), the next pass's first bounces fill the GPU. Accumulations stay
+// in sample order (each waits for the previous pass's), so the image is the same as with
+// one engine.
 #pragma once
 
 #include <memory>
@@ -19,6 +25,10 @@ struct Renderer {
   illume_render_params p{};
   int npix = 0, per_pass = 1;
   Engine eng;
+  Engine eng2;                  // second engine of a split render (samples per_pass..2 per_pass-1, ...)
+  bool split = false;
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t acc_ev[2] = {nullptr, nullptr}, join_ev = nullptr;
   DevBuffer sum32, comp32, sum64, sumsq, out_mean, out_rgb8;
   Accumulators acc{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

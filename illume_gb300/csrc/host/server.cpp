@@ -328,7 +328,8 @@ int Server::apply_candidate(ServerEngine& se, int idx) {
 void Server::tune(ServerEngine& se, double rays, double ms) {
   static constexpr int kWindow = 3;
   if (se.tune_state == 0) {
-    // binary BVH: the default kernel and its while-while form; 8-wide: both kernels
+    // binary BVH: the default kernel and its while-while form; 8-wide: both kernels;
+    // 4-wide: the traversal stack in local memory or partly in shared memory
     const std::vector<int> variants = se.eng->knobs.bvh_kind == BVH_BINARY ? std::vector<int>{0, 3}
                                                                            : std::vector<int>{0, 1};
     for (int cap : {1 << 23, 1 << 24}) {

@@ -167,10 +167,19 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) 
   const int parity = bounce & 1;
   const int* counts = ev_counts2(w, parity);
   __shared__ int prefix[EV_COUNT + 1];
+  // block-level aggregation of the counters every warp would otherwise hit with its own
+  // atomic (one address each, so those atomics serialise in L2): the rays of the block's
+  // first job, and the block's share of the next-bounce and shadow queues per iteration
+  __shared__ int s_job;
+  __shared__ unsigned long long s_rays;
+  __shared__ int s_warp_cnt[2][4], s_warp_base[2][4], s_base[2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     int acc = 0;
     for (int c = 0; c < EV_COUNT; ++c) { prefix[c] = acc; acc += counts[c]; }
     prefix[EV_COUNT] = acc;
+    s_job = -1;
+    s_rays = 0;
   }
   __syncthreads();
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -344,41 +353,51 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) 
         nt = make_float4(thr.x, thr.y, thr.z, nee ? bsdf_sampled_pdf(mat, s, d, N) : 0.0f);
       }
     done:;
-      // closest-hit queries of this bounce, per job
+      // closest-hit queries of this bounce, per job: the block's first job in shared
+      // memory, any other job with a global atomic
       const unsigned peers = __match_any_sync(live, myjob);
-      if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&w.jobs[myjob].rays, (unsigned long long)__popc(peers));
-    }
-    // compacted append of the shadow rays of this bounce
-    const unsigned sballot = NEE ? __ballot_sync(0xffffffffu, shadow) : 0u;
-    if (NEE && sballot) {
-      const int lane = threadIdx.x & 31;
-      const int leader = __ffs(sballot) - 1;
-      int slot = 0;
-      if (lane == leader) slot = atomicAdd(w.counters + 46 + parity, __popc(sballot));
-      slot = __shfl_sync(0xffffffffu, slot, leader);
-      if (shadow) {
-        const int j = slot + __popc(sballot & ((1u << lane) - 1));
-        w.s_orig[j] = so;
-        w.s_dir[j] = sd;
-        w.s_val[j] = sv;
+      if (lane == __ffs(peers) - 1) {
+        int bj = *(volatile int*)&s_job;
+        if (bj < 0) {
+          atomicCAS(&s_job, -1, myjob);
+          bj = *(volatile int*)&s_job;
+        }
+        if (bj == myjob) atomicAdd(&s_rays, (unsigned long long)__popc(peers));
+        else atomicAdd(&w.jobs[myjob].rays, (unsigned long long)__popc(peers));
       }
     }
-    // compacted append of the continuing paths into the next bounce's queue
+    // compacted appends of the shadow rays and of the continuing paths: one atomic per
+    // block and queue (the loop's trip count is uniform over the block)
     const unsigned ballot = __ballot_sync(0xffffffffu, cont);
-    if (ballot) {
-      const int lane = threadIdx.x & 31;
-      const int leader = __ffs(ballot) - 1;
-      int slot = 0;
-      if (lane == leader) slot = atomicAdd(next_count, __popc(ballot));
-      slot = __shfl_sync(0xffffffffu, slot, leader);
-      if (cont) {
-        const int j = slot + __popc(ballot & ((1u << lane) - 1));
-        w.q_orig[parity ^ 1][j] = no;
-        w.q_dir[parity ^ 1][j] = nd;
-        w.q_thr[parity ^ 1][j] = nt;
-      }
+    const unsigned sballot = NEE ? __ballot_sync(0xffffffffu, shadow) : 0u;
+    if (lane == 0) {
+      s_warp_cnt[0][warp] = __popc(ballot);
+      if (NEE) s_warp_cnt[1][warp] = __popc(sballot);
+    }
+    __syncthreads();
+    if (threadIdx.x < (NEE ? 2 : 1)) {
+      const int q = threadIdx.x;
+      int acc = 0;
+      for (int v = 0; v < 4; ++v) { s_warp_base[q][v] = acc; acc += s_warp_cnt[q][v]; }
+      s_base[q] = acc ? atomicAdd(q == 0 ? next_count : w.counters + 46 + parity, acc) : 0;
+    }
+    __syncthreads();
+    const unsigned below = (1u << lane) - 1;
+    if (NEE && shadow) {
+      const int j = s_base[1] + s_warp_base[1][warp] + __popc(sballot & below);
+      w.s_orig[j] = so;
+      w.s_dir[j] = sd;
+      w.s_val[j] = sv;
+    }
+    if (cont) {
+      const int j = s_base[0] + s_warp_base[0][warp] + __popc(ballot & below);
+      w.q_orig[parity ^ 1][j] = no;
+      w.q_dir[parity ^ 1][j] = nd;
+      w.q_thr[parity ^ 1][j] = nt;
     }
   }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_job >= 0 && s_rays) atomicAdd(&w.jobs[s_job].rays, s_rays);
 }
 
 // Adds the pass's per-path radiance into each job's per-pixel accumulators, sample by
@@ -432,9 +451,7 @@ __global__ void k_advance(JobDesc* jobs, int njobs) {
   if (j >= njobs) return;
   JobDesc& J = jobs[j];
   if (J.nsamples <= 0) return;
-  J.sample_base += J.nsamples;
-  const int left = J.sample_end - J.sample_base;
-  J.nsamples = left < J.per_pass ? (left > 0 ? left : 0) : J.per_pass;
+  advance_pass_state(J.sample_base, J.nsamples, J.sample_end, J.per_pass, J.flags);
 }
 
 // Tonemap of mean radiance: src/renderer.cu:426-441 and src/tonemapper.cu:32-76.
@@ -538,13 +555,20 @@ __global__ void k_bsdf_batch(int type, int dist, const float* in, int n, float* 
   }
 }
 
-// Shade kernel variants (RenderKnobs::shade_variant): 0 = compiler's register choice (72,
-// the default), 1 = at most 64 registers (8 blocks of 128 per SM: more loads in flight,
-// but the spills it needs cost more; measured slower on the traversal workload).
-const void* shade_kernel_ptr(int variant, bool nee) {
-  if (nee) return variant == 1 ? (const void*)k_shade<8, true> : (const void*)k_shade<1, true>;
-  return variant == 1 ? (const void*)k_shade<8, false> : (const void*)k_shade<1, false>;
+// Shade kernel variants (RenderKnobs::shade_variant), by the blocks of 128 that must fit
+// an SM: 0 = compiler's register choice (the default), 1 = 8 blocks (at most 64
+// registers: more loads in flight, but the spills it needs cost more; measured slower on
+// the traversal workload), 2 = 6 blocks (at most 80 registers), 3 = 7 blocks (72).
+template <bool NEE>
+static const void* shade_ptr(int variant) {
+  switch (variant) {
+    case 1: return (const void*)k_shade<8, NEE>;
+    case 2: return (const void*)k_shade<6, NEE>;
+    case 3: return (const void*)k_shade<7, NEE>;
+    default: return (const void*)k_shade<1, NEE>;
+  }
 }
+const void* shade_kernel_ptr(int variant, bool nee) { return nee ? shade_ptr<true>(variant) : shade_ptr<false>(variant); }
 
 void launch_plan(const WaveBuffers& w, cudaStream_t st) {
   const int threads = w.njobs >= 1024 ? 1024 : ((w.njobs + 31) / 32) * 32;
@@ -552,13 +576,9 @@ void launch_plan(const WaveBuffers& w, cudaStream_t st) {
 }
 void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st) { k_raygen<<<grid, 256, 0, st>>>(w); }
 void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st, bool nee) {
-  if (nee) {
-    if (k.shade_variant == 1) k_shade<8, true><<<grid, 128, 0, st>>>(w, bounce);
-    else k_shade<1, true><<<grid, 128, 0, st>>>(w, bounce);
-  } else {
-    if (k.shade_variant == 1) k_shade<8, false><<<grid, 128, 0, st>>>(w, bounce);
-    else k_shade<1, false><<<grid, 128, 0, st>>>(w, bounce);
-  }
+  const void* fn = shade_kernel_ptr(k.shade_variant, nee);
+  void* args[] = {const_cast<WaveBuffers*>(&w), &bounce};
+  cudaLaunchKernel(fn, dim3(grid), dim3(128), args, 0, st);
 }
 void launch_accumulate(const WaveBuffers& w, int grid, cudaStream_t st) { k_accumulate<<<grid, 256, 0, st>>>(w); }
 void launch_advance(const WaveBuffers& w, cudaStream_t st) {

@@ -28,7 +28,7 @@ struct JobDesc {
   uint32_t seed, job;        // Philox key
   int max_depth;             // closest-hit queries per path
   float ray_bias;
-  int flags, accum_mode;      // flags: JOB_EXACT_HG, JOB_NEE
+  int flags, accum_mode;      // flags: JOB_EXACT_HG, JOB_NEE, interleave (job_interleave)
   int npix, width;
   // pass state: samples [sample_base, sample_base + nsamples) of every pixel are in the
   // current pass; advanced by k_advance after every pass; nsamples == 0 = idle row
@@ -39,6 +39,22 @@ struct JobDesc {
 };
 static_assert(sizeof(JobDesc) == 256, "JobDesc layout");
 enum JobFlags : int { JOB_EXACT_HG = 1, JOB_NEE = 2 };
+// Bits 8..15 of the flags: how many job tables take turns on this job's sample ranges
+// (0 or 1: this table alone). With n tables, a pass of one table is followed by one pass
+// of each other table before its next range, so the row skips the others' samples.
+static constexpr int kInterleaveShift = 8;
+__host__ __device__ __forceinline__ int job_interleave(int flags) {
+  const int n = (flags >> kInterleaveShift) & 0xff;
+  return n > 1 ? n : 1;
+}
+// Pass state after a pass of `nsamples` (the same arithmetic on the host mirror and in
+// k_advance).
+__host__ __device__ __forceinline__ void advance_pass_state(int& sample_base, int& nsamples, int sample_end,
+                                                            int per_pass, int flags) {
+  sample_base += nsamples + (job_interleave(flags) - 1) * per_pass;
+  const int left = sample_end - sample_base;
+  nsamples = left < per_pass ? (left > 0 ? left : 0) : per_pass;
+}
 
 // A queued ray's fourth direction word packs its job row and medium:
 // (job << kMediumBits) | (medium + 1), medium -1 = air.

@@ -19,6 +19,7 @@ namespace illume {
 
 static constexpr float kExitSlack = 1.000001f;  // ~8 ulp widening of box exit distances
 static constexpr int kStack = 64;
+static constexpr int kTraceBlock = 128;   // threads per block of the trace kernels
 // Upper bound on node fetches of one ray in one mesh: a well-formed tree never comes
 // close (each node is fetched at most once per ray); it only bounds the loop.
 static constexpr int kMaxNodeVisits = 1 << 22;
@@ -280,6 +281,13 @@ __device__ __forceinline__ void bvh4_slot(float lox, float loy, float loz, float
   entry = h ? child : kEmptyEntry;
 }
 
+// Two consecutive float4 of read-only global memory in one 256-bit load (p 32-byte aligned).
+__device__ __forceinline__ void ldg_v8(const float4* p, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+
 __device__ __forceinline__ void sort_pair(float& ka, int& ea, float& kb, int& eb) {
   const bool s = kb < ka;
   const float k = s ? kb : ka;
@@ -294,18 +302,40 @@ __device__ __forceinline__ void sort_pair(float& ka, int& ea, float& kb, int& eb
 // children (inner or leaf) ordered by entry distance with a 5-comparator network; the
 // nearest becomes the next entry and the others are pushed farthest first. Leaves are
 // set aside and tested warp-together as in ww_round; triangles are the binary layout's.
-template <bool COUNT, bool ANY = false>
+// SH > 0: the first SH stack entries live in shared memory (sh points at this thread's
+// column of a [SH][kTraceBlock] array: one bank per lane, no conflicts, never evicted by
+// node fetches), deeper entries in the local array.
+// V8: the node's six box vectors arrive in three 256-bit loads instead of six 128-bit ones.
+template <bool COUNT, bool ANY = false, int SH = 0, bool V8 = false>
 __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
-                                                 int* stack, VisitCount& vc) {
+                                                 int* stack, VisitCount& vc, int* sh = nullptr) {
   constexpr int kEmpty = kEmptyEntry;
   int sp = 0, cur = 0, leaf = kEmpty, visits = 0;
+  auto push = [&](int v) {
+    if (sp < kStack) {
+      if (SH > 0 && sp < SH) sh[sp * kTraceBlock] = v;
+      else stack[sp - SH] = v;
+      ++sp;
+    }
+  };
+  auto pop = [&]() -> int {
+    --sp;
+    return (SH > 0 && sp < SH) ? sh[sp * kTraceBlock] : stack[sp - SH];
+  };
   do {
     while (cur >= 0) {
       if (COUNT) vc.nodes++;
       if (++visits > kMaxNodeVisits) { cur = kEmpty; leaf = kEmpty; sp = 0; break; }
       const Bvh4Node* n = m.bvh4 + cur;
-      const float4 lx = __ldg(&n->lox), ly = __ldg(&n->loy), lz = __ldg(&n->loz);
-      const float4 hx = __ldg(&n->hix), hy = __ldg(&n->hiy), hz = __ldg(&n->hiz);
+      float4 lx, ly, lz, hx, hy, hz;
+      if (V8) {
+        ldg_v8(&n->lox, lx, ly);
+        ldg_v8(&n->loz, lz, hx);
+        ldg_v8(&n->hiy, hy, hz);
+      } else {
+        lx = __ldg(&n->lox); ly = __ldg(&n->loy); lz = __ldg(&n->loz);
+        hx = __ldg(&n->hix); hy = __ldg(&n->hiy); hz = __ldg(&n->hiz);
+      }
       const int4 ch = __ldg(&n->child);
       float k0, k1, k2, k3;
       int e0, e1, e2, e3;
@@ -318,13 +348,13 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
       sort_pair(k0, e0, k2, e2);
       sort_pair(k1, e1, k3, e3);
       sort_pair(k1, e1, k2, e2);
-      if (e3 != kEmpty && sp < kStack) stack[sp++] = e3;
-      if (e2 != kEmpty && sp < kStack) stack[sp++] = e2;
-      if (e1 != kEmpty && sp < kStack) stack[sp++] = e1;
-      cur = e0 != kEmpty ? e0 : (sp > 0 ? stack[--sp] : kEmpty);
+      if (e3 != kEmpty) push(e3);
+      if (e2 != kEmpty) push(e2);
+      if (e1 != kEmpty) push(e1);
+      cur = e0 != kEmpty ? e0 : (sp > 0 ? pop() : kEmpty);
       if (cur < kEmpty && leaf == kEmpty) {
         leaf = cur;
-        cur = sp > 0 ? stack[--sp] : kEmpty;
+        cur = sp > 0 ? pop() : kEmpty;
       }
       if (__all_sync(__activemask(), leaf != kEmpty)) break;
     }
@@ -337,7 +367,7 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
       leaf = kEmpty;
       if (cur < kEmpty) {
         leaf = cur;
-        cur = sp > 0 ? stack[--sp] : kEmpty;
+        cur = sp > 0 ? pop() : kEmpty;
       }
     }
   } while (cur != kEmpty);
@@ -526,9 +556,12 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 // Full closest-hit query for a world-space ray (direction used as given).
 // tmax: only hits closer than tmax count (shadow rays). ANY: return at the first hit
 // found closer than tmax (occlusion; with the binary and 4-wide layouts).
-template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false, bool ANY = false>
+// SH: shared-memory stack entries of the 4-wide traversal (sh_stack: this thread's column).
+template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false, bool ANY = false, int SH = 0,
+          bool V8 = false>
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
-                                                 VisitCount* vcp = nullptr, float tmax = FLT_MAX) {
+                                                 VisitCount* vcp = nullptr, float tmax = FLT_MAX,
+                                                 int* sh_stack = nullptr) {
   VisitCount vc;
   HitRecord h;
   h.t = tmax; h.u = 0.0f; h.v = 0.0f; h.prim = -1; h.geom = -1;
@@ -560,7 +593,7 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     MeshBest b{h.t, -1, 0.0f, 0.0f};
     const DevMesh& m = sc.meshes[in.mesh];
     if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);
-    else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT, ANY>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
+    else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT, ANY, SH, V8>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc, sh_stack);
     else if (WW) traverse_bvh2_ww<COUNT, FMA, ANY>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else traverse_bvh2<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }

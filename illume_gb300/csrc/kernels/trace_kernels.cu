@@ -43,8 +43,10 @@ __device__ __forceinline__ int event_class(const WaveBuffers& w, const JobDesc& 
 // OPT: box tests in fused multiply-add form, and warps take their next 32 rays from a
 // shared counter (counters[44 + parity]) instead of a fixed grid stride, so that warps
 // whose rays finish early take over the remaining work.
-template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false>
-__global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
+// SH (4-wide only): stack entries kept in shared memory.
+template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false, int SH = 0, bool V8 = false>
+__global__ void __launch_bounds__(kTraceBlock, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
+  __shared__ int sh_stack[SH > 0 ? SH * kTraceBlock : 1];
   const int parity = bounce & 1;
   const int n = w.counters[parity];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -76,7 +78,8 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
     const SceneView& sc = J.sc;
     VisitCount vc;
     const HitRecord h =
-        closest_hit<KIND, COUNT, OPT, WW>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack, &vc);
+        closest_hit<KIND, COUNT, OPT, WW, false, SH, V8>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack,
+                                                     &vc, FLT_MAX, sh_stack + threadIdx.x);
     if (COUNT) { my_nodes += vc.nodes; my_tris += vc.tris; }
     const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
     w.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
@@ -435,9 +438,17 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 //   register choice, grid-stride rays, plain box tests, leaves tested where met; 2 =
 //   variant 1 held to 64 registers; 3 = variant 0 with leaves tested where met; 4 =
 //   variant 0 with lane refill (k_trace_refill);
-//   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine.
+//   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine;
+//   4-wide BVH: 0 = at most 64 registers (8 blocks of 128 per SM), traversal stack in
+//   local memory (the default); 1 = its first 8 entries in shared memory; 2 = node boxes
+//   in 256-bit loads; 3 = 6 blocks per SM (at most 80 registers, no spills).
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
-  if (bvh_kind == BVH_WIDE4) return (const void*)k_trace<BVH_WIDE4, false, 8, true>;
+  if (bvh_kind == BVH_WIDE4) {
+    if (variant == 1) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, 8>;
+    if (variant == 2) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, 0, true>;
+    if (variant == 3) return (const void*)k_trace<BVH_WIDE4, false, 6, true>;
+    return (const void*)k_trace<BVH_WIDE4, false, 8, true>;
+  }
   if (bvh_kind == BVH_WIDE8)
     return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
   if (variant == 1) return (const void*)k_trace<BVH_BINARY, false>;
@@ -450,8 +461,19 @@ const void* trace_kernel_ptr(int bvh_kind, int variant) {
 void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st,
                   bool count_visits) {
   if (k.bvh_kind == BVH_WIDE4) {
-    if (count_visits) k_trace<BVH_WIDE4, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
-    else k_trace<BVH_WIDE4, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    if (k.trace_variant == 1) {
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+    } else if (k.trace_variant == 2) {
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    } else if (k.trace_variant == 3) {
+      if (count_visits) k_trace<BVH_WIDE4, true, 6, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 6, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    } else {
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    }
     return;
   }
   if (k.bvh_kind == BVH_WIDE8) {

@@ -162,8 +162,13 @@ typedef struct {
   int32_t trace_variant;      /* binary BVH: 0 = 64 registers, fused box tests, dynamic ray fetch,
                                * while-while traversal (default); 1 = compiler's register choice,
                                * grid-stride rays, leaves tested where met; 2 = variant 1 held to 64
-                               * registers; 3 = variant 0 with leaves tested where met */
-  int32_t shade_variant;      /* 0 = compiler's register choice (default), 1 = at most 64 registers */
+                               * registers; 3 = variant 0 with leaves tested where met; 4 = variant
+                               * 0 with lane refill. 4-wide BVH: 0 = at most 64 registers,
+                               * traversal stack in local memory (default); 1 = its first 8
+                               * entries in shared memory; 2 = node boxes in 256-bit loads;
+                               * 3 = at most 80 registers. Other layouts ignore it. */
+  int32_t shade_variant;      /* 0 = compiler's register choice (default), 1 / 2 / 3 = at most
+                               * 64 / 80 / 72 registers */
   int32_t estimator;          /* illume_estimator */
   int32_t reserved;
 } illume_render_params;
