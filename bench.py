@@ -384,7 +384,7 @@ def _job_params(scene, d, C, camera=None):
     p.width, p.height = d["width"], d["height"]
     p.seed, p.job = d.get("seed", 0), d["job"]
     p.intersector = C.ISECT_WATERTIGHT
-    p.bvh_kind = C.BVH_BINARY
+    p.bvh_kind = C.BVH_WIDE4
     p.accum_mode = C.ACCUM_FP32
     if camera is not None:
         p.camera = C.fptr(camera)

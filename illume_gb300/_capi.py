@@ -35,7 +35,7 @@ ISECT_MT, ISECT_WATERTIGHT = range(2)
 BVH_BINARY, BVH_WIDE8, BVH_WIDE8_PERSISTENT, BVH_WIDE4 = range(4)
 ACCUM_FP32, ACCUM_KAHAN, ACCUM_FP64 = range(3)
 ESTIMATOR_REFERENCE, ESTIMATOR_NEE = range(2)
-SERVER_PATH_CAPACITY, SERVER_PASSES_PER_STEP, SERVER_AUTOTUNE, SERVER_TRACE_VARIANT = range(4)
+SERVER_PATH_CAPACITY, SERVER_PASSES_PER_STEP, SERVER_AUTOTUNE, SERVER_TRACE_VARIANT, SERVER_LANES = range(5)
 
 _pi32 = POINTER(c_int32)
 _pf = POINTER(c_float)

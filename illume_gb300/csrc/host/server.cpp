@@ -19,11 +19,50 @@ static constexpr size_t kBytesPerPath = 6 * sizeof(float4) + sizeof(float4) + si
                                         sizeof(float4);
 
 static int engine_key(const illume_render_params& p) { return p.intersector * 16 + p.bvh_kind; }
+static constexpr int kMaxLanes = 4;
+
+LaneStream::~LaneStream() {
+  if (stream) {
+    cudaStreamSynchronize(stream);
+    cudaStreamDestroy(stream);
+  }
+  if (done) cudaEventDestroy(done);
+}
 
 Server::~Server() {
   if (ctx) cudaStreamSynchronize(ctx->stream);
+  engines.clear();
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
+}
+
+// A job table of `cap` path slots for the trace-kernel setting of `p`, on a new stream.
+int Server::new_engine(const illume_render_params& p, int key, long long cap, ServerEngine** out) {
+  ServerEngine se;
+  se.lane = std::make_shared<LaneStream>();
+  ILLUME_CUDA_TRY(cudaStreamCreateWithFlags(&se.lane->stream, cudaStreamNonBlocking));
+  ILLUME_CUDA_TRY(cudaEventCreateWithFlags(&se.lane->done, cudaEventDisableTiming));
+  se.eng.reset(new Engine);
+  se.eng->stream = se.lane->stream;
+  se.base_key = key / kMaxLanes;
+  RenderKnobs k = render_knobs(p);
+  k.trace_variant = trace_variant >= 0 ? trace_variant : (p.bvh_kind == 2 ? 1 : 0);
+  k.shade_variant = 0;
+  std::string err;
+  const int st = se.eng->init(ctx, rows, (int)cap, k, &err);
+  if (st != ILLUME_OK) { set_error(err); return st; }
+  // a table that joins a tuned setting takes the tuned candidate
+  auto tit = tuners.find(se.base_key);
+  if (tit != tuners.end() && tit->second.state == 2) {
+    for (const auto& kv : engines)
+      if (kv.second.base_key == se.base_key) {
+        se.eng->set_trace_variant(kv.second.eng->knobs.trace_variant);
+        break;
+      }
+  }
+  se.row_job.assign(rows, 0);
+  *out = &engines.emplace(key, std::move(se)).first->second;
+  return ILLUME_OK;
 }
 
 // Device bytes a running job holds: its accumulators and output staging.
@@ -83,28 +122,52 @@ int Server::admit() {
     if (j->state == 3) { it = queue.erase(it); continue; }
     const illume_render_params& p = j->params;
     const int npix = p.width * p.height;
-    const int key = engine_key(p);
-    auto eit = engines.find(key);
-    if (eit == engines.end()) {
+    const int base = engine_key(p);
+    // the table of this setting with a free row and the least work to go; a table not
+    // created yet when every existing one has work (or there is none)
+    ServerEngine* pick = nullptr;
+    int key = -1, missing = -1;
+    double least = 0.0;
+    for (int lane = 0; lane < lanes; ++lane) {
+      auto eit = engines.find(base * kMaxLanes + lane);
+      if (eit == engines.end()) {
+        if (missing < 0) missing = lane;
+        continue;
+      }
+      ServerEngine& c = eit->second;
+      bool free_row = false;
+      double work = 0.0;
+      for (int r = 0; r < c.eng->rows; ++r) {
+        if (!c.row_job[r]) { free_row = true; continue; }
+        const JobDesc& J = c.eng->mirror[r];
+        work += (double)J.npix * std::max(J.sample_end - J.sample_base, 0);
+      }
+      if (free_row && (!pick || work < least)) {
+        pick = &c;
+        key = eit->first;
+        least = work;
+      }
+    }
+    if ((!pick || least > 0.0) && missing >= 0) {
       long long cap = std::max(path_capacity, npix);
+      auto tit = tuners.find(base);
+      if (tit != tuners.end() && tit->second.state == 2) {
+        for (const auto& kv : engines)
+          if (kv.second.base_key == base) cap = std::max<long long>(kv.second.eng->cap, npix);
+      }
       if (budget) {
         const long long used = (long long)(reserved + engines_bytes() + j->footprint + (1 << 20));
         const long long affordable = ((long long)budget - used) / (long long)kBytesPerPath;
         cap = std::min(cap, affordable);
-        if (cap < npix) { ++it; continue; }
       }
-      ServerEngine se;
-      se.eng.reset(new Engine);
-      RenderKnobs k = render_knobs(p);
-      k.trace_variant = trace_variant >= 0 ? trace_variant : (p.bvh_kind == 2 ? 1 : 0);
-      k.shade_variant = 0;
-      std::string err;
-      const int st = se.eng->init(ctx, rows, (int)cap, k, &err);
-      if (st != ILLUME_OK) { set_error(err); return st; }
-      se.row_job.assign(rows, 0);
-      eit = engines.emplace(key, std::move(se)).first;
+      if (cap >= npix) {
+        const int st = new_engine(p, base * kMaxLanes + missing, cap, &pick);
+        if (st != ILLUME_OK) return st;
+        key = base * kMaxLanes + missing;
+      }
     }
-    ServerEngine& se = eit->second;
+    if (!pick) { ++it; continue; }
+    ServerEngine& se = *pick;
     Engine& e = *se.eng;
     int running = 0;
     int free_row = -1;
@@ -312,52 +375,71 @@ int Server::retire(ServerEngine& se, std::vector<ServerJob*>* done) {
   return ILLUME_OK;
 }
 
-int Server::apply_candidate(ServerEngine& se, int idx) {
-  Engine& e = *se.eng;
-  const int cap = se.candidates[idx].first;
-  for (int r = 0; r < e.rows; ++r)
-    if (se.row_job[r] && e.mirror[r].npix > cap) return ILLUME_ERR_INVALID;
-  std::string err;
-  int st = e.resize(cap, &err);
-  if (st != ILLUME_OK) { set_error(err); return st; }
-  return e.set_trace_variant(se.candidates[idx].second);
+// Applies candidate `idx` (path slots per table, trace kernel variant) to every table of
+// a trace-kernel setting; fails without change if a running job does not fit the slots.
+int Server::apply_candidate(int base_key, int idx) {
+  const Tuner& t = tuners[base_key];
+  const int cap = t.candidates[idx].first;
+  for (const auto& kv : engines) {
+    if (kv.second.base_key != base_key) continue;
+    for (int r = 0; r < kv.second.eng->rows; ++r)
+      if (kv.second.row_job[r] && kv.second.eng->mirror[r].npix > cap) return ILLUME_ERR_INVALID;
+  }
+  for (auto& kv : engines) {
+    if (kv.second.base_key != base_key) continue;
+    Engine& e = *kv.second.eng;
+    std::string err;
+    int st = e.resize(cap, &err);
+    if (st != ILLUME_OK) { set_error(err); return st; }
+    if ((st = e.set_trace_variant(t.candidates[idx].second)) != ILLUME_OK) return st;
+  }
+  return ILLUME_OK;
 }
 
-// Online autotuner: every candidate runs a window of steps on the live jobs; the rate
-// of the window's steps after the first (rays per device ms) decides.
-void Server::tune(ServerEngine& se, double rays, double ms) {
+// Online autotuner of one trace-kernel setting: every candidate runs a window of steps
+// on the live jobs; the rate of the window's steps after the first (rays of the
+// setting's tables per device ms of the step) decides.
+void Server::tune(int base_key, double rays, double ms) {
   static constexpr int kWindow = 3;
-  if (se.tune_state == 0) {
+  Tuner& t = tuners[base_key];
+  if (t.state == 0) {
+    int kind = BVH_BINARY, ntables = 0;
+    size_t held = 0;
+    for (const auto& kv : engines)
+      if (kv.second.base_key == base_key) {
+        kind = kv.second.eng->knobs.bvh_kind;
+        held += kv.second.eng->device_bytes();
+        ++ntables;
+      }
     // binary BVH: the default kernel and its while-while form; 8-wide: both kernels;
     // 4-wide: the traversal stack in local memory or partly in shared memory
-    const std::vector<int> variants = se.eng->knobs.bvh_kind == BVH_BINARY ? std::vector<int>{0, 3}
-                                                                           : std::vector<int>{0, 1};
+    const std::vector<int> variants = kind == BVH_BINARY ? std::vector<int>{0, 3} : std::vector<int>{0, 1};
     for (int cap : {1 << 23, 1 << 24}) {
-      if (budget && reserved + engines_bytes() - se.eng->device_bytes() + (size_t)cap * kBytesPerPath > budget) continue;
-      for (int v : variants) se.candidates.push_back({cap, v});
+      if (budget && reserved + engines_bytes() - held + (size_t)ntables * cap * kBytesPerPath > budget) continue;
+      for (int v : variants) t.candidates.push_back({cap, v});
     }
-    se.rate.assign(se.candidates.size(), 0.0);
-    se.tune_state = 1;
-    se.tune_idx = -1;
+    t.rate.assign(t.candidates.size(), 0.0);
+    t.state = 1;
+    t.idx = -1;
   } else {
-    ++se.tune_steps;
-    if (se.tune_steps > 1) { se.tune_rays += rays; se.tune_ms += ms; }
-    if (se.tune_steps < kWindow) return;
-    se.rate[se.tune_idx] = se.tune_ms > 0 ? se.tune_rays / se.tune_ms : 0.0;
+    ++t.steps;
+    if (t.steps > 1) { t.rays += rays; t.ms += ms; }
+    if (t.steps < kWindow) return;
+    t.rate[t.idx] = t.ms > 0 ? t.rays / t.ms : 0.0;
   }
   // next candidate that fits the running jobs
-  for (++se.tune_idx; se.tune_idx < (int)se.candidates.size(); ++se.tune_idx)
-    if (apply_candidate(se, se.tune_idx) == ILLUME_OK) break;
-  if (se.tune_idx < (int)se.candidates.size()) {
-    se.tune_rays = se.tune_ms = 0;
-    se.tune_steps = 0;
+  for (++t.idx; t.idx < (int)t.candidates.size(); ++t.idx)
+    if (apply_candidate(base_key, t.idx) == ILLUME_OK) break;
+  if (t.idx < (int)t.candidates.size()) {
+    t.rays = t.ms = 0;
+    t.steps = 0;
     return;
   }
   int best = -1;
-  for (size_t i = 0; i < se.rate.size(); ++i)
-    if (se.rate[i] > 0 && (best < 0 || se.rate[i] > se.rate[best])) best = (int)i;
-  if (best >= 0) apply_candidate(se, best);
-  se.tune_state = 2;
+  for (size_t i = 0; i < t.rate.size(); ++i)
+    if (t.rate[i] > 0 && (best < 0 || t.rate[i] > t.rate[best])) best = (int)i;
+  if (best >= 0) apply_candidate(base_key, best);
+  t.state = 2;
 }
 
 int Server::step(int* running_out) {
@@ -368,6 +450,11 @@ int Server::step(int* running_out) {
   int st = admit();
   if (st != ILLUME_OK) return st;
   std::vector<ServerJob*> done;
+  // every table's passes are launched on its own stream before any is waited for
+  struct Launched { ServerEngine* se; int k; unsigned long long total; };
+  std::vector<Launched> launched;
+  launched.reserve(engines.size());
+  ILLUME_CUDA_TRY(cudaEventRecord(ev0, ctx->stream));
   for (auto& kv : engines) {
     ServerEngine& se = kv.second;
     Engine& e = *se.eng;
@@ -385,24 +472,33 @@ int Server::step(int* running_out) {
     if (depth == 0 && e.paths_in_pass() == 0) continue;
     k = std::max(k, 1);
     const int per_pass_launches = Engine::launches_per_pass(depth, e.any_nee());
-    ILLUME_CUDA_TRY(cudaEventRecord(ev0, ctx->stream));
+    ILLUME_CUDA_TRY(cudaStreamWaitEvent(e.stream, ev0, 0));   // after admission's clears
     if ((st = e.run(k, depth)) != ILLUME_OK) return st;
-    ILLUME_CUDA_TRY(cudaEventRecord(ev1, ctx->stream));
+    ILLUME_CUDA_TRY(cudaEventRecord(se.lane->done, e.stream));
+    ILLUME_CUDA_TRY(cudaStreamWaitEvent(ctx->stream, se.lane->done, 0));
     for (int r : active) jobs[se.row_job[r]]->stats.kernel_launches += (int64_t)k * per_pass_launches;
-    unsigned long long total = 0;
-    ILLUME_CUDA_TRY(cudaMemcpyAsync(&total, e.w.rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, ev0, ev1);
-    const double rays = (double)(total - se.rays_seen);
-    se.rays_seen = total;
-    totals.rays += (int64_t)rays;
     totals.passes += k;
     totals.kernel_launches += (int64_t)k * per_pass_launches;
-    totals.device_ms += ms;
-    if ((st = retire(se, &done)) != ILLUME_OK) return st;
-    if (autotune && se.tune_state != 2) tune(se, rays, ms);
+    launched.push_back({&se, k, 0});
   }
+  ILLUME_CUDA_TRY(cudaEventRecord(ev1, ctx->stream));
+  for (Launched& l : launched)
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&l.total, l.se->eng->w.rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  float ms = 0.0f;
+  if (!launched.empty()) cudaEventElapsedTime(&ms, ev0, ev1);
+  totals.device_ms += ms;
+  std::map<int, double> rays_by_key;
+  for (Launched& l : launched) {
+    const double rays = (double)(l.total - l.se->rays_seen);
+    l.se->rays_seen = l.total;
+    totals.rays += (int64_t)rays;
+    rays_by_key[l.se->base_key] += rays;
+    if ((st = retire(*l.se, &done)) != ILLUME_OK) return st;
+  }
+  if (autotune)
+    for (const auto& kr : rays_by_key)
+      if (tuners[kr.first].state != 2) tune(kr.first, kr.second, ms);
   const double t = now_ms();
   for (ServerJob* j : done) {
     j->finish_ms = t;
@@ -437,6 +533,7 @@ int Server::cancel(int64_t id) {
     ServerEngine& se = engines[j->key];
     se.eng->mirror[j->row].nsamples = 0;
     se.eng->write_pass_state(j->row);
+    ILLUME_CUDA_TRY(cudaStreamSynchronize(se.eng->stream));
     ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     se.row_job[j->row] = 0;
     se.eng->mirror[j->row] = JobDesc{};
@@ -469,6 +566,10 @@ int Server::set_option(int option, int64_t value) {
       if (value < -1 || value > 4) { set_error("unknown trace kernel variant"); return ILLUME_ERR_INVALID; }
       trace_variant = (int)value;
       return ILLUME_OK;
+    case ILLUME_SERVER_LANES:
+      if (value < 1 || value > kMaxLanes) { set_error("lanes out of range"); return ILLUME_ERR_INVALID; }
+      lanes = (int)value;
+      return ILLUME_OK;
     default:
       set_error("unknown server option");
       return ILLUME_ERR_INVALID;
@@ -483,8 +584,8 @@ void Server::get_stats(illume_server_stats* out) const {
   for (const auto& kv : engines) {
     out->path_capacity = std::max<int64_t>(out->path_capacity, kv.second.eng->cap);
     out->trace_variant = kv.second.eng->knobs.trace_variant;
-    out->tuned |= kv.second.tune_state == 2;
   }
+  for (const auto& kv : tuners) out->tuned |= kv.second.state == 2;
   out->device_bytes = (int64_t)(engines_bytes() + reserved);
 }
 

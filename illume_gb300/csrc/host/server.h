@@ -15,8 +15,13 @@
 // sample order whatever the pass split, so the result is bit-identical alone and in
 // any mix.
 //
-// The autotuner picks the table's path slots and trace kernel variant from measured
-// throughput on the live workload: each candidate runs a few passes of the real jobs
+// Every trace-kernel setting has up to `lanes` job tables, each on its own stream; an
+// admitted job joins the table with the least work to go and stays there. A step
+// launches every table's passes at once, so one table's last bounces (few, long rays
+// that leave most of the GPU idle) overlap the other tables' passes.
+//
+// The autotuner picks the tables' path slots and trace kernel variant from measured
+// throughput on the live workload: each candidate runs a few steps of the real jobs
 // (no work is thrown away, since the split of samples into passes and the kernel
 // variant do not change any result), then the fastest is kept.
 #pragma once
@@ -46,15 +51,30 @@ struct ServerJob {
   double submit_ms = 0, start_ms = 0, finish_ms = 0;
 };
 
+// A job table's stream and the event that marks the end of its work in a step.
+struct LaneStream {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  LaneStream() = default;
+  LaneStream(const LaneStream&) = delete;
+  LaneStream& operator=(const LaneStream&) = delete;
+  ~LaneStream();
+};
+
 struct ServerEngine {
+  std::shared_ptr<LaneStream> lane;      // declared before eng: outlives the engine's buffers
   std::unique_ptr<Engine> eng;
+  int base_key = 0;                      // trace-kernel setting (engine_key)
   std::vector<int64_t> row_job;          // job id per row, 0 = free
   unsigned long long rays_seen = 0;      // engine ray total at the last read
-  // autotuner
-  int tune_state = 0;                    // 0 not started, 1 measuring, 2 done
-  int tune_idx = 0, tune_steps = 0;
-  double tune_rays = 0, tune_ms = 0;
-  std::vector<std::pair<int, int>> candidates;   // (path slots, trace variant)
+};
+
+// Autotuner state of one trace-kernel setting (all its tables move together).
+struct Tuner {
+  int state = 0;                         // 0 not started, 1 measuring, 2 done
+  int idx = 0, steps = 0;
+  double rays = 0, ms = 0;
+  std::vector<std::pair<int, int>> candidates;   // (path slots per table, trace variant)
   std::vector<double> rate;                      // rays per ms of each candidate
 };
 
@@ -66,11 +86,13 @@ struct Server {
   int passes_per_step = 1;
   int autotune = 0;
   int trace_variant = -1;     // -1 = per-layout default
+  int lanes = 2;              // job tables per trace-kernel setting
   size_t reserved = 0;        // job footprints
   int64_t next_id = 1;
   std::map<int64_t, std::unique_ptr<ServerJob>> jobs;
   std::deque<int64_t> queue;
-  std::map<int, ServerEngine> engines;
+  std::map<int, ServerEngine> engines;   // by engine_key * kMaxLanes + lane
+  std::map<int, Tuner> tuners;           // by engine_key
   illume_server_stats totals{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -88,8 +110,9 @@ struct Server {
   int admit();
   void compose(ServerEngine& se);
   int retire(ServerEngine& se, std::vector<ServerJob*>* done);
-  void tune(ServerEngine& se, double rays, double ms);
-  int apply_candidate(ServerEngine& se, int idx);
+  int new_engine(const illume_render_params& p, int key, long long cap, ServerEngine** out);
+  void tune(int base_key, double rays, double ms);
+  int apply_candidate(int base_key, int idx);
 };
 
 double now_ms();

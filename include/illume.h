@@ -342,7 +342,9 @@ typedef enum {
   ILLUME_SERVER_PATH_CAPACITY = 0,    /* path slots of each job table (default 8388608) */
   ILLUME_SERVER_PASSES_PER_STEP = 1,  /* passes per illume_server_step (default 1) */
   ILLUME_SERVER_AUTOTUNE = 2,         /* 1 = choose path slots and trace kernel from measured throughput */
-  ILLUME_SERVER_TRACE_VARIANT = 3     /* trace kernel variant (-1 = default) */
+  ILLUME_SERVER_TRACE_VARIANT = 3,    /* trace kernel variant (-1 = default) */
+  ILLUME_SERVER_LANES = 4             /* job tables per trace-kernel setting, each on its own
+                                       * stream, whose passes overlap (1-4, default 2) */
 } illume_server_option;
 int illume_server_set_option(illume_server* s, int option, int64_t value);
 
