@@ -60,7 +60,8 @@ def parse():
                     help="reference: BSDF sampling only (the reference's estimator); nee: next-event estimation "
                          "with MIS (shadow rays count as rays)")
     ap.add_argument("--shade-variant", type=int, default=0,
-                    help="shade kernel: 0 compiler register choice (default), 1 at most 64 registers")
+                    help="shade kernel: 0 measured best register bound (default), 1 compiler's choice, "
+                         "2 / 3 / 4 at most 80 / 72 / 64 registers")
     ap.add_argument("--tris", type=int, default=100_000)
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--depth", type=int, default=25)
@@ -282,6 +283,27 @@ def run_ours(args):
         dev_ms_max, rays_all = dev_ms, rays
     value = rays_all / (dev_ms_max * 1e-3) / 1e6
 
+    # image quality of what was timed: every warm-up and timed step accumulated into one
+    # image; the FP64 oracle renders the same samples (same Philox streams) of a pixel
+    # subset, so the difference is the FP32 arithmetic of the GPU path
+    acc_spp = (args.warmup + args.steps) * args.spp_per_step
+    quality = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import pyoracle
+        g = r.read(mean=False, sums=True)
+        npix_q = args.res * args.res
+        subset = np.arange(npix_q // 97, npix_q, npix_q // 48, dtype=np.int32)[:48]
+        t0q = time.perf_counter()
+        osum, _, _ = pyoracle.OracleScene(sd).render(args.res, args.res, acc_spp, args.depth, seed=p.seed, job=p.job,
+                                                      isect=C.ISECT_WATERTIGHT, precision=64, pixels=subset,
+                                                      sample_begin=p.sample_begin)
+        om = osum / acc_spp
+        gm = g["sum"][subset] / acc_spp
+        quality = {"pixels": int(len(subset)), "spp": int(acc_spp),
+                   "rmse_vs_fp64_oracle": float(np.sqrt(np.mean((gm - om) ** 2))),
+                   "rel_rmse_vs_fp64_oracle": float(np.sqrt(np.mean((gm - om) ** 2)) / max(float(np.mean(np.abs(om))), 1e-12)),
+                   "max_rel_err": float(np.max(np.abs(gm - om) / np.maximum(np.abs(om), 1e-6))),
+                   "oracle_s": round(time.perf_counter() - t0q, 1)}
     # the renderer splits a step over two engines when each half-pass keeps >= 2M paths
     npix_all = args.res * args.res
     pass_spp = ((args.spp_per_step + 1) // 2 if args.spp_per_step >= 2 and args.spp_per_step * npix_all >= (1 << 22)
@@ -363,6 +385,7 @@ def run_ours(args):
                          "profiled_pass_spp": pass_spp,
                          "trace_ms_per_pass": round(prof_t.trace_ms, 3), "shade_ms_per_pass": round(prof_t.shade_ms, 3)},
             "cpu_baseline": cpu,
+            "quality": quality,
             "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s",
                     "h2d_bytes_per_step": int(up_bytes.value) + 16, "d2h_bytes_per_step": npix * (12 + 3) + 8,
                     "ms_per_step": round(e2e_s / e2e_steps * 1e3, 3),

@@ -115,20 +115,26 @@ struct DevMedium { float absorption[3]; float scattering, g; int active; int pad
 
 // Light sampling data of a scene (the opt-in next-event estimator; the reference
 // estimator never reads it).
+// Alias table entry (Walker): slot i keeps itself with probability `keep`, else `alias`.
+struct AliasEntry {
+  float keep;
+  int alias;
+};
+
 struct LightView {
   // environment: piecewise-constant density over the map's texels, proportional to
   // luminance x cos(elevation); env_w == 0 when the environment is not sampled
   int env_w, env_h;
-  const float* env_func;        // env_h x env_w texel weights
-  const float* env_marginal;    // env_h + 1 cumulative row weights (last = 1)
-  const float* env_cond;        // env_h x (env_w + 1) cumulative weights within each row
-  float env_integral;           // mean texel weight (density normaliser)
-  float env_prob;               // probability of sampling the environment rather than a triangle
+  const float* env_func;          // env_h x env_w texel weights
+  const AliasEntry* env_rows;     // env_h entries: a row by its total weight
+  const AliasEntry* env_cols;     // env_h x env_w entries: a texel of a row by its weight
+  float env_integral;             // mean texel weight (density normaliser)
+  float env_prob;                 // probability of sampling the environment rather than a triangle
   // emissive triangles of mesh instances, world space, chosen by area x luminance
   int num_tri;
-  const float4* tri;            // 3 float4 per light: (v0, area), (e1, select prob), (e2, instance / prim bits)
-  const float* tri_cdf;         // num_tri + 1 cumulative select probabilities
-  const int* inst_light_base;   // per instance: index of its first light (-1: not emissive)
+  const float4* tri;              // 3 float4 per light: (v0, area), (e1, select prob), (e2, instance / prim bits)
+  const AliasEntry* tri_alias;    // num_tri entries: a triangle by its weight
+  const int* inst_light_base;     // per instance: index of its first light (-1: not emissive)
   int pad[2];
 };
 

@@ -352,6 +352,20 @@ int illume_trace_closest(illume_context* ctx, illume_scene* scene, const float* 
   return ILLUME_OK;
 }
 
+int illume_alias_table(int n, const double* weights, float* keep, int32_t* alias) {
+  CHECK_ARG(n >= 0 && (n == 0 || (weights && keep && alias)), "null argument");
+  std::vector<AliasEntry> t(n);
+  if (!build_alias(weights, (size_t)n, t.data())) {
+    set_error("weights sum to zero");
+    return ILLUME_ERR_INVALID;
+  }
+  for (int i = 0; i < n; ++i) {
+    keep[i] = t[i].keep;
+    alias[i] = t[i].alias;
+  }
+  return ILLUME_OK;
+}
+
 int illume_bsdf_batch(illume_context* ctx, int material_type, int distribution, const float* inputs, int n,
                       float* outputs) {
   CHECK_ARG(ctx && n >= 0 && (n == 0 || (inputs && outputs)), "bad argument");

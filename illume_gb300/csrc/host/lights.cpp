@@ -63,30 +63,18 @@ void build_env(const SceneHost& h, HostLights* L) {
   L->env_w = w;
   L->env_h = hh;
   L->env_func.resize((size_t)w * hh);
-  L->env_cond.resize((size_t)hh * (w + 1));
-  L->env_marginal.resize(hh + 1);
+  L->env_cols.resize((size_t)w * hh);
+  L->env_rows.resize(hh);
   std::vector<double> row(hh);
   double total = 0.0;
   for (int y = 0; y < hh; ++y) {
+    build_alias(&f[(size_t)y * w], w, &L->env_cols[(size_t)y * w]);
     double acc = 0.0;
-    float* cdf = &L->env_cond[(size_t)y * (w + 1)];
-    cdf[0] = 0.0f;
-    for (int x = 0; x < w; ++x) {
-      acc += f[(size_t)y * w + x];
-      cdf[x + 1] = (float)acc;
-    }
-    for (int x = 1; x <= w; ++x) cdf[x] = (float)(cdf[x] / acc);
-    cdf[w] = 1.0f;
+    for (int x = 0; x < w; ++x) acc += f[(size_t)y * w + x];
     row[y] = acc;
     total += acc;
   }
-  L->env_marginal[0] = 0.0f;
-  double acc = 0.0;
-  for (int y = 0; y < hh; ++y) {
-    acc += row[y];
-    L->env_marginal[y + 1] = (float)(acc / total);
-  }
-  L->env_marginal[hh] = 1.0f;
+  build_alias(row.data(), hh, L->env_rows.data());
   const double mean = total / ((double)w * hh);
   for (size_t i = 0; i < f.size(); ++i) L->env_func[i] = (float)f[i];
   L->env_integral = (float)mean;
@@ -134,27 +122,49 @@ void build_triangles(const SceneHost& h, HostLights* L) {
   for (double w : weight) total += w;
   if (!(total > 0.0)) {
     L->tri.clear();
-    L->tri_cdf.clear();
+    L->tri_alias.clear();
     for (int& b : L->inst_light_base) b = -1;
     return;
   }
-  L->tri_cdf.assign(n + 1, 0.0f);
-  double acc = 0.0;
-  for (size_t k = 0; k < n; ++k) {
-    acc += weight[k];
-    L->tri_cdf[k + 1] = (float)(acc / total);
-    L->tri[3 * k + 1].w = (float)(weight[k] / total);
-  }
-  L->tri_cdf[n] = 1.0f;
+  L->tri_alias.resize(n);
+  build_alias(weight.data(), n, L->tri_alias.data());
+  for (size_t k = 0; k < n; ++k) L->tri[3 * k + 1].w = (float)(weight[k] / total);
 }
 
 }  // namespace
+
+bool build_alias(const double* weights, size_t n, AliasEntry* out) {
+  double total = 0.0;
+  for (size_t i = 0; i < n; ++i) total += std::max(weights[i], 0.0);
+  for (size_t i = 0; i < n; ++i) out[i] = AliasEntry{1.0f, (int)i};
+  if (!(total > 0.0) || n == 0) return false;
+  std::vector<double> scaled(n);
+  std::vector<size_t> small, large;
+  for (size_t i = 0; i < n; ++i) {
+    scaled[i] = std::max(weights[i], 0.0) * (double)n / total;
+    (scaled[i] < 1.0 ? small : large).push_back(i);
+  }
+  while (!small.empty() && !large.empty()) {
+    const size_t s = small.back(), l = large.back();
+    small.pop_back();
+    out[s] = AliasEntry{(float)scaled[s], (int)l};
+    scaled[l] = (scaled[l] + scaled[s]) - 1.0;
+    if (scaled[l] < 1.0) {
+      large.pop_back();
+      small.push_back(l);
+    }
+  }
+  // what is left has probability 1 up to rounding: keeps itself
+  for (size_t i : large) out[i] = AliasEntry{1.0f, (int)i};
+  for (size_t i : small) out[i] = AliasEntry{1.0f, (int)i};
+  return true;
+}
 
 void build_lights(const SceneHost& h, HostLights* out) {
   *out = HostLights{};
   build_env(h, out);
   build_triangles(h, out);
-  const bool env = out->env_w > 0, tri = !out->tri_cdf.empty();
+  const bool env = out->env_w > 0, tri = !out->tri_alias.empty();
   out->env_prob = env && tri ? 0.5f : (env ? 1.0f : 0.0f);
 }
 

@@ -40,7 +40,7 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if (p.bvh_kind == 3 && (p.trace_variant < 0 || p.trace_variant > 3)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.accum_mode < ACCUM_FP32 || p.accum_mode > ACCUM_FP64) { *err = "unknown accumulation mode"; return ILLUME_ERR_INVALID; }
   if (p.samples_per_pass < 0) { *err = "negative samples per pass"; return ILLUME_ERR_INVALID; }
-  if (p.shade_variant < 0 || p.shade_variant > 3) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
+  if (p.shade_variant < 0 || p.shade_variant > 4) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.estimator < ILLUME_ESTIMATOR_REFERENCE || p.estimator > ILLUME_ESTIMATOR_NEE) { *err = "unknown estimator"; return ILLUME_ERR_INVALID; }
   if ((int)scene.t_mediums.size() > kMaxMediums) { *err = "too many mediums"; return ILLUME_ERR_UNSUPPORTED; }
   if (!scene.ctx || !scene.view_dev) { *err = "scene has not been uploaded to a device"; return ILLUME_ERR_INVALID; }

@@ -551,13 +551,13 @@ int Scene::build_and_upload(std::string* err) {
     lv.env_prob = L.env_prob;
     if (L.env_w > 0) {
       UP(L.env_func.data(), L.env_func.size() * sizeof(float), lv.env_func);
-      UP(L.env_marginal.data(), L.env_marginal.size() * sizeof(float), lv.env_marginal);
-      UP(L.env_cond.data(), L.env_cond.size() * sizeof(float), lv.env_cond);
+      UP(L.env_rows.data(), L.env_rows.size() * sizeof(AliasEntry), lv.env_rows);
+      UP(L.env_cols.data(), L.env_cols.size() * sizeof(AliasEntry), lv.env_cols);
     }
-    lv.num_tri = (int)L.tri_cdf.size() > 0 ? (int)L.tri_cdf.size() - 1 : 0;
+    lv.num_tri = (int)L.tri_alias.size();
     if (lv.num_tri > 0) {
       UP(L.tri.data(), L.tri.size() * sizeof(float4), lv.tri);
-      UP(L.tri_cdf.data(), L.tri_cdf.size() * sizeof(float), lv.tri_cdf);
+      UP(L.tri_alias.data(), L.tri_alias.size() * sizeof(AliasEntry), lv.tri_alias);
     }
     if (!L.inst_light_base.empty()) UP(L.inst_light_base.data(), L.inst_light_base.size() * sizeof(int), lv.inst_light_base);
     lights_view = lv;

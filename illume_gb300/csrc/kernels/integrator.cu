@@ -556,16 +556,18 @@ __global__ void k_bsdf_batch(int type, int dist, const float* in, int n, float* 
 }
 
 // Shade kernel variants (RenderKnobs::shade_variant), by the blocks of 128 that must fit
-// an SM: 0 = compiler's register choice (the default), 1 = 8 blocks (at most 64
-// registers: more loads in flight, but the spills it needs cost more; measured slower on
-// the traversal workload), 2 = 6 blocks (at most 80 registers), 3 = 7 blocks (72).
+// an SM (the kernel waits on chains of dependent gathers, so resident warps matter):
+// 0 = the measured best (8 blocks, at most 64 registers, for both estimators, although
+// the next-event instance spills), 1 = compiler's register choice, 2 = 6 blocks (at most
+// 80 registers), 3 = 7 blocks (72), 4 = 8 blocks.
 template <bool NEE>
 static const void* shade_ptr(int variant) {
   switch (variant) {
-    case 1: return (const void*)k_shade<8, NEE>;
+    case 1: return (const void*)k_shade<1, NEE>;
     case 2: return (const void*)k_shade<6, NEE>;
     case 3: return (const void*)k_shade<7, NEE>;
-    default: return (const void*)k_shade<1, NEE>;
+    case 4: return (const void*)k_shade<8, NEE>;
+    default: return (const void*)k_shade<8, NEE>;
   }
 }
 const void* shade_kernel_ptr(int variant, bool nee) { return nee ? shade_ptr<true>(variant) : shade_ptr<false>(variant); }

@@ -4,9 +4,10 @@
 // At a surface vertex with a non-delta reflection lobe (lambert, rough conductor, rough
 // dielectric reflection) that is not the path's last, one light sample is taken: the
 // environment (piecewise-constant density over the map, luminance x cos(elevation)) or
-// an emissive mesh triangle (chosen by area x luminance, uniform over its area). Its
-// contribution, weighted by the power heuristic against the BSDF's density for the same
-// direction, is added if a shadow ray finds nothing in between. A BSDF-sampled ray that
+// an emissive mesh triangle (chosen by area x luminance, uniform over its area), each
+// choice an alias-table lookup. Its contribution, weighted by the power heuristic
+// against the BSDF's density for the same direction, is added if a shadow ray finds
+// nothing in between. A BSDF-sampled ray that
 // then reaches an emitter or escapes is weighted by the power heuristic against the
 // light density; after delta or transmissive interactions, in media, and for emissive
 // spheres (not light-sampled) the weight is 1. Both estimators have the same
@@ -44,18 +45,24 @@ __device__ __forceinline__ float env_light_pdf(const LightView& L, V3 d) {
 __device__ __forceinline__ float tri_light_pdf(const LightView& L, int l, float t, float cos_l) {
   if (l < 0 || fabsf(cos_l) < 1e-7f) return 0.0f;
   const float area = __ldg(&L.tri[3 * l].w), psel = __ldg(&L.tri[3 * l + 1].w);
+  if (!(area > 0.0f)) return 0.0f;
   return (1.0f - L.env_prob) * psel * t * t / (area * fabsf(cos_l));
 }
 
-// Index of the last cumulative entry <= u in cdf[0..n] (cdf[0] = 0, cdf[n] = 1).
-__device__ __forceinline__ int cdf_find(const float* cdf, int n, float u) {
-  int lo = 0, hi = n;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(cdf + mid) <= u) lo = mid;
-    else hi = mid;
+// Entry of an alias table of n slots chosen by u in [0, 1): one load instead of a binary
+// search's chain of dependent loads. `frac` receives the rest of u's randomness, uniform
+// in [0, 1) given the choice.
+__device__ __forceinline__ int alias_pick(const AliasEntry* table, int n, float u, float& frac) {
+  const float x = u * (float)n;
+  const int i = min(max((int)x, 0), n - 1);
+  const float f = fminf(fmaxf(x - (float)i, 0.0f), 0.99999994f);
+  const float2 e = __ldg(reinterpret_cast<const float2*>(table + i));
+  if (f < e.x) {
+    frac = fminf(f / e.x, 0.99999994f);
+    return i;
   }
-  return lo;
+  frac = fminf((f - e.x) / (1.0f - e.x), 0.99999994f);
+  return __float_as_int(e.y);
 }
 
 struct LightSample {
@@ -76,15 +83,11 @@ __device__ __forceinline__ LightSample sample_light(const SceneView& sc, const L
   s.Le = v3(0.0f, 0.0f, 0.0f);
   s.dir = v3(0.0f, 0.0f, 1.0f);
   if (u0 < L.env_prob) {
-    // environment: row from the marginal, column from the row's conditional
-    const int y = cdf_find(L.env_marginal, L.env_h, u2);
-    const float* cond = L.env_cond + (size_t)y * (L.env_w + 1);
-    const int x = cdf_find(cond, L.env_w, u1);
-    const float m0 = __ldg(L.env_marginal + y), m1 = __ldg(L.env_marginal + y + 1);
-    const float c0 = __ldg(cond + x), c1 = __ldg(cond + x + 1);
-    const float fy = (float)y + (m1 > m0 ? fminf((u2 - m0) / (m1 - m0), 0.999999f) : 0.5f);
-    const float fx = (float)x + (c1 > c0 ? fminf((u1 - c0) / (c1 - c0), 0.999999f) : 0.5f);
-    const float u = fx / (float)L.env_w, v = fy / (float)L.env_h;
+    // environment: a row by its weight, then a texel of the row, uniform within the texel
+    float ry, rx;
+    const int y = alias_pick(L.env_rows, L.env_h, u2, ry);
+    const int x = alias_pick(L.env_cols + (size_t)y * L.env_w, L.env_w, u1, rx);
+    const float u = ((float)x + rx) / (float)L.env_w, v = ((float)y + ry) / (float)L.env_h;
     const float phi = (u - 0.5f) * 6.28318530717958648f;
     const float elev = (0.5f - v) * 3.14159265358979324f;
     const float ce = cosf(elev);
@@ -98,7 +101,8 @@ __device__ __forceinline__ LightSample sample_light(const SceneView& sc, const L
   }
   if (L.num_tri == 0) return s;
   const float ut = (u0 - L.env_prob) / (1.0f - L.env_prob);
-  const int l = cdf_find(L.tri_cdf, L.num_tri, fminf(ut, 0.99999994f));
+  float rest;
+  const int l = alias_pick(L.tri_alias, L.num_tri, fminf(fmaxf(ut, 0.0f), 0.99999994f), rest);
   const float4 a = __ldg(&L.tri[3 * l]), b = __ldg(&L.tri[3 * l + 1]), c = __ldg(&L.tri[3 * l + 2]);
   // uniform point on the triangle
   const float su = sqrtf(u1);

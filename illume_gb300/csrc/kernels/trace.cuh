@@ -281,11 +281,16 @@ __device__ __forceinline__ void bvh4_slot(float lox, float loy, float loz, float
   entry = h ? child : kEmptyEntry;
 }
 
-// Two consecutive float4 of read-only global memory in one 256-bit load (p 32-byte aligned).
-__device__ __forceinline__ void ldg_v8(const float4* p, float4& a, float4& b) {
-  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
-      : "l"(p));
+// The same test with the near and far planes already chosen by the ray's direction signs.
+__device__ __forceinline__ void bvh4_slot_nf(float nx, float ny, float nz, float fx, float fy, float fz, int child,
+                                             const TraceRay& r, float tbest, float& key, int& entry) {
+  const float t0 = max3f(__fmaf_rn(nx, r.idir.x, -r.oi.x), __fmaf_rn(ny, r.idir.y, -r.oi.y),
+                         fmaxf(__fmaf_rn(nz, r.idir.z, -r.oi.z), 0.0f));
+  const float t1 = min3f(__fmaf_rn(fx, r.idir.x, -r.oi.x), __fmaf_rn(fy, r.idir.y, -r.oi.y),
+                         __fmaf_rn(fz, r.idir.z, -r.oi.z)) * kExitSlack;
+  const bool h = t0 <= t1 && t0 <= tbest * kExitSlack;
+  key = h ? t0 : FLT_MAX;
+  entry = h ? child : kEmptyEntry;
 }
 
 __device__ __forceinline__ void sort_pair(float& ka, int& ea, float& kb, int& eb) {
@@ -305,12 +310,18 @@ __device__ __forceinline__ void sort_pair(float& ka, int& ea, float& kb, int& eb
 // SH > 0: the first SH stack entries live in shared memory (sh points at this thread's
 // column of a [SH][kTraceBlock] array: one bank per lane, no conflicts, never evicted by
 // node fetches), deeper entries in the local array.
-// V8: the node's six box vectors arrive in three 256-bit loads instead of six 128-bit ones.
-template <bool COUNT, bool ANY = false, int SH = 0, bool V8 = false>
+// NF: each ray loads its near and far planes straight from their byte offsets in the
+// node (chosen once per ray by the direction's signs and OR-ed into the 128-byte-aligned
+// node address) instead of loading lo and hi and selecting per child box; the box test
+// arithmetic is the same, so are the results.
+template <bool COUNT, bool ANY = false, int SH = 0, bool NF = false>
 __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
                                                  int* stack, VisitCount& vc, int* sh = nullptr) {
   constexpr int kEmpty = kEmptyEntry;
   int sp = 0, cur = 0, leaf = kEmpty, visits = 0;
+  // near-plane offsets in a Bvh4Node: lox/loy/loz at 0/16/32, hix/hiy/hiz at 48/64/80
+  const unsigned near_x = r.idir.x >= 0.0f ? 0u : 48u, near_y = r.idir.y >= 0.0f ? 16u : 64u,
+                 near_z = r.idir.z >= 0.0f ? 32u : 80u;
   auto push = [&](int v) {
     if (sp < kStack) {
       if (SH > 0 && sp < SH) sh[sp * kTraceBlock] = v;
@@ -327,22 +338,26 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
       if (COUNT) vc.nodes++;
       if (++visits > kMaxNodeVisits) { cur = kEmpty; leaf = kEmpty; sp = 0; break; }
       const Bvh4Node* n = m.bvh4 + cur;
-      float4 lx, ly, lz, hx, hy, hz;
-      if (V8) {
-        ldg_v8(&n->lox, lx, ly);
-        ldg_v8(&n->loz, lz, hx);
-        ldg_v8(&n->hiy, hy, hz);
-      } else {
-        lx = __ldg(&n->lox); ly = __ldg(&n->loy); lz = __ldg(&n->loz);
-        hx = __ldg(&n->hix); hy = __ldg(&n->hiy); hz = __ldg(&n->hiz);
-      }
       const int4 ch = __ldg(&n->child);
       float k0, k1, k2, k3;
       int e0, e1, e2, e3;
-      bvh4_slot(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, ch.x, r, best.t, k0, e0);
-      bvh4_slot(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, ch.y, r, best.t, k1, e1);
-      bvh4_slot(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, ch.z, r, best.t, k2, e2);
-      bvh4_slot(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, ch.w, r, best.t, k3, e3);
+      if (NF) {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(n);
+        auto plane = [&](unsigned off) { return __ldg(reinterpret_cast<const float4*>(a | off)); };
+        const float4 nx = plane(near_x), fx = plane(near_x ^ 48u), ny = plane(near_y), fy = plane(near_y ^ 80u);
+        const float4 nz = plane(near_z), fz = plane(near_z ^ 112u);
+        bvh4_slot_nf(nx.x, ny.x, nz.x, fx.x, fy.x, fz.x, ch.x, r, best.t, k0, e0);
+        bvh4_slot_nf(nx.y, ny.y, nz.y, fx.y, fy.y, fz.y, ch.y, r, best.t, k1, e1);
+        bvh4_slot_nf(nx.z, ny.z, nz.z, fx.z, fy.z, fz.z, ch.z, r, best.t, k2, e2);
+        bvh4_slot_nf(nx.w, ny.w, nz.w, fx.w, fy.w, fz.w, ch.w, r, best.t, k3, e3);
+      } else {
+        const float4 lx = __ldg(&n->lox), ly = __ldg(&n->loy), lz = __ldg(&n->loz);
+        const float4 hx = __ldg(&n->hix), hy = __ldg(&n->hiy), hz = __ldg(&n->hiz);
+        bvh4_slot(lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, ch.x, r, best.t, k0, e0);
+        bvh4_slot(lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, ch.y, r, best.t, k1, e1);
+        bvh4_slot(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, ch.z, r, best.t, k2, e2);
+        bvh4_slot(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, ch.w, r, best.t, k3, e3);
+      }
       sort_pair(k0, e0, k1, e1);
       sort_pair(k2, e2, k3, e3);
       sort_pair(k0, e0, k2, e2);
@@ -558,7 +573,7 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 // found closer than tmax (occlusion; with the binary and 4-wide layouts).
 // SH: shared-memory stack entries of the 4-wide traversal (sh_stack: this thread's column).
 template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false, bool ANY = false, int SH = 0,
-          bool V8 = false>
+          bool NF = false>
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
                                                  VisitCount* vcp = nullptr, float tmax = FLT_MAX,
                                                  int* sh_stack = nullptr) {
@@ -593,7 +608,7 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     MeshBest b{h.t, -1, 0.0f, 0.0f};
     const DevMesh& m = sc.meshes[in.mesh];
     if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);
-    else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT, ANY, SH, V8>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc, sh_stack);
+    else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT, ANY, SH, NF>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc, sh_stack);
     else if (WW) traverse_bvh2_ww<COUNT, FMA, ANY>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else traverse_bvh2<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }

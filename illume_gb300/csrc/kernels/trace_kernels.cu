@@ -44,7 +44,7 @@ __device__ __forceinline__ int event_class(const WaveBuffers& w, const JobDesc& 
 // shared counter (counters[44 + parity]) instead of a fixed grid stride, so that warps
 // whose rays finish early take over the remaining work.
 // SH (4-wide only): stack entries kept in shared memory.
-template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false, int SH = 0, bool V8 = false>
+template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false, int SH = 0, bool NF = false>
 __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
   __shared__ int sh_stack[SH > 0 ? SH * kTraceBlock : 1];
   const int parity = bounce & 1;
@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace(WaveBuffers w, Rend
     const SceneView& sc = J.sc;
     VisitCount vc;
     const HitRecord h =
-        closest_hit<KIND, COUNT, OPT, WW, false, SH, V8>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack,
+        closest_hit<KIND, COUNT, OPT, WW, false, SH, NF>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack,
                                                      &vc, FLT_MAX, sh_stack + threadIdx.x);
     if (COUNT) { my_nodes += vc.nodes; my_tris += vc.tris; }
     const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
@@ -440,8 +440,9 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 //   variant 0 with lane refill (k_trace_refill);
 //   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine;
 //   4-wide BVH: 0 = at most 64 registers (8 blocks of 128 per SM), traversal stack in
-//   local memory (the default); 1 = its first 8 entries in shared memory; 2 = node boxes
-//   in 256-bit loads; 3 = 6 blocks per SM (at most 80 registers, no spills).
+//   local memory (the default); 1 = its first 8 entries in shared memory; 2 = near and
+//   far planes loaded by per-ray byte offsets; 3 = 6 blocks per SM (at most 80
+//   registers, no spills).
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (bvh_kind == BVH_WIDE4) {
     if (variant == 1) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, 8>;

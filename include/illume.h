@@ -165,10 +165,11 @@ typedef struct {
                                * registers; 3 = variant 0 with leaves tested where met; 4 = variant
                                * 0 with lane refill. 4-wide BVH: 0 = at most 64 registers,
                                * traversal stack in local memory (default); 1 = its first 8
-                               * entries in shared memory; 2 = node boxes in 256-bit loads;
-                               * 3 = at most 80 registers. Other layouts ignore it. */
-  int32_t shade_variant;      /* 0 = compiler's register choice (default), 1 / 2 / 3 = at most
-                               * 64 / 80 / 72 registers */
+                               * entries in shared memory; 2 = near and far planes loaded by
+                               * per-ray offsets; 3 = at most 80 registers. Other layouts
+                               * ignore it. */
+  int32_t shade_variant;      /* 0 = the measured best register bound (default), 1 = the
+                               * compiler's choice, 2 / 3 / 4 = at most 80 / 72 / 64 registers */
   int32_t estimator;          /* illume_estimator */
   int32_t reserved;
 } illume_render_params;
@@ -366,6 +367,13 @@ int illume_server_get_stats(const illume_server* s, illume_server_stats* out);
  * samples of job i go into each pass, sum(per_pass[i] * npix[i]) <= cap.
  * ILLUME_ERR_BUDGET when one sample of every job does not fit. */
 int illume_plan_pass_shares(int n, const int32_t* npix, const int32_t* left, int64_t cap, int32_t* per_pass);
+
+/* The alias table (Walker) that the next-event estimator picks lights with, for n
+ * non-negative weights (host only; exposed for tests; no counterpart in the reference,
+ * which samples no lights): u in [0, 1) picks slot floor(u n), which keeps itself when
+ * the fraction of u n is below keep[i] and becomes alias[i] otherwise, so that i comes
+ * out with probability weights[i] / sum. ILLUME_ERR_INVALID when the weights sum to 0. */
+int illume_alias_table(int n, const double* weights, float* keep, int32_t* alias);
 
 /* Renders n jobs together through one server (all submitted at once) and returns each
  * job's mean radiance (3 floats per pixel) and RGB8 in the nullable per-job buffers.

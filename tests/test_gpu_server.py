@@ -166,3 +166,18 @@ def test_split_render_same_image(ctx, scenes, accum):
     assert np.array_equal(big.read(mean=False, sums=True)["sum"], small.read(mean=False, sums=True)["sum"])
     big.close()
     small.close()
+
+
+def test_shade_variants_same_image(ctx, scenes):
+    """Every register bound of the shade kernel gives the same image, for both estimators."""
+    from illume_gb300.api import Renderer
+    for est in (C.ESTIMATOR_REFERENCE, C.ESTIMATOR_NEE):
+        for sc, p in job_list(scenes)[:3]:
+            p.estimator = est
+            want = Renderer(ctx, sc, params=p).render(mean=True)
+            for v in (1, 2, 3, 4):
+                q = C.RenderParams.from_buffer_copy(p)
+                q.shade_variant = v
+                got = Renderer(ctx, sc, params=q).render(mean=True)
+                assert np.array_equal(got["mean"], want["mean"], equal_nan=True), (est, v)
+                assert got["stats"].rays == want["stats"].rays
