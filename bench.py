@@ -139,6 +139,24 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def l2_copy_gbs(dev):
+    """Copy bandwidth between two L2-resident 24 MB buffers (read + write bytes), CUDA events."""
+    import torch
+    a = torch.empty(24 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    b = torch.empty_like(a)
+    for _ in range(20):
+        b.copy_(a)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 400
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(n):
+        b.copy_(a)
+    e1.record()
+    torch.cuda.synchronize()
+    return 2 * a.numel() * n / (e0.elapsed_time(e1) * 1e-3) / 1e9
+
+
 def measured_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -320,6 +338,7 @@ def run_ours(args):
     achieved_gbs = trace_bytes / (prof_t.trace_ms * 1e-3) / 1e9
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
+    l2_gbs = l2_copy_gbs(dev)
     # DRAM traffic of the trace kernel per launch: bytes per ray from the committed ncu
     # summary, times this workload's rays per trace launch
     traffic = None
@@ -383,6 +402,10 @@ def run_ours(args):
                          "node_fetches_per_ray": round(prof_c.node_fetches / max(prof_c.rays, 1), 2),
                          "tri_tests_per_ray": round(prof_c.tri_tests / max(prof_c.rays, 1), 2),
                          "profiled_pass_spp": pass_spp,
+                         "l2_copy_gbs": round(l2_gbs, 1),
+                         "frac_of_l2": round(achieved_gbs / l2_gbs, 4) if l2_gbs else None,
+                         "l2_note": "the traversal data (~10 MB) is L2-resident; l2_copy_gbs is a copy between "
+                                    "two 24 MB buffers measured here, the bound such a scene would meet",
                          "trace_ms_per_pass": round(prof_t.trace_ms, 3), "shade_ms_per_pass": round(prof_t.shade_ms, 3)},
             "cpu_baseline": cpu,
             "quality": quality,

@@ -254,8 +254,9 @@ __global__ void __launch_bounds__(128, 8) k_shadow(WaveBuffers w, RenderKnobs k,
     const float4 so = w.s_orig[i], sd = w.s_dir[i], sv = w.s_val[i];
     const int job = __float_as_int(so.w);
     const SceneView& sc = w.jobs[job].sc;
-    const HitRecord h = closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY, KIND != BVH_WIDE8>(
-        sc, v3(so.x, so.y, so.z), v3(sd.x, sd.y, sd.z), k.isect, stack, nullptr, sd.w);
+    const HitRecord h =
+        closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY, KIND != BVH_WIDE8, 0, KIND == BVH_WIDE4>(
+            sc, v3(so.x, so.y, so.z), v3(sd.x, sd.y, sd.z), k.isect, stack, nullptr, sd.w);
     if (h.geom == -1) {
       float4* c = w.contrib + __float_as_int(sv.w);
       const float4 v = *c;
@@ -419,7 +420,8 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
     // the binary layout is tested with the box arithmetic and traversal order of the
     // default trace kernel
     const HitRecord h =
-        closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY>(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), isect, stack);
+        closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY, false, 0, KIND == BVH_WIDE4>(
+            sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), isect, stack);
     illume_hit o;
     o.t = h.t;
     o.u = h.geom >= 0 ? h.u : 0.0f;
@@ -439,16 +441,16 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 //   variant 1 held to 64 registers; 3 = variant 0 with leaves tested where met; 4 =
 //   variant 0 with lane refill (k_trace_refill);
 //   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine;
-//   4-wide BVH: 0 = at most 64 registers (8 blocks of 128 per SM), traversal stack in
-//   local memory (the default); 1 = its first 8 entries in shared memory; 2 = near and
-//   far planes loaded by per-ray byte offsets; 3 = 6 blocks per SM (at most 80
-//   registers, no spills).
+//   4-wide BVH: 0 = at most 64 registers (8 blocks of 128 per SM), near and far planes
+//   loaded by per-ray byte offsets, traversal stack in local memory (the default); 1 =
+//   its first 8 stack entries in shared memory; 2 = lo and hi planes loaded and selected
+//   per child box; 3 = 6 blocks per SM (at most 80 registers, no spills).
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (bvh_kind == BVH_WIDE4) {
-    if (variant == 1) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, 8>;
-    if (variant == 2) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, 0, true>;
-    if (variant == 3) return (const void*)k_trace<BVH_WIDE4, false, 6, true>;
-    return (const void*)k_trace<BVH_WIDE4, false, 8, true>;
+    if (variant == 1) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, 8, true>;
+    if (variant == 2) return (const void*)k_trace<BVH_WIDE4, false, 8, true>;
+    if (variant == 3) return (const void*)k_trace<BVH_WIDE4, false, 6, true, false, 0, true>;
+    return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, 0, true>;
   }
   if (bvh_kind == BVH_WIDE8)
     return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
@@ -463,17 +465,17 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
                   bool count_visits) {
   if (k.bvh_kind == BVH_WIDE4) {
     if (k.trace_variant == 1) {
-      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
-      else k_trace<BVH_WIDE4, false, 8, true, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
     } else if (k.trace_variant == 2) {
-      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
-      else k_trace<BVH_WIDE4, false, 8, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
-    } else if (k.trace_variant == 3) {
-      if (count_visits) k_trace<BVH_WIDE4, true, 6, true><<<grid, 128, 0, st>>>(w, k, bounce);
-      else k_trace<BVH_WIDE4, false, 6, true><<<grid, 128, 0, st>>>(w, k, bounce);
-    } else {
       if (count_visits) k_trace<BVH_WIDE4, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE4, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    } else if (k.trace_variant == 3) {
+      if (count_visits) k_trace<BVH_WIDE4, true, 6, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 6, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    } else {
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
     }
     return;
   }

@@ -164,10 +164,10 @@ typedef struct {
                                * grid-stride rays, leaves tested where met; 2 = variant 1 held to 64
                                * registers; 3 = variant 0 with leaves tested where met; 4 = variant
                                * 0 with lane refill. 4-wide BVH: 0 = at most 64 registers,
-                               * traversal stack in local memory (default); 1 = its first 8
-                               * entries in shared memory; 2 = near and far planes loaded by
-                               * per-ray offsets; 3 = at most 80 registers. Other layouts
-                               * ignore it. */
+                               * near / far planes loaded by per-ray offsets, stack in local
+                               * memory (default); 1 = its first 8 stack entries in shared
+                               * memory; 2 = lo / hi planes selected per child box; 3 = at
+                               * most 80 registers. Other layouts ignore it. */
   int32_t shade_variant;      /* 0 = the measured best register bound (default), 1 = the
                                * compiler's choice, 2 / 3 / 4 = at most 80 / 72 / 64 registers */
   int32_t estimator;          /* illume_estimator */
