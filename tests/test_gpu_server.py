@@ -53,7 +53,7 @@ def test_same_alone_and_in_the_mix(ctx, scenes, bvh):
     jobs = job_list(scenes, bvh)
     ref = [alone(ctx, sc, p) for sc, p in jobs]
     variants = [{"trace_variant": v} for v in ((1, 2, 3, 4) if bvh == C.BVH_BINARY else (1, 2, 3))]
-    for opts in [{}, {"path_capacity": 40000}, {"passes_per_step": 4}] + variants:
+    for opts in [{}, {"path_capacity": 40000}, {"passes_per_step": 4}, {"lanes": 1}, {"lanes": 3}] + variants:
         srv = Server(ctx, **opts)
         ids = [srv.submit(sc, p) for sc, p in jobs]
         srv.run()
