@@ -109,16 +109,34 @@ __global__ void __launch_bounds__(1024) k_plan(WaveBuffers w) {
 
 // init_rays, src/renderer.cu:81-110, for path slot g of job row j: pid = g - path_base
 // = sample_in_pass * npix + pixel.
+// Pixel of queue position q (0 <= q < w * h) when a sample's camera rays are queued in
+// 8x4 tiles: the pixels of whole tiles first, tile after tile in row-major order (so a
+// warp's 32 rays cover a compact patch of the image and traverse alike), then the pixels
+// of the partial tiles at the right and bottom edges in row-major order.
+__device__ __forceinline__ int tiled_pixel(int q, int w, int h) {
+  const int tw = w >> 3, th = h >> 2;
+  const int full = tw * th * 32;
+  if (q < full) {
+    const int t = q >> 5, k = q & 31;
+    return ((t / tw) * 4 + (k >> 3)) * w + (t % tw) * 8 + (k & 7);
+  }
+  const int r = q - full, rw = w - tw * 8, right = th * 4 * rw;
+  if (r < right) return (r / rw) * w + tw * 8 + r % rw;
+  return th * 4 * w + (r - right);
+}
+
 __global__ void __launch_bounds__(256) k_raygen(WaveBuffers w) {
   const int total = w.counters[kCounterPaths];
-  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
-    const int j = find_row(w.job_path_base, w.njobs, g);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int j = find_row(w.job_path_base, w.njobs, i);
     const JobDesc& J = w.jobs[j];
-    const int pid = g - J.path_base;
     const int npix = J.npix;
-    const int pixel = pid % npix;
-    const int sample = J.sample_base + pid / npix;
+    const int s = (i - J.path_base) / npix;
     const CameraView& cam = J.cam;
+    // queue position i holds the path of this pixel; its slot g keys the radiance
+    const int pixel = tiled_pixel(i - J.path_base - s * npix, cam.width, cam.height);
+    const int g = J.path_base + s * npix + pixel;
+    const int sample = J.sample_base + s;
     RngStream rng;
     rng.init((uint32_t)pixel, (uint32_t)sample, 0u, J.seed, J.job);
     const int x = pixel % cam.width, y = pixel / cam.width;
@@ -134,9 +152,9 @@ __global__ void __launch_bounds__(256) k_raygen(WaveBuffers w) {
     const V3 origin = xform(cam.m, pos, 1.0f);
     const V3 image_pos = xform(cam.m, v3(r_x, r_y, cam.dof), 1.0f);
     const V3 dir = normalize(sub(image_pos, origin));
-    w.q_orig[0][g] = make_float4(origin.x, origin.y, origin.z, __int_as_float(g));
-    w.q_dir[0][g] = make_float4(dir.x, dir.y, dir.z, pack_job_medium(j, -1));
-    w.q_thr[0][g] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    w.q_orig[0][i] = make_float4(origin.x, origin.y, origin.z, __int_as_float(g));
+    w.q_dir[0][i] = make_float4(dir.x, dir.y, dir.z, pack_job_medium(j, -1));
+    w.q_thr[0][i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     w.contrib[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
 }
