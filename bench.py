@@ -139,30 +139,6 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def l2_gbs(dev):
-    """Bandwidth of L2-resident data, CUDA events: a copy between two 16 MB buffers (read +
-    write bytes) and a sum over a 32 MB buffer (read bytes); the larger of the two."""
-    import torch
-    a = torch.ones(4 << 20, dtype=torch.float32, device=f"cuda:{dev}")
-    b = torch.empty_like(a)
-    c = torch.ones(8 << 20, dtype=torch.float32, device=f"cuda:{dev}")
-    out = torch.empty((), dtype=torch.float32, device=f"cuda:{dev}")
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    best = 0.0
-    for op, nbytes in ((lambda: b.copy_(a), 2 * a.numel() * 4), (lambda: torch.sum(c, out=out), c.numel() * 4)):
-        for _ in range(20):
-            op()
-        n = 400
-        torch.cuda.synchronize()
-        e0.record()
-        for _ in range(n):
-            op()
-        e1.record()
-        torch.cuda.synchronize()
-        best = max(best, nbytes * n / (e0.elapsed_time(e1) * 1e-3) / 1e9)
-    return best
-
-
 def measured_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -344,7 +320,9 @@ def run_ours(args):
     achieved_gbs = trace_bytes / (prof_t.trace_ms * 1e-3) / 1e9
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
-    l2_peak = l2_gbs(dev)
+    l2_peak = ctypes.c_double(0.0)
+    C.check(C.lib().illume_measure_l2_read(ctx.handle, 32 << 20, 200, ctypes.byref(l2_peak)))
+    l2_peak = l2_peak.value
     # DRAM traffic of the trace kernel per launch: bytes per ray from the committed ncu
     # summary, times this workload's rays per trace launch
     traffic = None
@@ -410,8 +388,8 @@ def run_ours(args):
                          "profiled_pass_spp": pass_spp,
                          "l2_gbs": round(l2_peak, 1),
                          "frac_of_l2": round(achieved_gbs / l2_peak, 4) if l2_peak else None,
-                         "l2_note": "the traversal data (~10 MB) is L2-resident; l2_gbs is measured here on "
-                                    "L2-resident buffers (16 MB copy, 32 MB sum), the larger",
+                         "l2_note": "the traversal data (~10 MB) is L2-resident; l2_gbs is the read bandwidth "
+                                    "of a 32 MB buffer swept 200 times by illume_measure_l2_read, here",
                          "trace_ms_per_pass": round(prof_t.trace_ms, 3), "shade_ms_per_pass": round(prof_t.shade_ms, 3)},
             "cpu_baseline": cpu,
             "quality": quality,

@@ -167,6 +167,7 @@ PROTOTYPES = {
     "illume_server_get_stats": (c_int, [c_void_p, POINTER(ServerStats)]),
     "illume_plan_pass_shares": (c_int, [c_int, _pi32, _pi32, c_int64, _pi32]),
     "illume_alias_table": (c_int, [c_int, POINTER(c_double), _pf, _pi32]),
+    "illume_measure_l2_read": (c_int, [c_void_p, c_size_t, c_int, POINTER(c_double)]),
     "illume_render_batch": (c_int, [c_void_p, c_int, POINTER(c_void_p), POINTER(RenderParams), POINTER(_pf),
                                     POINTER(POINTER(c_uint8)), POINTER(RenderStats), c_int, POINTER(ServerStats)]),
 }

@@ -352,6 +352,35 @@ int illume_trace_closest(illume_context* ctx, illume_scene* scene, const float* 
   return ILLUME_OK;
 }
 
+int illume_measure_l2_read(illume_context* ctx, size_t bytes, int reps, double* gbs) {
+  CHECK_ARG(ctx && gbs && bytes >= 16 && reps >= 1, "invalid argument");
+  cudaSetDevice(ctx->c.device);
+  bytes &= ~(size_t)15;
+  DevBuffer buf, sink;
+  int st;
+  if ((st = buf.alloc(&ctx->c, bytes)) != ILLUME_OK) return st;
+  if ((st = sink.alloc(&ctx->c, sizeof(unsigned))) != ILLUME_OK) return st;
+  cudaStream_t s = ctx->c.stream;
+  ILLUME_CUDA_TRY(cudaMemsetAsync(buf.get(), 1, bytes, s));
+  const int grid = kernel_grid_blocks(l2_read_kernel_ptr(), 256, ctx->c.device);
+  launch_l2_read(buf.get(), bytes, 2, sink.as<unsigned>(), grid, s);   // warm L2
+  cudaEvent_t e0, e1;
+  ILLUME_CUDA_TRY(cudaEventCreate(&e0));
+  ILLUME_CUDA_TRY(cudaEventCreate(&e1));
+  cudaEventRecord(e0, s);
+  launch_l2_read(buf.get(), bytes, reps, sink.as<unsigned>(), grid, s);
+  cudaEventRecord(e1, s);
+  const cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ILLUME_CUDA_TRY(e);
+  ILLUME_CUDA_TRY(cudaGetLastError());
+  *gbs = ms > 0.0f ? (double)bytes * reps / (ms * 1e-3) / 1e9 : 0.0;
+  return ILLUME_OK;
+}
+
 int illume_alias_table(int n, const double* weights, float* keep, int32_t* alias) {
   CHECK_ARG(n >= 0 && (n == 0 || (weights && keep && alias)), "null argument");
   std::vector<AliasEntry> t(n);

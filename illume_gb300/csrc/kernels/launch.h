@@ -122,6 +122,9 @@ void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float
 void launch_bsdf_batch(int type, int distribution, const float* in, int n, float* out, cudaStream_t st);
 
 const void* trace_kernel_ptr(int bvh_kind, int variant = 0);
+// L2 read-bandwidth probe (measurement only).
+void launch_l2_read(const void* buf, size_t bytes, int reps, unsigned* sink, int grid, cudaStream_t st);
+const void* l2_read_kernel_ptr();
 const void* shade_kernel_ptr(int variant = 0, bool nee = false);
 const void* shadow_kernel_ptr(int bvh_kind);
 

@@ -19,7 +19,6 @@ namespace illume {
 
 static constexpr float kExitSlack = 1.000001f;  // ~8 ulp widening of box exit distances
 static constexpr int kStack = 64;
-static constexpr int kTraceBlock = 128;   // threads per block of the trace kernels
 // Upper bound on node fetches of one ray in one mesh: a well-formed tree never comes
 // close (each node is fetched at most once per ray); it only bounds the loop.
 static constexpr int kMaxNodeVisits = 1 << 22;
@@ -307,32 +306,24 @@ __device__ __forceinline__ void sort_pair(float& ka, int& ea, float& kb, int& eb
 // children (inner or leaf) ordered by entry distance with a 5-comparator network; the
 // nearest becomes the next entry and the others are pushed farthest first. Leaves are
 // set aside and tested warp-together as in ww_round; triangles are the binary layout's.
-// SH > 0: the first SH stack entries live in shared memory (sh points at this thread's
-// column of a [SH][kTraceBlock] array: one bank per lane, no conflicts, never evicted by
-// node fetches), deeper entries in the local array.
 // NF: each ray loads its near and far planes straight from their byte offsets in the
 // node (chosen once per ray by the direction's signs and OR-ed into the 128-byte-aligned
 // node address) instead of loading lo and hi and selecting per child box; the box test
 // arithmetic is the same, so are the results.
-template <bool COUNT, bool ANY = false, int SH = 0, bool NF = false>
+// PS: four compare-swaps instead of five: the nearest child is exact, the middle two of
+// the pushed ones may come out of order (order changes the work, never the result).
+template <bool COUNT, bool ANY = false, bool PS = false, bool NF = false>
 __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
-                                                 int* stack, VisitCount& vc, int* sh = nullptr) {
+                                                 int* stack, VisitCount& vc) {
   constexpr int kEmpty = kEmptyEntry;
   int sp = 0, cur = 0, leaf = kEmpty, visits = 0;
   // near-plane offsets in a Bvh4Node: lox/loy/loz at 0/16/32, hix/hiy/hiz at 48/64/80
   const unsigned near_x = r.idir.x >= 0.0f ? 0u : 48u, near_y = r.idir.y >= 0.0f ? 16u : 64u,
                  near_z = r.idir.z >= 0.0f ? 32u : 80u;
   auto push = [&](int v) {
-    if (sp < kStack) {
-      if (SH > 0 && sp < SH) sh[sp * kTraceBlock] = v;
-      else stack[sp - SH] = v;
-      ++sp;
-    }
+    if (sp < kStack) stack[sp++] = v;
   };
-  auto pop = [&]() -> int {
-    --sp;
-    return (SH > 0 && sp < SH) ? sh[sp * kTraceBlock] : stack[sp - SH];
-  };
+  auto pop = [&]() -> int { return stack[--sp]; };
   do {
     while (cur >= 0) {
       if (COUNT) vc.nodes++;
@@ -362,7 +353,7 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
       sort_pair(k2, e2, k3, e3);
       sort_pair(k0, e0, k2, e2);
       sort_pair(k1, e1, k3, e3);
-      sort_pair(k1, e1, k2, e2);
+      if (!PS) sort_pair(k1, e1, k2, e2);
       if (e3 != kEmpty) push(e3);
       if (e2 != kEmpty) push(e2);
       if (e1 != kEmpty) push(e1);
@@ -571,12 +562,11 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 // Full closest-hit query for a world-space ray (direction used as given).
 // tmax: only hits closer than tmax count (shadow rays). ANY: return at the first hit
 // found closer than tmax (occlusion; with the binary and 4-wide layouts).
-// SH: shared-memory stack entries of the 4-wide traversal (sh_stack: this thread's column).
-template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false, bool ANY = false, int SH = 0,
+// PS, NF: options of the 4-wide traversal (traverse_bvh4_ww).
+template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false, bool ANY = false, bool PS = false,
           bool NF = false>
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
-                                                 VisitCount* vcp = nullptr, float tmax = FLT_MAX,
-                                                 int* sh_stack = nullptr) {
+                                                 VisitCount* vcp = nullptr, float tmax = FLT_MAX) {
   VisitCount vc;
   HitRecord h;
   h.t = tmax; h.u = 0.0f; h.v = 0.0f; h.prim = -1; h.geom = -1;
@@ -608,7 +598,7 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     MeshBest b{h.t, -1, 0.0f, 0.0f};
     const DevMesh& m = sc.meshes[in.mesh];
     if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);
-    else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT, ANY, SH, NF>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc, sh_stack);
+    else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT, ANY, PS, NF>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else if (WW) traverse_bvh2_ww<COUNT, FMA, ANY>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else traverse_bvh2<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }

@@ -43,10 +43,9 @@ __device__ __forceinline__ int event_class(const WaveBuffers& w, const JobDesc& 
 // OPT: box tests in fused multiply-add form, and warps take their next 32 rays from a
 // shared counter (counters[44 + parity]) instead of a fixed grid stride, so that warps
 // whose rays finish early take over the remaining work.
-// SH (4-wide only): stack entries kept in shared memory.
-template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false, int SH = 0, bool NF = false>
-__global__ void __launch_bounds__(kTraceBlock, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
-  __shared__ int sh_stack[SH > 0 ? SH * kTraceBlock : 1];
+// PS, NF (4-wide only): see traverse_bvh4_ww.
+template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false, bool PS = false, bool NF = false>
+__global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
   const int parity = bounce & 1;
   const int n = w.counters[parity];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -78,8 +77,8 @@ __global__ void __launch_bounds__(kTraceBlock, MINB) k_trace(WaveBuffers w, Rend
     const SceneView& sc = J.sc;
     VisitCount vc;
     const HitRecord h =
-        closest_hit<KIND, COUNT, OPT, WW, false, SH, NF>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack,
-                                                     &vc, FLT_MAX, sh_stack + threadIdx.x);
+        closest_hit<KIND, COUNT, OPT, WW, false, PS, NF>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack,
+                                                     &vc);
     if (COUNT) { my_nodes += vc.nodes; my_tris += vc.tris; }
     const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
     w.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
@@ -255,7 +254,7 @@ __global__ void __launch_bounds__(128, 8) k_shadow(WaveBuffers w, RenderKnobs k,
     const int job = __float_as_int(so.w);
     const SceneView& sc = w.jobs[job].sc;
     const HitRecord h =
-        closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY, KIND != BVH_WIDE8, 0, KIND == BVH_WIDE4>(
+        closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY, KIND != BVH_WIDE8, false, KIND == BVH_WIDE4>(
             sc, v3(so.x, so.y, so.z), v3(sd.x, sd.y, sd.z), k.isect, stack, nullptr, sd.w);
     if (h.geom == -1) {
       float4* c = w.contrib + __float_as_int(sv.w);
@@ -420,7 +419,7 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
     // the binary layout is tested with the box arithmetic and traversal order of the
     // default trace kernel
     const HitRecord h =
-        closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY, false, 0, KIND == BVH_WIDE4>(
+        closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY, false, false, KIND == BVH_WIDE4>(
             sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), isect, stack);
     illume_hit o;
     o.t = h.t;
@@ -443,14 +442,14 @@ __global__ void __launch_bounds__(128) k_trace_hook(SceneView sc, const float4* 
 //   8-wide BVH: 0 = one ray per lane to completion, 1 = persistent state machine;
 //   4-wide BVH: 0 = at most 64 registers (8 blocks of 128 per SM), near and far planes
 //   loaded by per-ray byte offsets, traversal stack in local memory (the default); 1 =
-//   its first 8 stack entries in shared memory; 2 = lo and hi planes loaded and selected
-//   per child box; 3 = 6 blocks per SM (at most 80 registers, no spills).
+//   four compare-swaps instead of five in the child ordering; 2 = lo and hi planes
+//   loaded and selected per child box; 3 = 6 blocks per SM (at most 80 registers).
 const void* trace_kernel_ptr(int bvh_kind, int variant) {
   if (bvh_kind == BVH_WIDE4) {
-    if (variant == 1) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, 8, true>;
+    if (variant == 1) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, true, true>;
     if (variant == 2) return (const void*)k_trace<BVH_WIDE4, false, 8, true>;
-    if (variant == 3) return (const void*)k_trace<BVH_WIDE4, false, 6, true, false, 0, true>;
-    return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, 0, true>;
+    if (variant == 3) return (const void*)k_trace<BVH_WIDE4, false, 6, true, false, false, true>;
+    return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true>;
   }
   if (bvh_kind == BVH_WIDE8)
     return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
@@ -465,17 +464,17 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
                   bool count_visits) {
   if (k.bvh_kind == BVH_WIDE4) {
     if (k.trace_variant == 1) {
-      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
-      else k_trace<BVH_WIDE4, false, 8, true, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true, false, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
     } else if (k.trace_variant == 2) {
       if (count_visits) k_trace<BVH_WIDE4, true, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE4, false, 8, true><<<grid, 128, 0, st>>>(w, k, bounce);
     } else if (k.trace_variant == 3) {
-      if (count_visits) k_trace<BVH_WIDE4, true, 6, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
-      else k_trace<BVH_WIDE4, false, 6, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      if (count_visits) k_trace<BVH_WIDE4, true, 6, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 6, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
     } else {
-      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
-      else k_trace<BVH_WIDE4, false, 8, true, false, 0, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
     }
     return;
   }
@@ -547,6 +546,25 @@ void launch_trace_hook(const SceneView& sc, const SceneView* d_view, const float
   else
     k_trace_hook<BVH_BINARY><<<grid, 128, 0, st>>>(sc, (const float4*)rays8, n, isect, (illume_hit*)hits);
 }
+
+// Read bandwidth of data that stays in L2: a grid-stride sweep of the buffer with
+// 16-byte loads that skip L1, `reps` times, XOR-folded so the loads are kept.
+__global__ void __launch_bounds__(256) k_l2_read(const uint4* buf, size_t n16, int reps, unsigned* sink) {
+  unsigned acc = 0;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < reps; ++r)
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) {
+      const uint4 v = __ldcg(buf + i);
+      acc ^= v.x ^ v.y ^ v.z ^ v.w;
+    }
+  if (acc == 0x9e3779b9u) atomicAdd(sink, 1u);
+}
+
+void launch_l2_read(const void* buf, size_t bytes, int reps, unsigned* sink, int grid, cudaStream_t st) {
+  k_l2_read<<<grid, 256, 0, st>>>(reinterpret_cast<const uint4*>(buf), bytes / 16, reps, sink);
+}
+
+const void* l2_read_kernel_ptr() { return (const void*)k_l2_read; }
 
 int kernel_grid_blocks(const void* fn, int block, int device) {
   int sms = 0, per_sm = 0;

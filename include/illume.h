@@ -165,9 +165,9 @@ typedef struct {
                                * registers; 3 = variant 0 with leaves tested where met; 4 = variant
                                * 0 with lane refill. 4-wide BVH: 0 = at most 64 registers,
                                * near / far planes loaded by per-ray offsets, stack in local
-                               * memory (default); 1 = its first 8 stack entries in shared
-                               * memory; 2 = lo / hi planes selected per child box; 3 = at
-                               * most 80 registers. Other layouts ignore it. */
+                               * memory (default); 1 = four compare-swaps instead of five in
+                               * the child ordering; 2 = lo / hi planes selected per child
+                               * box; 3 = at most 80 registers. Other layouts ignore it. */
   int32_t shade_variant;      /* 0 = the measured best register bound (default), 1 = the
                                * compiler's choice, 2 / 3 / 4 = at most 80 / 72 / 64 registers */
   int32_t estimator;          /* illume_estimator */
@@ -374,6 +374,12 @@ int illume_plan_pass_shares(int n, const int32_t* npix, const int32_t* left, int
  * the fraction of u n is below keep[i] and becomes alias[i] otherwise, so that i comes
  * out with probability weights[i] / sum. ILLUME_ERR_INVALID when the weights sum to 0. */
 int illume_alias_table(int n, const double* weights, float* keep, int32_t* alias);
+
+/* Read bandwidth (GB/s) of a `bytes` buffer the device's L2 holds, swept `reps` times by
+ * a grid-stride kernel with 16-byte loads that bypass L1 (measurement hook for the
+ * traversal roofline, whose node and triangle data stay in L2; no counterpart in the
+ * reference). Allocates and frees the buffer itself. */
+int illume_measure_l2_read(illume_context* ctx, size_t bytes, int reps, double* gbs);
 
 /* Renders n jobs together through one server (all submitted at once) and returns each
  * job's mean radiance (3 floats per pixel) and RGB8 in the nullable per-job buffers.
