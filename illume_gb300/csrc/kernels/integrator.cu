@@ -428,6 +428,7 @@ __global__ void __launch_bounds__(256) k_accumulate(WaveBuffers w) {
     const int p = x - J.pixel_base;
     const int ns = J.nsamples, npix = J.npix, mode = J.accum_mode, path_base = J.path_base;
     const Accumulators acc = J.acc;
+    const bool squares = acc.sumsq != nullptr;   // FP64 work only where it is kept
     float s32[3], c32[3];
     double s64[3], q64[3];
     for (int c = 0; c < 3; ++c) {
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(256) k_accumulate(WaveBuffers w) {
         } else {
           s64[c] += (double)l[c];
         }
-        q64[c] += (double)l[c] * (double)l[c];
+        if (squares) q64[c] += (double)l[c] * (double)l[c];
       }
     }
     for (int c = 0; c < 3; ++c) {
