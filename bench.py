@@ -385,6 +385,7 @@ def run_ours(args):
                          "traffic_source": "profiles/trace_traffic.txt (ncu DRAM bytes per ray x rays per launch)",
                          "node_fetches_per_ray": round(prof_c.node_fetches / max(prof_c.rays, 1), 2),
                          "tri_tests_per_ray": round(prof_c.tri_tests / max(prof_c.rays, 1), 2),
+                         "node_fetch_lane_utilisation": round(prof_c.node_fetches / max(prof_c.lane_slots, 1), 3),
                          "profiled_pass_spp": pass_spp,
                          "l2_gbs": round(l2_peak, 1),
                          "frac_of_l2": round(achieved_gbs / l2_peak, 4) if l2_peak else None,

@@ -94,7 +94,8 @@ class Profile(ctypes.Structure):
     """illume_profile"""
     _fields_ = [("raygen_ms", c_double), ("trace_ms", c_double), ("shade_ms", c_double), ("accumulate_ms", c_double),
                 ("trace_launches", c_int64), ("shade_launches", c_int64), ("rays", c_int64),
-                ("node_fetches", c_int64), ("tri_tests", c_int64), ("node_bytes", c_int64), ("tri_bytes", c_int64)]
+                ("node_fetches", c_int64), ("tri_tests", c_int64), ("node_bytes", c_int64), ("tri_bytes", c_int64),
+                ("lane_slots", c_int64)]
 
 
 class ServerStats(ctypes.Structure):

@@ -104,7 +104,7 @@ int Engine::init(Context* c, int nrows, int ncap, const RenderKnobs& k, std::str
 #define ALLOC(buf, bytes) if ((st = (buf).alloc(ctx, (bytes))) != ILLUME_OK) { *err = last_error(); return st; }
   ALLOC(counters, sizeof(int) * kCounterWords);
   ALLOC(rays, sizeof(unsigned long long));
-  ALLOC(visits, 2 * sizeof(unsigned long long));
+  ALLOC(visits, 3 * sizeof(unsigned long long));
   ALLOC(jobs, sizeof(JobDesc) * (size_t)rows);
   ALLOC(path_base, sizeof(int) * (size_t)(rows + 1));
   ALLOC(pixel_base, sizeof(int) * (size_t)(rows + 1));

@@ -224,10 +224,10 @@ int Renderer::profile(bool count_visits, illume_profile* out) {
     for (auto& e : ev) if (e) cudaEventDestroy(e);
     return ps;
   }
-  unsigned long long vis[2] = {0, 0};
+  unsigned long long vis[3] = {0, 0, 0};
   ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_after, reinterpret_cast<const char*>(eng.w.jobs) + offsetof(JobDesc, rays), 8,
                                   cudaMemcpyDeviceToHost, st));
-  ILLUME_CUDA_TRY(cudaMemcpyAsync(vis, eng.visits.get(), 16, cudaMemcpyDeviceToHost, st));
+  ILLUME_CUDA_TRY(cudaMemcpyAsync(vis, eng.visits.get(), sizeof(vis), cudaMemcpyDeviceToHost, st));
   ILLUME_CUDA_TRY(cudaStreamSynchronize(st));
   auto ms = [&](int a, int b) {
     float x = 0.0f;
@@ -245,6 +245,7 @@ int Renderer::profile(bool count_visits, illume_profile* out) {
   out->rays = (int64_t)(rays_after - rays_before);
   out->node_fetches = (int64_t)vis[0];
   out->tri_tests = (int64_t)vis[1];
+  out->lane_slots = (int64_t)vis[2];
   out->node_bytes = eng.knobs.bvh_kind == BVH_WIDE8 ? (int64_t)sizeof(WideNode)
                     : eng.knobs.bvh_kind == BVH_WIDE4 ? (int64_t)sizeof(Bvh4Node) : (int64_t)sizeof(Bvh2Node);
   out->tri_bytes = 3 * (int64_t)sizeof(float4);

@@ -77,7 +77,7 @@ struct WaveBuffers {
   float4* s_dir;         //   direction, maximum distance
   float4* s_val;         //   contribution if unoccluded, path slot (int bits)
   unsigned long long* rays;   // closest-hit queries traced (running total)
-  unsigned long long* visits; // [node fetches, triangle tests] of the instrumented trace kernel
+  unsigned long long* visits; // [node fetches, triangle tests, warp node-fetch slots] of the instrumented trace kernel
   JobDesc* jobs;
   int* job_path_base;    // njobs + 1 prefix sums of the pass's paths (k_plan)
   int* job_pixel_base;   // njobs + 1 prefix sums of the pass's pixels (k_plan)

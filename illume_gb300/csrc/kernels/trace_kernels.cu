@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
   int* fetch = w.counters + 44 + parity;
   const int lane = threadIdx.x & 31;
   typename std::conditional<KIND == BVH_WIDE8, uint2, int>::type stack[kStack];
-  unsigned long long my_nodes = 0, my_tris = 0;
+  unsigned long long my_nodes = 0, my_tris = 0, my_slots = 0;
   int base = OPT ? 0 : blockIdx.x * blockDim.x + (threadIdx.x & ~31);
   for (;;) {
     if (OPT) {
@@ -79,7 +79,13 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
     const HitRecord h =
         closest_hit<KIND, COUNT, OPT, WW, false, PS, NF>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack,
                                                      &vc);
-    if (COUNT) { my_nodes += vc.nodes; my_tris += vc.tris; }
+    if (COUNT) {
+      my_nodes += vc.nodes;
+      my_tris += vc.tris;
+      // node-fetch slots the warp spends on this batch: 32 lanes x its longest ray
+      const unsigned longest = __reduce_max_sync(mask, (unsigned)vc.nodes);
+      if (lane == __ffs(mask) - 1) my_slots += 32ull * longest;
+    }
     const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
     w.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
     w.hit_geom[i] = h.geom;
@@ -90,10 +96,12 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
     for (int off = 16; off > 0; off >>= 1) {
       my_nodes += __shfl_down_sync(0xffffffffu, my_nodes, off);
       my_tris += __shfl_down_sync(0xffffffffu, my_tris, off);
+      my_slots += __shfl_down_sync(0xffffffffu, my_slots, off);
     }
     if ((threadIdx.x & 31) == 0) {
       atomicAdd(w.visits, my_nodes);
       atomicAdd(w.visits + 1, my_tris);
+      atomicAdd(w.visits + 2, my_slots);
     }
   }
 }

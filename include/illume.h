@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define ILLUME_ABI_VERSION 1
+#define ILLUME_ABI_VERSION 2
 
 enum illume_status {
   ILLUME_OK = 0,
@@ -269,6 +269,9 @@ typedef struct {
   int64_t rays;
   int64_t node_fetches, tri_tests;   /* count_visits only */
   int64_t node_bytes, tri_bytes;     /* bytes of one node / one triangle record in the BVH used */
+  int64_t lane_slots;                /* count_visits only: sum over the trace kernel's 32-ray warp
+                                      * batches of 32 x the batch's most node fetches
+                                      * (node_fetches / lane_slots = lane utilisation) */
 } illume_profile;
 int illume_renderer_profile(illume_renderer* r, int count_visits, illume_profile* out);
 
