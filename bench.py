@@ -4,9 +4,9 @@
 Workload (the configuration the headline metric is quoted on): displaced icosphere of
 ~100k triangles (rough gold conductor, GGX alpha 0.2) over a checkerboard ground quad,
 2048x1024 HDR environment map with a sun lobe, 1024x1024 pixels, max depth 25, seeded
-synthetic data. One step = `--spp-per-step` samples of every pixel (32 by default, 33.5M
-paths), rendered as two passes of 16 samples on two engines that take turns, so that one
-pass's last bounces overlap the next pass's first; a full 1024-spp render is 32 such steps.
+synthetic data. One step = `--spp-per-step` samples of every pixel (64 by default, 67M
+paths), rendered as four passes of 16 samples on four engines that take turns, so that
+one pass's last bounces overlap the next passes; a full 1024-spp render is 16 such steps.
 
 * value: rays traced (closest-hit queries, counted as the reference counts them) per
   second of device time, inputs resident in HBM, L2 flushed between timed steps.
@@ -47,11 +47,11 @@ WORKLOAD = "triangle-heavy traversal: displaced icosphere 100k tris, GGX rough g
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=32)
+    ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--bvh", default="wide4", choices=["wide4", "binary", "wide", "wide-persistent"])
-    ap.add_argument("--spp-per-step", type=int, default=32)
+    ap.add_argument("--spp-per-step", type=int, default=64)
     ap.add_argument("--trace-variant", type=int, default=0,
                     help="binary traversal: 0 64 registers + fused box tests + dynamic ray fetch + while-while "
                          "(default), 1 compiler register choice, 2 variant 1 held to 64 registers, 3 variant 0 with "
@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--shade-variant", type=int, default=0,
                     help="shade kernel: 0 measured best register bound (default), 1 compiler's choice, "
                          "2 / 3 / 4 at most 80 / 72 / 64 registers")
+    ap.add_argument("--engines", type=int, default=0,
+                    help="engines taking turns on a step's passes (0: the library's choice)")
     ap.add_argument("--tris", type=int, default=100_000)
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--depth", type=int, default=25)
@@ -78,6 +80,8 @@ def parse():
     ap.add_argument("--plain-1spp", action="store_true",
                     help="batched: also time one job at a time with one sample per pass")
     ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--lanes", type=int, default=0,
+                    help="served: job tables per kernel setting (0: the library's default)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -244,6 +248,7 @@ def run_ours(args):
     p.estimator = C.ESTIMATOR_NEE if args.estimator == "nee" else C.ESTIMATOR_REFERENCE
     p.trace_variant = args.trace_variant
     p.shade_variant = args.shade_variant
+    p.engines = args.engines
     r = Renderer(ctx, scene, params=p)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")   # > 129 MB L2
 
@@ -304,10 +309,14 @@ def run_ours(args):
                    "rel_rmse_vs_fp64_oracle": float(np.sqrt(np.mean((gm - om) ** 2)) / max(float(np.mean(np.abs(om))), 1e-12)),
                    "max_rel_err": float(np.max(np.abs(gm - om) / np.maximum(np.abs(om), 1e-6))),
                    "oracle_s": round(time.perf_counter() - t0q, 1)}
-    # the renderer splits a step over two engines when each half-pass keeps >= 2M paths
+    # the renderer splits a step over its engines (by default two when each half-pass
+    # keeps >= 2M paths)
     npix_all = args.res * args.res
-    pass_spp = ((args.spp_per_step + 1) // 2 if args.spp_per_step >= 2 and args.spp_per_step * npix_all >= (1 << 22)
-                else args.spp_per_step)
+    step_paths = args.spp_per_step * npix_all
+    n_eng = args.engines if args.engines > 0 else (max(2, min(4, step_paths >> 24)) if args.spp_per_step >= 2 and
+                                                   step_paths >= (1 << 22) else 1)
+    n_eng = max(1, min(n_eng, args.spp_per_step))
+    pass_spp = (args.spp_per_step + n_eng - 1) // n_eng
     # roofline of the trace kernel: counts from an instrumented pass, time from a plain pass
     # (one pass of one engine, kernels launched one by one)
     prof_t = C.Profile()
@@ -370,8 +379,8 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "mode": "plain wavefront" + (", passes of %d samples on two engines taking "
-                       "turns" % pass_spp if pass_spp < args.spp_per_step else ""), "bvh": args.bvh, "intersector": "watertight",
+            "config": {"workload": WORKLOAD, "mode": "plain wavefront" + (", passes of %d samples on %d engines taking "
+                       "turns" % (pass_spp, n_eng) if n_eng > 1 else ""), "bvh": args.bvh, "intersector": "watertight",
                        "estimator": args.estimator, "trace_variant": args.trace_variant,
                        "spp_per_step": args.spp_per_step, "paths_per_step": npix * args.spp_per_step,
                        "triangles": sd.num_triangles(), "resolution": [args.res, args.res], "max_depth": args.depth,
@@ -552,7 +561,8 @@ def run_served(args):
         return float(np.percentile(np.asarray(xs), q))
 
     # served arm
-    srv = Server(ctx, hbm_budget_bytes=150 << 30, max_jobs_in_flight=64, autotune=int(args.autotune))
+    opts = {"lanes": args.lanes} if args.lanes > 0 else {}
+    srv = Server(ctx, hbm_budget_bytes=150 << 30, max_jobs_in_flight=64, autotune=int(args.autotune), **opts)
     warm = srv.submit(scenes[0], _job_params(scenes[0], dict(width=64, height=64, spp=4, max_depth=4, job=999), C))
     srv.run()
     srv.poll(warm)

@@ -41,6 +41,7 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if (p.accum_mode < ACCUM_FP32 || p.accum_mode > ACCUM_FP64) { *err = "unknown accumulation mode"; return ILLUME_ERR_INVALID; }
   if (p.samples_per_pass < 0) { *err = "negative samples per pass"; return ILLUME_ERR_INVALID; }
   if (p.shade_variant < 0 || p.shade_variant > 4) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
+  if (p.engines < 0 || p.engines > 16) { *err = "engines out of range (0-16)"; return ILLUME_ERR_INVALID; }
   if (p.estimator < ILLUME_ESTIMATOR_REFERENCE || p.estimator > ILLUME_ESTIMATOR_NEE) { *err = "unknown estimator"; return ILLUME_ERR_INVALID; }
   if ((int)scene.t_mediums.size() > kMaxMediums) { *err = "too many mediums"; return ILLUME_ERR_UNSUPPORTED; }
   if (!scene.ctx || !scene.view_dev) { *err = "scene has not been uploaded to a device"; return ILLUME_ERR_INVALID; }
@@ -74,16 +75,20 @@ JobDesc job_row(const Scene& scene, const illume_render_params& p, const Accumul
 }
 
 Renderer::~Renderer() {
-  if (stream2) cudaStreamSynchronize(stream2);
+  for (cudaStream_t s : more_streams) cudaStreamSynchronize(s);
   if (ev0) cudaEventDestroy(ev0);
   if (ev1) cudaEventDestroy(ev1);
-  for (cudaEvent_t e : {acc_ev[0], acc_ev[1], join_ev})
+  for (cudaEvent_t e : acc_ev)
     if (e) cudaEventDestroy(e);
-  if (stream2) cudaStreamDestroy(stream2);
+  for (cudaEvent_t e : join_ev)
+    if (e) cudaEventDestroy(e);
+  more.clear();   // the extra engines' buffers before their streams
+  for (cudaStream_t s : more_streams) cudaStreamDestroy(s);
 }
 
 size_t Renderer::device_bytes() const {
-  size_t b = eng.device_bytes() + (split ? eng2.device_bytes() : 0);
+  size_t b = eng.device_bytes();
+  for (const auto& e : more) b += e->device_bytes();
   const DevBuffer* all[] = {&sum32, &comp32, &sum64, &sumsq, &out_mean, &out_rgb8};
   for (const DevBuffer* d : all) b += d->size();
   return b;
@@ -96,9 +101,14 @@ int Renderer::init(std::string* err) {
   const long long target = 1LL << 22;  // paths in flight per pass
   per_pass = p.samples_per_pass > 0 ? p.samples_per_pass : (int)std::max(1LL, std::min<long long>(std::max(p.spp, 1), target / npix));
   if ((long long)per_pass * npix > (1LL << 30)) { *err = "too many paths per pass"; return ILLUME_ERR_INVALID; }
-  // two engines taking turns when each half still fills the GPU (2M paths)
-  split = per_pass >= 2 && (long long)per_pass * npix >= (1LL << 22);
-  if (split) per_pass = (per_pass + 1) / 2;
+  // engines taking turns: by default, for a pass of 4M paths or more, one per 16M paths
+  // of the pass, at least two and at most four; p.engines asks for a number (1 = never)
+  const long long pass_paths = (long long)per_pass * npix;
+  nengines = p.engines > 0 ? p.engines
+                           : (per_pass >= 2 && pass_paths >= (1LL << 22)
+                                  ? (int)std::max(2LL, std::min(4LL, pass_paths >> 24)) : 1);
+  nengines = std::max(1, std::min(nengines, per_pass));
+  per_pass = (per_pass + nengines - 1) / nengines;
 #define ALLOC(buf, bytes) if ((st = (buf).alloc(ctx, (bytes))) != ILLUME_OK) { *err = last_error(); return st; }
   if (p.accum_mode == ACCUM_FP64) { ALLOC(sum64, sizeof(double) * 3 * (size_t)npix); }
   else { ALLOC(sum32, sizeof(float) * 3 * (size_t)npix); }
@@ -111,19 +121,28 @@ int Renderer::init(std::string* err) {
   acc.sumsq = sumsq.as<double>();
   if ((st = eng.init(ctx, 1, per_pass * npix, render_knobs(p), err)) != ILLUME_OK) return st;
   JobDesc row = job_row(*scene, p, acc);
-  if (split) row.flags |= 2 << kInterleaveShift;
+  if (nengines > 1) row.flags |= nengines << kInterleaveShift;
   eng.mirror[0] = row;
   p.camera = nullptr;   // read once; the caller's array need not outlive this call
   if ((st = eng.write_row(0)) != ILLUME_OK) { *err = last_error(); return st; }
-  if (split) {
-    ILLUME_CUDA_TRY(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
-    eng2.stream = stream2;
-    if ((st = eng2.init(ctx, 1, per_pass * npix, render_knobs(p), err)) != ILLUME_OK) return st;
-    eng2.mirror[0] = row;
-    if ((st = eng2.write_row(0)) != ILLUME_OK) { *err = last_error(); return st; }
-    for (cudaEvent_t* e : {&acc_ev[0], &acc_ev[1], &join_ev})
-      ILLUME_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-    ILLUME_CUDA_TRY(cudaStreamSynchronize(stream2));
+  if (nengines > 1) {
+    acc_ev.assign(nengines, nullptr);
+    for (cudaEvent_t& e : acc_ev) ILLUME_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (int e = 1; e < nengines; ++e) {
+      cudaStream_t s = nullptr;
+      ILLUME_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+      more_streams.push_back(s);
+      cudaEvent_t j = nullptr;
+      ILLUME_CUDA_TRY(cudaEventCreateWithFlags(&j, cudaEventDisableTiming));
+      join_ev.push_back(j);
+      more.emplace_back(new Engine);
+      Engine& x = *more.back();
+      x.stream = s;
+      if ((st = x.init(ctx, 1, per_pass * npix, render_knobs(p), err)) != ILLUME_OK) return st;
+      x.mirror[0] = row;
+      if ((st = x.write_row(0)) != ILLUME_OK) { *err = last_error(); return st; }
+      ILLUME_CUDA_TRY(cudaStreamSynchronize(s));
+    }
   }
   ILLUME_CUDA_TRY(cudaEventCreate(&ev0));
   ILLUME_CUDA_TRY(cudaEventCreate(&ev1));
@@ -139,12 +158,12 @@ void Renderer::set_range(int first, int count) {
   J.sample_end = first + count;
   J.per_pass = per_pass;
   J.nsamples = std::min(per_pass, count);
-  if (split) {   // the second engine starts one pass later
-    JobDesc& K = eng2.mirror[0];
-    K.sample_base = first + per_pass;
+  for (int e = 1; e < nengines; ++e) {   // engine e starts e passes later
+    JobDesc& K = engine(e).mirror[0];
+    K.sample_base = first + e * per_pass;
     K.sample_end = first + count;
     K.per_pass = per_pass;
-    K.nsamples = std::max(0, std::min(per_pass, count - per_pass));
+    K.nsamples = std::max(0, std::min(per_pass, count - e * per_pass));
   }
 }
 
@@ -159,45 +178,48 @@ int Renderer::render_device(bool accumulate, illume_render_stats* stats) {
   const int spp = p.spp;
   set_range(next_sample, spp);
   int s;
-  if ((s = eng.write_pass_state(0)) != ILLUME_OK) return s;
-  if (split && (s = eng2.write_pass_state(0)) != ILLUME_OK) return s;
-  unsigned long long rays_before[2] = {0, 0}, rays_after[2] = {0, 0};
+  for (int e = 0; e < nengines; ++e)
+    if ((s = engine(e).write_pass_state(0)) != ILLUME_OK) return s;
+  // every engine's ray total before and after, read on the context's stream (the extra
+  // engines' streams are idle here and joined into it before the second read)
+  std::vector<unsigned long long> rays_before(nengines, 0), rays_after(nengines, 0);
   const size_t rays_off = offsetof(JobDesc, rays);
-  ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_before[0], reinterpret_cast<const char*>(eng.w.jobs) + rays_off, 8,
-                                  cudaMemcpyDeviceToHost, st));
-  if (split)
-    ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_before[1], reinterpret_cast<const char*>(eng2.w.jobs) + rays_off, 8,
-                                    cudaMemcpyDeviceToHost, stream2));
+  for (int e = 0; e < nengines; ++e) {
+    if (e > 0) ILLUME_CUDA_TRY(cudaStreamSynchronize(more_streams[e - 1]));   // its row write
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_before[e], reinterpret_cast<const char*>(engine(e).w.jobs) + rays_off, 8,
+                                    cudaMemcpyDeviceToHost, st));
+  }
   const int npasses = spp > 0 ? (spp + per_pass - 1) / per_pass : 0;
   ILLUME_CUDA_TRY(cudaEventRecord(ev0, st));
-  if (split) {
-    // passes alternate between the engines; each accumulation waits for the previous one
-    ILLUME_CUDA_TRY(cudaStreamWaitEvent(stream2, ev0, 0));
+  if (nengines > 1) {
+    // passes go round the engines; each accumulation waits for the previous one
+    for (cudaStream_t x : more_streams) ILLUME_CUDA_TRY(cudaStreamWaitEvent(x, ev0, 0));
     for (int i = 0; i < npasses; ++i) {
-      Engine& e = (i & 1) ? eng2 : eng;
-      if ((s = e.run_interleaved(p.max_depth, i > 0 ? acc_ev[(i - 1) & 1] : nullptr, acc_ev[i & 1])) != ILLUME_OK)
-        return s;
+      const int e = i % nengines;
+      cudaEvent_t wait = i > 0 ? acc_ev[(i - 1) % nengines] : nullptr;
+      if ((s = engine(e).run_interleaved(p.max_depth, wait, acc_ev[e])) != ILLUME_OK) return s;
     }
-    ILLUME_CUDA_TRY(cudaEventRecord(join_ev, stream2));
-    ILLUME_CUDA_TRY(cudaStreamWaitEvent(st, join_ev, 0));
+    for (int e = 1; e < nengines; ++e) {
+      ILLUME_CUDA_TRY(cudaEventRecord(join_ev[e - 1], more_streams[e - 1]));
+      ILLUME_CUDA_TRY(cudaStreamWaitEvent(st, join_ev[e - 1], 0));
+    }
   } else {
     if ((s = eng.run(npasses, p.max_depth)) != ILLUME_OK) return s;
   }
   ILLUME_CUDA_TRY(cudaEventRecord(ev1, st));
-  ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_after[0], reinterpret_cast<const char*>(eng.w.jobs) + rays_off, 8,
-                                  cudaMemcpyDeviceToHost, st));
-  if (split)
-    ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_after[1], reinterpret_cast<const char*>(eng2.w.jobs) + rays_off, 8,
+  for (int e = 0; e < nengines; ++e)
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_after[e], reinterpret_cast<const char*>(engine(e).w.jobs) + rays_off, 8,
                                     cudaMemcpyDeviceToHost, st));
   ILLUME_CUDA_TRY(cudaStreamSynchronize(st));
-  if (split) ILLUME_CUDA_TRY(cudaStreamSynchronize(stream2));
   ILLUME_CUDA_TRY(cudaGetLastError());
   samples_done += spp;
   next_sample += spp;
   if (stats) {
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, ev0, ev1);
-    stats->rays = (int64_t)(rays_after[0] - rays_before[0] + rays_after[1] - rays_before[1]);
+    int64_t rays = 0;
+    for (int e = 0; e < nengines; ++e) rays += (int64_t)(rays_after[e] - rays_before[e]);
+    stats->rays = rays;
     stats->paths = (int64_t)spp * npix;
     stats->render_ms = ms;
     stats->kernel_launches = (int64_t)npasses * Engine::launches_per_pass(p.max_depth, p.estimator == ILLUME_ESTIMATOR_NEE);

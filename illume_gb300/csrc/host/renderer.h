@@ -6,14 +6,15 @@
 // replayed; the sample range lives in the device's job row, so the host issues one
 // graph launch per pass and never waits inside the loop.
 //
-// Large renders split the path slots over two engines on two streams that take turns on
-// the sample ranges: while one pass is in its last bounces (few, long rays that leave
-// most of the GPU idle), the next pass's first bounces fill the GPU. Accumulations stay
-// in sample order (each waits for the previous pass's), so the image is the same as with
-// one engine.
+// Large renders split the path slots over several engines on their own streams that
+// take turns on the sample ranges: while one pass is in its last bounces (few, long rays
+// that leave most of the GPU idle), the next passes' first bounces fill the GPU.
+// Accumulations stay in sample order (each waits for the previous pass's), so the image
+// is the same as with one engine.
 #pragma once
 
 #include <memory>
+#include <vector>
 
 #include "engine.h"
 
@@ -24,11 +25,14 @@ struct Renderer {
   Scene* scene = nullptr;
   illume_render_params p{};
   int npix = 0, per_pass = 1;
-  Engine eng;
-  Engine eng2;                  // second engine of a split render (samples per_pass..2 per_pass-1, ...)
-  bool split = false;
-  cudaStream_t stream2 = nullptr;
-  cudaEvent_t acc_ev[2] = {nullptr, nullptr}, join_ev = nullptr;
+  Engine eng;                   // engine 0, on the context's stream
+  // engines 1..nengines-1 of a split render, each on a stream of its own; engine e
+  // renders samples [e p, (e + 1) p), [(e + n) p, (e + n + 1) p), ... of each call
+  std::vector<std::unique_ptr<Engine>> more;
+  std::vector<cudaStream_t> more_streams;
+  int nengines = 1;
+  std::vector<cudaEvent_t> acc_ev;   // per engine: its last pass's accumulation
+  std::vector<cudaEvent_t> join_ev;  // per extra engine: the end of its work in a call
   DevBuffer sum32, comp32, sum64, sumsq, out_mean, out_rgb8;
   Accumulators acc{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -46,6 +50,7 @@ struct Renderer {
 
  private:
   void set_range(int first, int count);
+  Engine& engine(int e) { return e == 0 ? eng : *more[e - 1]; }
 };
 
 CameraView make_camera(const SceneHost& h, int width, int height);

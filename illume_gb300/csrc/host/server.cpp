@@ -19,7 +19,7 @@ static constexpr size_t kBytesPerPath = 6 * sizeof(float4) + sizeof(float4) + si
                                         sizeof(float4);
 
 static int engine_key(const illume_render_params& p) { return p.intersector * 16 + p.bvh_kind; }
-static constexpr int kMaxLanes = 4;
+static constexpr int kMaxLanes = 16;
 
 LaneStream::~LaneStream() {
   if (stream) {

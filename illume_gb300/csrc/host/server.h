@@ -15,10 +15,11 @@
 // sample order whatever the pass split, so the result is bit-identical alone and in
 // any mix.
 //
-// Every trace-kernel setting has up to `lanes` job tables, each on its own stream; an
-// admitted job joins the table with the least work to go and stays there. A step
-// launches every table's passes at once, so one table's last bounces (few, long rays
-// that leave most of the GPU idle) overlap the other tables' passes.
+// Every trace-kernel setting has up to `lanes` job tables (8 by default), each on its
+// own stream; an admitted job joins the table with the least work to go and stays
+// there, and a new table is made only when every existing one has work. A step launches
+// every table's passes at once, so one table's last bounces (few, long rays that leave
+// most of the GPU idle) overlap the other tables' passes.
 //
 // The autotuner picks the tables' path slots and trace kernel variant from measured
 // throughput on the live workload: each candidate runs a few steps of the real jobs
@@ -86,7 +87,7 @@ struct Server {
   int passes_per_step = 1;
   int autotune = 0;
   int trace_variant = -1;     // -1 = per-layout default
-  int lanes = 2;              // job tables per trace-kernel setting
+  int lanes = 8;              // job tables per trace-kernel setting
   size_t reserved = 0;        // job footprints
   int64_t next_id = 1;
   std::map<int64_t, std::unique_ptr<ServerJob>> jobs;

@@ -171,7 +171,13 @@ typedef struct {
   int32_t shade_variant;      /* 0 = the measured best register bound (default), 1 = the
                                * compiler's choice, 2 / 3 / 4 = at most 80 / 72 / 64 registers */
   int32_t estimator;          /* illume_estimator */
-  int32_t reserved;
+  int32_t engines;            /* renderer: engines (path tables on their own streams) taking
+                               * turns on the passes of a call, so that one pass's last bounces
+                               * overlap the next passes; 0 = for a pass of 4M paths or more one
+                               * per 16M paths, 2 to 4, else 1; at most 16 and at most the
+                               * samples per pass.
+                               * The image does not depend on it. The server ignores it
+                               * (ILLUME_SERVER_LANES). */
 } illume_render_params;
 
 typedef struct {
@@ -348,7 +354,8 @@ typedef enum {
   ILLUME_SERVER_AUTOTUNE = 2,         /* 1 = choose path slots and trace kernel from measured throughput */
   ILLUME_SERVER_TRACE_VARIANT = 3,    /* trace kernel variant (-1 = default) */
   ILLUME_SERVER_LANES = 4             /* job tables per trace-kernel setting, each on its own
-                                       * stream, whose passes overlap (1-4, default 2) */
+                                       * stream, whose passes overlap (1-16, default 8); a table
+                                       * is created only when every existing one has work */
 } illume_server_option;
 int illume_server_set_option(illume_server* s, int option, int64_t value);
 
