@@ -349,15 +349,23 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
         bvh4_slot(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, ch.z, r, best.t, k2, e2);
         bvh4_slot(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, ch.w, r, best.t, k3, e3);
       }
-      sort_pair(k0, e0, k1, e1);
-      sort_pair(k2, e2, k3, e3);
-      sort_pair(k0, e0, k2, e2);
-      sort_pair(k1, e1, k3, e3);
-      if (!PS) sort_pair(k1, e1, k2, e2);
-      if (e3 != kEmpty) push(e3);
-      if (e2 != kEmpty) push(e2);
-      if (e1 != kEmpty) push(e1);
-      cur = e0 != kEmpty ? e0 : (sp > 0 ? pop() : kEmpty);
+      if (ANY) {
+        // occlusion: any hit ends the walk, so the children go unordered
+        if (e3 != kEmpty) push(e3);
+        if (e2 != kEmpty) push(e2);
+        if (e1 != kEmpty) push(e1);
+        cur = e0 != kEmpty ? e0 : (sp > 0 ? pop() : kEmpty);
+      } else {
+        sort_pair(k0, e0, k1, e1);
+        sort_pair(k2, e2, k3, e3);
+        sort_pair(k0, e0, k2, e2);
+        sort_pair(k1, e1, k3, e3);
+        if (!PS) sort_pair(k1, e1, k2, e2);
+        if (e3 != kEmpty) push(e3);
+        if (e2 != kEmpty) push(e2);
+        if (e1 != kEmpty) push(e1);
+        cur = e0 != kEmpty ? e0 : (sp > 0 ? pop() : kEmpty);
+      }
       if (cur < kEmpty && leaf == kEmpty) {
         leaf = cur;
         cur = sp > 0 ? pop() : kEmpty;
