@@ -400,7 +400,9 @@ def run_ours(args):
                          "frac_of_l2": round(achieved_gbs / l2_peak, 4) if l2_peak else None,
                          "l2_note": "the traversal data (~10 MB) is L2-resident; l2_gbs is the read bandwidth "
                                     "of a 32 MB buffer swept 200 times by illume_measure_l2_read, here",
-                         "trace_ms_per_pass": round(prof_t.trace_ms, 3), "shade_ms_per_pass": round(prof_t.shade_ms, 3)},
+                         "trace_ms_per_pass": round(prof_t.trace_ms, 3), "shade_ms_per_pass": round(prof_t.shade_ms, 3),
+                         "accumulate_ms_per_pass": round(prof_t.accumulate_ms, 3),
+                         "raygen_ms_per_pass": round(prof_t.raygen_ms, 3)},
             "cpu_baseline": cpu,
             "quality": quality,
             "e2e": {"value": round(e2e_value, 3), "unit": "Mrays/s",

@@ -437,6 +437,9 @@ __global__ void __launch_bounds__(256) k_accumulate(WaveBuffers w) {
       s64[c] = mode == ACCUM_FP64 ? acc.sum64[3 * p + c] : 0.0;
       q64[c] = acc.sumsq ? acc.sumsq[3 * p + c] : 0.0;
     }
+    // squares of this pass's samples summed in FP32 (at most samples-per-pass terms),
+    // then added to the FP64 total once per pass
+    float qp[3] = {0.0f, 0.0f, 0.0f};
     for (int s = 0; s < ns; ++s) {
       const float4 L = w.contrib[path_base + (size_t)s * npix + p];
       const float l[3] = {L.x, L.y, L.z};
@@ -452,9 +455,11 @@ __global__ void __launch_bounds__(256) k_accumulate(WaveBuffers w) {
         } else {
           s64[c] += (double)l[c];
         }
-        if (squares) q64[c] += (double)l[c] * (double)l[c];
+        if (squares) qp[c] = __fmaf_rn(l[c], l[c], qp[c]);
       }
     }
+    if (squares)
+      for (int c = 0; c < 3; ++c) q64[c] += (double)qp[c];
     for (int c = 0; c < 3; ++c) {
       if (mode != ACCUM_FP64) acc.sum32[3 * p + c] = s32[c];
       if (mode == ACCUM_KAHAN) acc.comp32[3 * p + c] = c32[c];

@@ -254,7 +254,8 @@ int illume_renderer_get_height(const illume_renderer* r);
 int illume_render_to_bitmap(illume_renderer* r, illume_bitmap* bitmap, illume_render_stats* stats);
 /* Render into host buffers (each nullable): mean linear radiance (W*H*3 floats), the
  * per-pixel sum and sum of squares of per-sample radiance (W*H*3 doubles each) and the
- * tonemapped RGB8 image (W*H*3 bytes). */
+ * tonemapped RGB8 image (W*H*3 bytes). The sum follows accum_mode; the sum of squares is
+ * an FP64 total of each pass's squares summed in FP32 (for variance estimates). */
 int illume_render(illume_renderer* r, float* out_mean, double* out_sum, double* out_sumsq, uint8_t* out_rgb8,
                   illume_render_stats* stats);
 /* Device-resident variant: runs the bounce loop only, leaving the accumulators on the
