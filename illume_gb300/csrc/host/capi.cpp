@@ -274,7 +274,8 @@ int illume_render_to_bitmap(illume_renderer* r, illume_bitmap* bitmap, illume_re
 illume_bitmap* illume_bitmap_new(size_t width, size_t height) {
   illume_bitmap* b = (illume_bitmap*)calloc(1, sizeof(illume_bitmap));
   if (!b) return nullptr;
-  b->pixels = (illume_pixel*)calloc(width * height ? width * height : 1, sizeof(illume_pixel));
+  const size_t n = width * height;
+  b->pixels = (illume_pixel*)calloc(n > 0 ? n : 1, sizeof(illume_pixel));
   if (!b->pixels) { free(b); return nullptr; }
   b->width = width;
   b->height = height;

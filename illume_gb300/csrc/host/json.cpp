@@ -73,11 +73,11 @@ struct Parser {
         case 'r': *o += '\r'; break;
         case 't': *o += '\t'; break;
         case 'u': {
-          unsigned cp;
+          unsigned cp = 0;
           if (!hex4(&cp)) return false;
           if (cp >= 0xD800 && cp < 0xDC00 && i + 6 <= n && s[i] == '\\' && s[i + 1] == 'u') {
             i += 2;
-            unsigned lo;
+            unsigned lo = 0;
             if (!hex4(&lo)) return false;
             cp = 0x10000 + ((cp - 0xD800) << 10) + (lo - 0xDC00);
           }
