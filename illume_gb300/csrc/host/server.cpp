@@ -335,9 +335,15 @@ void Server::compose(ServerEngine& se) {
 int Server::retire(ServerEngine& se, std::vector<ServerJob*>* done) {
   Engine& e = *se.eng;
   cudaStream_t st = ctx->stream;
-  std::vector<std::pair<int, unsigned long long>> rays;
-  for (int r = 0; r < e.rows; ++r) {
-    if (!se.row_job[r] || e.mirror[r].sample_base < e.mirror[r].sample_end) continue;
+  // every finished job's tonemap and copies first, one wait for all of them
+  std::vector<int> rows_done;
+  std::vector<unsigned long long> rays;
+  for (int r = 0; r < e.rows; ++r)
+    if (se.row_job[r] && e.mirror[r].sample_base >= e.mirror[r].sample_end) rows_done.push_back(r);
+  if (rows_done.empty()) return ILLUME_OK;
+  rays.assign(rows_done.size(), 0);
+  for (size_t k = 0; k < rows_done.size(); ++k) {
+    const int r = rows_done[k];
     ServerJob* j = jobs[se.row_job[r]].get();
     const illume_render_params& p = j->params;
     const int npix = p.width * p.height;
@@ -353,12 +359,16 @@ int Server::retire(ServerEngine& se, std::vector<ServerJob*>* done) {
     ILLUME_CUDA_TRY(cudaMemcpyAsync(j->mean.data(), j->out_mean.get(), sizeof(float) * j->mean.size(),
                                     cudaMemcpyDeviceToHost, st));
     ILLUME_CUDA_TRY(cudaMemcpyAsync(j->rgb8.data(), j->out_rgb8.get(), j->rgb8.size(), cudaMemcpyDeviceToHost, st));
-    unsigned long long n = 0;
-    ILLUME_CUDA_TRY(cudaMemcpyAsync(&n, reinterpret_cast<const char*>(e.w.jobs + r) + offsetof(JobDesc, rays), 8,
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays[k], reinterpret_cast<const char*>(e.w.jobs + r) + offsetof(JobDesc, rays), 8,
                                     cudaMemcpyDeviceToHost, st));
-    ILLUME_CUDA_TRY(cudaStreamSynchronize(st));
-    j->stats.rays = (int64_t)n;
-    j->stats.paths = (int64_t)p.spp * npix;
+  }
+  ILLUME_CUDA_TRY(cudaStreamSynchronize(st));
+  for (size_t k = 0; k < rows_done.size(); ++k) {
+    const int r = rows_done[k];
+    ServerJob* j = jobs[se.row_job[r]].get();
+    const illume_render_params& p = j->params;
+    j->stats.rays = (int64_t)rays[k];
+    j->stats.paths = (int64_t)p.spp * p.width * p.height;
     j->stats.d2h_bytes = (int64_t)(j->mean.size() * sizeof(float) + j->rgb8.size());
     j->sum32.release();
     j->comp32.release();
