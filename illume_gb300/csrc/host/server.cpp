@@ -452,18 +452,46 @@ void Server::tune(int base_key, double rays, double ms) {
   t.state = 2;
 }
 
+// Waits for the passes the last step launched, then retires the jobs they finished and
+// feeds the autotuner.
+int Server::finish_in_flight(std::vector<ServerJob*>* done) {
+  if (in_flight.empty()) return ILLUME_OK;
+  for (Launched& l : in_flight)
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&l.total, l.se->eng->w.rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  totals.device_ms += ms;
+  std::map<int, double> rays_by_key;
+  int st;
+  for (Launched& l : in_flight) {
+    const double rays = (double)(l.total - l.se->rays_seen);
+    l.se->rays_seen = l.total;
+    totals.rays += (int64_t)rays;
+    rays_by_key[l.se->base_key] += rays;
+    if ((st = retire(*l.se, done)) != ILLUME_OK) return st;
+  }
+  in_flight.clear();
+  if (autotune)
+    for (const auto& kr : rays_by_key)
+      if (tuners[kr.first].state != 2) tune(kr.first, kr.second, ms);
+  return ILLUME_OK;
+}
+
+// One scheduling round. The passes it launches run on while the caller does its own
+// work; the next call waits for them before it admits, composes and launches again, so
+// the device does not sit idle between rounds. A job whose last samples were in those
+// passes is retired (its results readable by poll) by that next call.
 int Server::step(int* running_out) {
   if (!ev0) {
     ILLUME_CUDA_TRY(cudaEventCreate(&ev0));
     ILLUME_CUDA_TRY(cudaEventCreate(&ev1));
   }
-  int st = admit();
-  if (st != ILLUME_OK) return st;
   std::vector<ServerJob*> done;
-  // every table's passes are launched on its own stream before any is waited for
-  struct Launched { ServerEngine* se; int k; unsigned long long total; };
-  std::vector<Launched> launched;
-  launched.reserve(engines.size());
+  int st = finish_in_flight(&done);
+  if (st != ILLUME_OK) return st;
+  if ((st = admit()) != ILLUME_OK) return st;
+  // every table's passes are launched on its own stream, and none is waited for here
   ILLUME_CUDA_TRY(cudaEventRecord(ev0, ctx->stream));
   for (auto& kv : engines) {
     ServerEngine& se = kv.second;
@@ -489,26 +517,9 @@ int Server::step(int* running_out) {
     for (int r : active) jobs[se.row_job[r]]->stats.kernel_launches += (int64_t)k * per_pass_launches;
     totals.passes += k;
     totals.kernel_launches += (int64_t)k * per_pass_launches;
-    launched.push_back({&se, k, 0});
+    in_flight.push_back({&se, k, 0});
   }
   ILLUME_CUDA_TRY(cudaEventRecord(ev1, ctx->stream));
-  for (Launched& l : launched)
-    ILLUME_CUDA_TRY(cudaMemcpyAsync(&l.total, l.se->eng->w.rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  float ms = 0.0f;
-  if (!launched.empty()) cudaEventElapsedTime(&ms, ev0, ev1);
-  totals.device_ms += ms;
-  std::map<int, double> rays_by_key;
-  for (Launched& l : launched) {
-    const double rays = (double)(l.total - l.se->rays_seen);
-    l.se->rays_seen = l.total;
-    totals.rays += (int64_t)rays;
-    rays_by_key[l.se->base_key] += rays;
-    if ((st = retire(*l.se, &done)) != ILLUME_OK) return st;
-  }
-  if (autotune)
-    for (const auto& kr : rays_by_key)
-      if (tuners[kr.first].state != 2) tune(kr.first, kr.second, ms);
   const double t = now_ms();
   for (ServerJob* j : done) {
     j->finish_ms = t;

@@ -96,6 +96,9 @@ struct Server {
   std::map<int, Tuner> tuners;           // by engine_key
   illume_server_stats totals{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // the passes of the last step, still running on the device when step() returned
+  struct Launched { ServerEngine* se; int k; unsigned long long total; };
+  std::vector<Launched> in_flight;
 
   ~Server();
   static size_t footprint(const illume_render_params& p);
@@ -112,6 +115,7 @@ struct Server {
   void compose(ServerEngine& se);
   int retire(ServerEngine& se, std::vector<ServerJob*>* done);
   int new_engine(const illume_render_params& p, int key, long long cap, ServerEngine** out);
+  int finish_in_flight(std::vector<ServerJob*>* done);
   void tune(int base_key, double rays, double ms);
   int apply_candidate(int base_key, int idx);
 };

@@ -335,10 +335,13 @@ int illume_server_destroy(illume_server* s);
 /* Queue a job (ILLUME_ERR_BUDGET if its footprint can never fit the budget). The
  * server ignores params->samples_per_pass and the binary-kernel variant word. */
 int illume_job_submit(illume_server* s, illume_scene* scene, const illume_render_params* params, illume_job_id* out);
-/* One scheduling round: admit what fits, compose the passes (jobs grouped by scene,
- * smallest remaining job first, slots shared by water-filling), run up to
- * ILLUME_SERVER_PASSES_PER_STEP wavefront passes (fewer if a job finishes sooner),
- * retire finished jobs. *jobs_running = running + queued jobs afterwards. */
+/* One scheduling round: wait for the passes the previous round launched and retire the
+ * jobs they finished, admit what fits, compose the passes (jobs grouped by scene,
+ * smallest remaining job first, slots shared by water-filling) and launch up to
+ * ILLUME_SERVER_PASSES_PER_STEP wavefront passes (fewer if a job finishes sooner)
+ * without waiting for them, so the device works while the caller does. A job's results
+ * are ready (illume_job_poll) after the round that retires it; stats lag by a round.
+ * *jobs_running = running + queued jobs afterwards (0 once everything is retired). */
 int illume_server_step(illume_server* s, int* jobs_running);
 /* ILLUME_OK when done (results copied to the nullable buffers), ILLUME_ERR_NOT_READY
  * otherwise. stats: rays of this job, paths, render_ms = submit-to-finish minus queue
