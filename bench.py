@@ -516,7 +516,7 @@ def run_batched(args):
                     "device_s": round(bs.device_ms * 1e-3, 3), "wall_s": round(wall_b, 3), "passes": int(bs.passes)},
         "plain": {"mrays_device": round(plain_dev, 2), "mrays_wall": round(plain_wall, 2), "rays": int(pl["rays"]),
                   "device_s": round(pl["device_ms"] * 1e-3, 3), "wall_s": round(pl["wall_s"], 3),
-                  "samples_per_pass": "auto (min(spp, 4M / pixels))"},
+                  "samples_per_pass": "auto (min(spp, 32M / pixels))"},
         "speedup_device": round(batched_dev / plain_dev, 3), "speedup_wall": round(batched_wall / plain_wall, 3),
         "images_identical_across_arms": bool(same), "nan_pixels": nan_pixels,
         "e2e": {"value": round(batched_wall, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,

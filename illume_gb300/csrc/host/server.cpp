@@ -413,18 +413,21 @@ void Server::tune(int base_key, double rays, double ms) {
   static constexpr int kWindow = 3;
   Tuner& t = tuners[base_key];
   if (t.state == 0) {
-    int kind = BVH_BINARY, ntables = 0;
+    int kind = BVH_BINARY, ntables = 0, current = 0;
     size_t held = 0;
     for (const auto& kv : engines)
       if (kv.second.base_key == base_key) {
         kind = kv.second.eng->knobs.bvh_kind;
         held += kv.second.eng->device_bytes();
+        current = std::max(current, kv.second.eng->cap);
         ++ntables;
       }
     // binary BVH: the default kernel and its while-while form; 8-wide: both kernels;
     // 4-wide: the traversal stack in local memory or partly in shared memory
     const std::vector<int> variants = kind == BVH_BINARY ? std::vector<int>{0, 3} : std::vector<int>{0, 1};
-    for (int cap : {1 << 23, 1 << 24}) {
+    // the tables' present size first: its windows need no reallocation
+    const int other = current == (1 << 24) ? 1 << 25 : 1 << 24;
+    for (int cap : {current == (1 << 24) ? 1 << 24 : 1 << 25, other}) {
       if (budget && reserved + engines_bytes() - held + (size_t)ntables * cap * kBytesPerPath > budget) continue;
       for (int v : variants) t.candidates.push_back({cap, v});
     }
@@ -694,6 +697,7 @@ int illume_render_batch(illume_context* ctx, int n, illume_scene* const* scenes,
   if (st != ILLUME_OK) return st;
   s->s.autotune = autotune != 0;
   s->s.passes_per_step = 8;
+  s->s.lanes = 8;   // throughput over latency: more tables overlap more passes' tails
   std::vector<illume_job_id> ids(n);
   for (int i = 0; i < n && st == ILLUME_OK; ++i) {
     if (!scenes[i]) { illume::set_error("null scene"); st = ILLUME_ERR_INVALID; break; }

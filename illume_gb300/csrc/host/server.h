@@ -15,9 +15,9 @@
 // sample order whatever the pass split, so the result is bit-identical alone and in
 // any mix.
 //
-// Every trace-kernel setting has up to `lanes` job tables (8 by default), each on its
-// own stream; an admitted job joins the table with the least work to go and stays
-// there, and a new table is made only when every existing one has work. A step launches
+// Every trace-kernel setting has up to `lanes` job tables (4 by default, 8 for a
+// batch), each on its own stream; an admitted job joins the table with the least work
+// to go and stays there, and a new table is made only when every existing one has work. A step launches
 // every table's passes at once, so one table's last bounces (few, long rays that leave
 // most of the GPU idle) overlap the other tables' passes.
 //
@@ -83,11 +83,11 @@ struct Server {
   Context* ctx = nullptr;
   size_t budget = 0;          // device bytes for engines and job buffers (0 = unlimited)
   int rows = 64;              // job-table rows per engine
-  int path_capacity = 1 << 23;
+  int path_capacity = 1 << 25;
   int passes_per_step = 1;
   int autotune = 0;
   int trace_variant = -1;     // -1 = per-layout default
-  int lanes = 8;              // job tables per trace-kernel setting
+  int lanes = 4;              // job tables per trace-kernel setting
   size_t reserved = 0;        // job footprints
   int64_t next_id = 1;
   std::map<int64_t, std::unique_ptr<ServerJob>> jobs;

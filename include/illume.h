@@ -154,7 +154,8 @@ typedef struct {
   int32_t intersector;        /* illume_intersector */
   int32_t bvh_kind;           /* illume_bvh_kind */
   int32_t exact_hg;           /* 0 = reference Henyey-Greenstein sampler, 1 = exact */
-  int32_t samples_per_pass;   /* samples of every pixel kept in flight per wavefront pass (0 = auto) */
+  int32_t samples_per_pass;   /* samples of every pixel kept in flight per wavefront pass (0 = auto:
+                               * min(spp, 32M paths / pixels), at least 1) */
   /* Nullable camera override, read when a renderer is created or a job is submitted: 12
    * floats of the camera-to-world rows (3x4, the layout of illume_scene_desc's
    * camera_transform), then fov (degrees), dof and aperture. NULL = the scene's camera. */
@@ -353,12 +354,13 @@ int illume_job_poll(illume_server* s, illume_job_id id, float* out_mean, uint8_t
 int illume_job_cancel(illume_server* s, illume_job_id id);
 
 typedef enum {
-  ILLUME_SERVER_PATH_CAPACITY = 0,    /* path slots of each job table (default 8388608) */
+  ILLUME_SERVER_PATH_CAPACITY = 0,    /* path slots of each job table (default 33554432) */
   ILLUME_SERVER_PASSES_PER_STEP = 1,  /* passes per illume_server_step (default 1) */
   ILLUME_SERVER_AUTOTUNE = 2,         /* 1 = choose path slots and trace kernel from measured throughput */
   ILLUME_SERVER_TRACE_VARIANT = 3,    /* trace kernel variant (-1 = default) */
   ILLUME_SERVER_LANES = 4             /* job tables per trace-kernel setting, each on its own
-                                       * stream, whose passes overlap (1-16, default 8); a table
+                                       * stream, whose passes overlap (1-16, default 4;
+                                       * illume_render_batch uses 8); a table
                                        * is created only when every existing one has work */
 } illume_server_option;
 int illume_server_set_option(illume_server* s, int option, int64_t value);
