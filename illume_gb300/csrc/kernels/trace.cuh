@@ -349,23 +349,25 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
         bvh4_slot(lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, ch.z, r, best.t, k2, e2);
         bvh4_slot(lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, ch.w, r, best.t, k3, e3);
       }
-      if (ANY) {
-        // occlusion: any hit ends the walk, so the children go unordered
-        if (e3 != kEmpty) push(e3);
-        if (e2 != kEmpty) push(e2);
-        if (e1 != kEmpty) push(e1);
-        cur = e0 != kEmpty ? e0 : (sp > 0 ? pop() : kEmpty);
-      } else {
+      if (!ANY) {
         sort_pair(k0, e0, k1, e1);
         sort_pair(k2, e2, k3, e3);
         sort_pair(k0, e0, k2, e2);
         sort_pair(k1, e1, k3, e3);
         if (!PS) sort_pair(k1, e1, k2, e2);
+      }
+      // (occlusion: any hit ends the walk, so the children go unordered.) The room for
+      // the three pushes is checked once per node; a full stack drops what does not fit.
+      if (__builtin_expect(sp <= kStack - 3, 1)) {
+        if (e3 != kEmpty) stack[sp++] = e3;
+        if (e2 != kEmpty) stack[sp++] = e2;
+        if (e1 != kEmpty) stack[sp++] = e1;
+      } else {
         if (e3 != kEmpty) push(e3);
         if (e2 != kEmpty) push(e2);
         if (e1 != kEmpty) push(e1);
-        cur = e0 != kEmpty ? e0 : (sp > 0 ? pop() : kEmpty);
       }
+      cur = e0 != kEmpty ? e0 : (sp > 0 ? pop() : kEmpty);
       if (cur < kEmpty && leaf == kEmpty) {
         leaf = cur;
         cur = sp > 0 ? pop() : kEmpty;
