@@ -696,10 +696,11 @@ int illume_render_batch(illume_context* ctx, int n, illume_scene* const* scenes,
   int st = illume_server_create(ctx, 0, std::max(1, std::min(n, 1024)), &s);
   if (st != ILLUME_OK) return st;
   s->s.autotune = autotune != 0;
-  // throughput over latency: more tables overlap more passes' tails. One pass per step
-  // (the default): a finished job's row is refilled at the next step, not up to seven
-  // passes later (64-job batch: 4739 against 4606 Mrays/s with 8 passes per step)
-  s->s.lanes = 8;
+  // throughput over latency: more tables overlap more passes' tails (64-job batch: 4773,
+  // 4851, 4911 Mrays/s with 8, 12, 16 tables). One pass per step (the default): a
+  // finished job's row is refilled at the next step, not up to seven passes later (4739
+  // against 4606 Mrays/s with 8 passes per step)
+  s->s.lanes = illume::kMaxLanes;
   std::vector<illume_job_id> ids(n);
   for (int i = 0; i < n && st == ILLUME_OK; ++i) {
     if (!scenes[i]) { illume::set_error("null scene"); st = ILLUME_ERR_INVALID; break; }

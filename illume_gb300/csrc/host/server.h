@@ -15,7 +15,7 @@
 // sample order whatever the pass split, so the result is bit-identical alone and in
 // any mix.
 //
-// Every trace-kernel setting has up to `lanes` job tables (4 by default, 8 for a
+// Every trace-kernel setting has up to `lanes` job tables (4 by default, 16 for a
 // batch), each on its own stream; an admitted job joins the table with the least work
 // to go and stays there, and a new table is made only when every existing one has work. A step launches
 // every table's passes at once, so one table's last bounces (few, long rays that leave

@@ -360,7 +360,7 @@ typedef enum {
   ILLUME_SERVER_TRACE_VARIANT = 3,    /* trace kernel variant (-1 = default) */
   ILLUME_SERVER_LANES = 4             /* job tables per trace-kernel setting, each on its own
                                        * stream, whose passes overlap (1-16, default 4;
-                                       * illume_render_batch uses 8); a table
+                                       * illume_render_batch uses 16); a table
                                        * is created only when every existing one has work */
 } illume_server_option;
 int illume_server_set_option(illume_server* s, int option, int64_t value);
