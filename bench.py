@@ -4,9 +4,9 @@
 Workload (the configuration the headline metric is quoted on): displaced icosphere of
 ~100k triangles (rough gold conductor, GGX alpha 0.2) over a checkerboard ground quad,
 2048x1024 HDR environment map with a sun lobe, 1024x1024 pixels, max depth 25, seeded
-synthetic data. One step = `--spp-per-step` samples of every pixel (64 by default, 67M
-paths), rendered as four passes of 16 samples on four engines that take turns, so that
-one pass's last bounces overlap the next passes; a full 1024-spp render is 16 such steps.
+synthetic data. One step = `--spp-per-step` samples of every pixel (128 by default, 134M
+paths), rendered as four passes of 32 samples on four engines that take turns, so that
+one pass's last bounces overlap the next passes; a full 1024-spp render is 8 such steps.
 
 * value: rays traced (closest-hit queries, counted as the reference counts them) per
   second of device time, inputs resident in HBM, L2 flushed between timed steps.
@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--bvh", default="wide4", choices=["wide4", "binary", "wide", "wide-persistent"])
-    ap.add_argument("--spp-per-step", type=int, default=64)
+    ap.add_argument("--spp-per-step", type=int, default=128)
     ap.add_argument("--trace-variant", type=int, default=0,
                     help="binary traversal: 0 64 registers + fused box tests + dynamic ray fetch + while-while "
                          "(default), 1 compiler register choice, 2 variant 1 held to 64 registers, 3 variant 0 with "
@@ -516,7 +516,7 @@ def run_batched(args):
                     "device_s": round(bs.device_ms * 1e-3, 3), "wall_s": round(wall_b, 3), "passes": int(bs.passes)},
         "plain": {"mrays_device": round(plain_dev, 2), "mrays_wall": round(plain_wall, 2), "rays": int(pl["rays"]),
                   "device_s": round(pl["device_ms"] * 1e-3, 3), "wall_s": round(pl["wall_s"], 3),
-                  "samples_per_pass": "auto (min(spp, 32M / pixels))"},
+                  "samples_per_pass": "auto (min(spp, 128M / pixels))"},
         "speedup_device": round(batched_dev / plain_dev, 3), "speedup_wall": round(batched_wall / plain_wall, 3),
         "images_identical_across_arms": bool(same), "nan_pixels": nan_pixels,
         "e2e": {"value": round(batched_wall, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,

@@ -98,7 +98,7 @@ int Renderer::init(std::string* err) {
   int st = check_render_params(p, *scene, err);
   if (st != ILLUME_OK) return st;
   npix = p.width * p.height;
-  const long long target = 1LL << 25;  // paths in flight per pass (32M: 5.6 GB of path state)
+  const long long target = 1LL << 27;  // paths in flight per pass (128M: 22.5 GB of path state)
   per_pass = p.samples_per_pass > 0 ? p.samples_per_pass : (int)std::max(1LL, std::min<long long>(std::max(p.spp, 1), target / npix));
   if ((long long)per_pass * npix > (1LL << 30)) { *err = "too many paths per pass"; return ILLUME_ERR_INVALID; }
   // engines taking turns: by default, for a pass of 4M paths or more, one per 16M paths

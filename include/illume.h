@@ -155,7 +155,7 @@ typedef struct {
   int32_t bvh_kind;           /* illume_bvh_kind */
   int32_t exact_hg;           /* 0 = reference Henyey-Greenstein sampler, 1 = exact */
   int32_t samples_per_pass;   /* samples of every pixel kept in flight per wavefront pass (0 = auto:
-                               * min(spp, 32M paths / pixels), at least 1) */
+                               * min(spp, 128M paths / pixels), at least 1) */
   /* Nullable camera override, read when a renderer is created or a job is submitted: 12
    * floats of the camera-to-world rows (3x4, the layout of illume_scene_desc's
    * camera_transform), then fov (degrees), dof and aperture. NULL = the scene's camera. */
