@@ -126,7 +126,7 @@ int Server::admit() {
     // the table of this setting with a free row and the least work to go; a table not
     // created yet when every existing one has work (or there is none)
     ServerEngine* pick = nullptr;
-    int key = -1, missing = -1;
+    int key = -1, missing = -1, existing = 0;
     double least = 0.0;
     for (int lane = 0; lane < lanes; ++lane) {
       auto eit = engines.find(base * kMaxLanes + lane);
@@ -135,6 +135,7 @@ int Server::admit() {
         continue;
       }
       ServerEngine& c = eit->second;
+      ++existing;
       bool free_row = false;
       double work = 0.0;
       for (int r = 0; r < c.eng->rows; ++r) {
@@ -162,8 +163,15 @@ int Server::admit() {
       }
       if (cap >= npix) {
         const int st = new_engine(p, base * kMaxLanes + missing, cap, &pick);
-        if (st != ILLUME_OK) return st;
-        key = base * kMaxLanes + missing;
+        if (st == ILLUME_OK) {
+          key = base * kMaxLanes + missing;
+        } else if ((st == ILLUME_ERR_OOM || st == ILLUME_ERR_BUDGET) && existing > 0) {
+          // the device has no room for another table: the setting's existing tables
+          // take the job (now, or when a row frees up)
+          cudaGetLastError();
+        } else {
+          return st;
+        }
       }
     }
     if (!pick) { ++it; continue; }

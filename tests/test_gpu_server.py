@@ -181,3 +181,32 @@ def test_shade_variants_same_image(ctx, scenes):
                 got = Renderer(ctx, sc, params=q).render(mean=True)
                 assert np.array_equal(got["mean"], want["mean"], equal_nan=True), (est, v)
                 assert got["stats"].rays == want["stats"].rays
+
+
+def test_a_table_that_does_not_fit_falls_back():
+    """A context whose memory budget holds one job table but not two: the second table's
+    allocation is refused and the setting's first table takes every job, each image
+    still the one it gets alone."""
+    from illume_gb300 import synth
+    from illume_gb300.api import Context, HostScene, Server
+    slots = 1 << 22                                       # ~0.74 GB of path state per table
+    ctx = Context(0, hbm_budget_bytes=(1 << 30) + (1 << 28))
+    try:
+        a = HostScene.from_data(ctx, synth.cornell_scene(48, 48))
+        jobs = [params(a, 48, 48, 16, 6, seed=s, job=s) for s in (1, 2, 3)]
+        ref = []
+        for p in jobs:
+            srv = Server(ctx, path_capacity=slots)
+            j = srv.submit(a, p)
+            srv.run()
+            ref.append(srv.poll(j)["mean"])
+            srv.close()
+        srv = Server(ctx, path_capacity=slots, lanes=4)
+        ids = [srv.submit(a, p) for p in jobs]
+        srv.run()
+        for k, j in enumerate(ids):
+            assert np.array_equal(srv.poll(j)["mean"], ref[k]), k
+        assert srv.stats().jobs_done == len(jobs)
+        srv.close()
+    finally:
+        ctx.close()
