@@ -10,13 +10,16 @@ one pass's last bounces overlap the next passes; a full 1024-spp render is 8 suc
 
 * value: rays traced (closest-hit queries, counted as the reference counts them) per
   second of device time, inputs resident in HBM, L2 flushed between timed steps.
-* e2e: the same metric through the reference-facing C-ABI with host buffers: every step
+* e2e: the same metric through the reference-facing C-ABI with host buffers, over as
+  many steps as the device leg, L2 flushed before each: every step
   re-uploads the scene geometry (what the reference's SceneRef does on every render;
   the library keeps a page-locked copy of it) and reads the mean image and the
   tonemapped RGB8 image back into pinned host arrays.
 * roofline: the trace kernel's algorithmic bytes (node fetches x node size + triangle
   tests x triangle record size + ray in / hit out, counted by an instrumented pass)
-  over its measured time, against the measured HBM copy bandwidth.
+  over its measured time, against the L2 read bandwidth measured in the same run (the
+  scene's traversal data is L2-resident); the fraction of the measured HBM copy
+  bandwidth is kept beside it.
 * cpu_baseline: the CPU restatement of the reference integrator (oracle/), OpenMP on all
   host cores, on a bounded pixel subset of the same scene.
 
@@ -332,14 +335,6 @@ def run_ours(args):
     l2_peak = ctypes.c_double(0.0)
     C.check(C.lib().illume_measure_l2_read(ctx.handle, 32 << 20, 200, ctypes.byref(l2_peak)))
     l2_peak = l2_peak.value
-    # DRAM traffic of the trace kernel per launch: bytes per ray from the committed ncu
-    # summary, times this workload's rays per trace launch
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "trace_traffic.txt")
-    if os.path.exists(tf):
-        for line in open(tf):
-            if line.startswith("dram_bytes_per_ray:"):
-                traffic = round(float(line.split(":")[1]) * prof_t.rays / max(prof_t.trace_launches, 1))
     algo_per_launch = round(trace_bytes / max(prof_t.trace_launches, 1))
 
     # end to end through the C-ABI with host buffers
@@ -347,21 +342,25 @@ def run_ours(args):
     # the step's results land in pinned host memory (page-locked, DMA-able)
     mean = torch.zeros((npix, 3), dtype=torch.float32, pin_memory=True).numpy()
     rgb8 = torch.zeros((npix, 3), dtype=torch.uint8, pin_memory=True).numpy()
-    e2e_steps = max(1, min(args.steps, 4))
+    # every step as in the device leg: the L2 flushed before it (outside the step's time),
+    # then upload, render and read back, timed on the host clock
+    e2e_steps = args.steps
     up_bytes = ctypes.c_size_t()
     st = C.RenderStats()
     barrier()
-    t0 = time.perf_counter()
+    e2e_s = 0.0
     e2e_rays = 0
     t_up = t_dev = 0.0
     for k in range(e2e_steps):
+        flush.fill_((k + 1) & 0xFF)
+        torch.cuda.synchronize()
         ta = time.perf_counter()
         C.check(C.lib().illume_scene_upload(scene.handle, ctypes.byref(up_bytes)))
         t_up += time.perf_counter() - ta
         C.check(C.lib().illume_render(r.handle, C.fptr(mean), None, None, C.u8ptr(rgb8), ctypes.byref(st)))
+        e2e_s += time.perf_counter() - ta
         t_dev += st.render_ms * 1e-3
         e2e_rays += st.rays
-    e2e_s = time.perf_counter() - t0
     e2e_value = e2e_rays / e2e_s / 1e6
     if world > 1:
         t = torch.tensor([e2e_s, float(e2e_rays)], dtype=torch.float64, device=f"cuda:{dev}")
@@ -386,20 +385,23 @@ def run_ours(args):
                        "triangles": sd.num_triangles(), "resolution": [args.res, args.res], "max_depth": args.depth,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}",
                        "wall_s": round(wall, 3), "rays_per_step": rays_all // args.steps},
-            "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved_gbs / peak, 4), "traffic": traffic,
-                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
+            # the scene's node and triangle bytes (~10 MB) fit in L2, so the traversal roofline
+            # is the L2 read bandwidth, measured in this run (MEASURED_PEAKS.json has no L2
+            # figure); the HBM copy bandwidth is kept beside it
+            "roofline": {"bound": "l2", "achieved": round(achieved_gbs, 1), "peak": round(l2_peak, 1), "unit": "GB/s",
+                         "frac": round(achieved_gbs / l2_peak, 4) if l2_peak else None, "traffic": None,
+                         "peak_source": "measured in this run: L2 read bandwidth of a 32 MB buffer swept 200 times "
+                                        "with 16-byte loads that bypass L1 (illume_measure_l2_read)",
+                         "traffic_note": "DRAM bytes per trace launch come from ncu only (profiles/); not measured "
+                                         "in this run",
+                         "hbm_gbs": peak, "frac_of_hbm": round(achieved_gbs / peak, 4),
+                         "hbm_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
                          "kernel": "k_trace", "bytes_per_ray": round(bytes_per_ray, 1),
                          "algorithmic_bytes_per_launch": algo_per_launch,
-                         "traffic_source": "profiles/trace_traffic.txt (ncu DRAM bytes per ray x rays per launch)",
                          "node_fetches_per_ray": round(prof_c.node_fetches / max(prof_c.rays, 1), 2),
                          "tri_tests_per_ray": round(prof_c.tri_tests / max(prof_c.rays, 1), 2),
                          "node_fetch_lane_utilisation": round(prof_c.node_fetches / max(prof_c.lane_slots, 1), 3),
                          "profiled_pass_spp": pass_spp,
-                         "l2_gbs": round(l2_peak, 1),
-                         "frac_of_l2": round(achieved_gbs / l2_peak, 4) if l2_peak else None,
-                         "l2_note": "the traversal data (~10 MB) is L2-resident; l2_gbs is the read bandwidth "
-                                    "of a 32 MB buffer swept 200 times by illume_measure_l2_read, here",
                          "trace_ms_per_pass": round(prof_t.trace_ms, 3), "shade_ms_per_pass": round(prof_t.shade_ms, 3),
                          "accumulate_ms_per_pass": round(prof_t.accumulate_ms, 3),
                          "raygen_ms_per_pass": round(prof_t.raygen_ms, 3)},

@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_size_t, c_uint8, c_uint32, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_float, c_int, c_int32, c_int64, c_size_t, c_uint8, c_uint32, c_uint64, c_void_p
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_DIR = os.path.join(HERE, "_lib")
@@ -25,6 +25,7 @@ ERR_TIMEOUT = -7
 ERR_CANCELLED = -8
 ERR_UNSUPPORTED = -9
 ERR_NOT_READY = -10
+ERR_TRAVERSAL = -11
 
 MAT_EMISSIVE, MAT_LAMBERT, MAT_REFLECTIVE, MAT_REFRACTIVE, MAT_ROUGHREFLECTIVE, MAT_ROUGHREFRACTIVE, \
     MAT_CONDUCTOR, MAT_ROUGHCONDUCTOR, MAT_PLASTIC = range(9)
@@ -134,6 +135,7 @@ PROTOTYPES = {
     "illume_scene_describe": (c_int, [c_void_p, POINTER(SceneDesc)]),
     "illume_scene_device_bytes": (c_int, [c_void_p, POINTER(c_size_t)]),
     "illume_scene_check_bvh": (c_int, [c_void_p, c_char_p, c_size_t]),
+    "illume_scene_bvh_digest": (c_int, [c_void_p, c_int, POINTER(c_uint64)]),
     "illume_bvh_cache_stats": (c_int, [POINTER(c_int64), POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
     "illume_bvh_cache_clear": (c_int, []),
     "illume_scene_upload": (c_int, [c_void_p, POINTER(c_size_t)]),

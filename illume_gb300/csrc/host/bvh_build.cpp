@@ -8,8 +8,15 @@
 #include <atomic>
 #include <cfloat>
 #include <thread>
+#include <stdlib.h>
 
 namespace illume {
+
+int build_threads() {
+  const char* e = getenv("ILLUME_BUILD_THREADS");
+  if (e && atoi(e) > 0) return std::min(256, atoi(e));
+  return std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+}
 
 namespace {
 
@@ -137,8 +144,10 @@ void build_step(const Work& w, const std::vector<Box>& boxes, const std::vector<
 
 // Binned SAH build; returns nodes (root at 0) and fills order. The top of the tree is
 // split on one thread until the pending subtrees are small; those are built on the host
-// cores (each into its own node list, on a disjoint range of `order`) and stitched in.
-// The splits do not depend on the scheduling, so the tree is the same on any core count.
+// cores (each into its own node list, on a disjoint range of `order`) and stitched in
+// the order they were set aside. Neither the splits nor the size at which subtrees are
+// set aside depend on the thread count, so the node arrays are identical on any number
+// of cores.
 std::vector<BNode> build_binary(const std::vector<Box>& boxes, std::vector<int>& order, int max_leaf) {
   const int N = (int)boxes.size();
   order.resize(N);
@@ -149,8 +158,8 @@ std::vector<BNode> build_binary(const std::vector<Box>& boxes, std::vector<int>&
   std::vector<BNode> nodes;
   nodes.reserve(2 * (size_t)N + 1);
   nodes.emplace_back();
-  const int threads = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
-  const int grain = threads > 1 && N > 20000 ? std::max(4096, N / (8 * threads)) : N + 1;
+  const int threads = build_threads();
+  const int grain = N > 20000 ? std::max(4096, N / 128) : N + 1;
   std::vector<Work> stack{{0, 0, N}}, deferred;
   while (!stack.empty()) {
     const Work w = stack.back();

@@ -39,6 +39,10 @@ struct MeshBvh {
   BuildStats stats;
 };
 
+// Host threads of a BVH build: ILLUME_BUILD_THREADS if set (>= 1), else the cores (at
+// most 16). The result does not depend on it.
+int build_threads();
+
 // positions: 3 floats per vertex; tris: 3 ints per triangle.
 void build_mesh_bvh(const float* positions, int num_vertices, const int* tris, int num_tris, MeshBvh* out);
 

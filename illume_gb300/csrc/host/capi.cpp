@@ -173,6 +173,25 @@ int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t repor
   return ILLUME_OK;
 }
 
+static uint64_t fnv1a(uint64_t h, const void* data, size_t bytes) {
+  const unsigned char* p = static_cast<const unsigned char*>(data);
+  for (size_t i = 0; i < bytes; ++i) h = (h ^ p[i]) * 0x100000001b3ULL;
+  return h;
+}
+
+int illume_scene_bvh_digest(const illume_scene* scene, int mesh, uint64_t out[4]) {
+  CHECK_ARG(scene && out, "null argument");
+  CHECK_ARG(mesh >= 0 && mesh < (int)scene->s.bvhs.size(), "mesh index out of range");
+  const MeshBvh& b = scene->s.bvhs[mesh];
+  const uint64_t h0 = 0xcbf29ce484222325ULL;
+  out[0] = fnv1a(h0, b.bvh2.data(), b.bvh2.size() * sizeof(Bvh2Node));
+  out[1] = fnv1a(h0, b.bvh4.data(), b.bvh4.size() * sizeof(Bvh4Node));
+  out[2] = fnv1a(h0, b.bvh2_tris.data(), b.bvh2_tris.size() * sizeof(float4));
+  out[3] = fnv1a(fnv1a(h0, b.wide.data(), b.wide.size() * sizeof(WideNode)), b.wide_tris.data(),
+                 b.wide_tris.size() * sizeof(float4));
+  return ILLUME_OK;
+}
+
 int illume_scene_destroy(illume_scene* scene) {
   if (!scene) return ILLUME_OK;
   if (scene->s.ctx) cudaStreamSynchronize(scene->s.ctx->stream);
@@ -228,10 +247,19 @@ int illume_renderer_destroy(illume_renderer* r) {
 int illume_renderer_get_width(const illume_renderer* r) { return r ? r->r.p.width : 0; }
 int illume_renderer_get_height(const illume_renderer* r) { return r ? r->r.p.height : 0; }
 
+// The status of a finished render: ILLUME_ERR_TRAVERSAL (outputs written) when a
+// traversal of the call found its stack full.
+static int traversal_status(illume_renderer* r) {
+  if (!r->r.stack_overflow) return ILLUME_OK;
+  set_error("a BVH traversal stack overflowed during the render: the outputs are written, but rays may have missed hits");
+  return ILLUME_ERR_TRAVERSAL;
+}
+
 int illume_render_device(illume_renderer* r, int accumulate, illume_render_stats* stats) {
   CHECK_ARG(r, "null renderer");
   cudaSetDevice(r->r.ctx->device);
-  return r->r.render_device(accumulate != 0, stats);
+  const int st = r->r.render_device(accumulate != 0, stats);
+  return st != ILLUME_OK ? st : traversal_status(r);
 }
 
 int illume_renderer_read(illume_renderer* r, float* out_mean, double* out_sum, double* out_sumsq, uint8_t* out_rgb8) {
@@ -244,7 +272,7 @@ int illume_render(illume_renderer* r, float* out_mean, double* out_sum, double* 
                   illume_render_stats* stats) {
   CHECK_ARG(r, "null renderer");
   auto t0 = std::chrono::steady_clock::now();
-  int st = illume_render_device(r, 0, stats);
+  int st = r->r.render_device(false, stats);
   if (st != ILLUME_OK) return st;
   st = r->r.read(out_mean, out_sum, out_sumsq, out_rgb8);
   if (st != ILLUME_OK) return st;
@@ -253,7 +281,7 @@ int illume_render(illume_renderer* r, float* out_mean, double* out_sum, double* 
     const size_t n = 3 * (size_t)r->r.npix;
     stats->d2h_bytes += (out_mean ? 4 * n : 0) + (out_sum ? 8 * n : 0) + (out_sumsq ? 8 * n : 0) + (out_rgb8 ? n : 0);
   }
-  return ILLUME_OK;
+  return traversal_status(r);
 }
 
 int illume_render_to_bitmap(illume_renderer* r, illume_bitmap* bitmap, illume_render_stats* stats) {
@@ -262,13 +290,13 @@ int illume_render_to_bitmap(illume_renderer* r, illume_bitmap* bitmap, illume_re
             "bitmap size differs from the renderer's resolution");
   std::vector<uint8_t> rgb(3 * (size_t)r->r.npix);
   const int st = illume_render(r, nullptr, nullptr, nullptr, rgb.data(), stats);
-  if (st != ILLUME_OK) return st;
+  if (st != ILLUME_OK && st != ILLUME_ERR_TRAVERSAL) return st;
   for (size_t i = 0; i < (size_t)r->r.npix; ++i) {
     bitmap->pixels[i].red = rgb[3 * i];
     bitmap->pixels[i].green = rgb[3 * i + 1];
     bitmap->pixels[i].blue = rgb[3 * i + 2];
   }
-  return ILLUME_OK;
+  return st;
 }
 
 illume_bitmap* illume_bitmap_new(size_t width, size_t height) {

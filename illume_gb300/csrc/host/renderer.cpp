@@ -44,6 +44,11 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if (p.engines < 0 || p.engines > 16) { *err = "engines out of range (0-16)"; return ILLUME_ERR_INVALID; }
   if (p.estimator < ILLUME_ESTIMATOR_REFERENCE || p.estimator > ILLUME_ESTIMATOR_NEE) { *err = "unknown estimator"; return ILLUME_ERR_INVALID; }
   if ((int)scene.t_mediums.size() > kMaxMediums) { *err = "too many mediums"; return ILLUME_ERR_UNSUPPORTED; }
+  // the 8-wide kernels push up to two stack entries per level (a triangle group and a
+  // node group); upload bounds the binary and 4-wide trees the same way
+  if (p.bvh_kind == ILLUME_BVH_WIDE8 || p.bvh_kind == ILLUME_BVH_WIDE8_PERSISTENT)
+    for (const MeshBvh& b : scene.bvhs)
+      if (2 * b.stats.wide_depth > 60) { *err = "8-wide BVH deeper than the traversal stack"; return ILLUME_ERR_UNSUPPORTED; }
   if (!scene.ctx || !scene.view_dev) { *err = "scene has not been uploaded to a device"; return ILLUME_ERR_INVALID; }
   return ILLUME_OK;
 }
@@ -207,11 +212,17 @@ int Renderer::render_device(bool accumulate, illume_render_stats* stats) {
     if ((s = eng.run(npasses, p.max_depth)) != ILLUME_OK) return s;
   }
   ILLUME_CUDA_TRY(cudaEventRecord(ev1, st));
-  for (int e = 0; e < nengines; ++e)
+  std::vector<int> drops(nengines, 0);
+  for (int e = 0; e < nengines; ++e) {
     ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_after[e], reinterpret_cast<const char*>(engine(e).w.jobs) + rays_off, 8,
                                     cudaMemcpyDeviceToHost, st));
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&drops[e], engine(e).w.counters + kCounterStackDrops, sizeof(int),
+                                    cudaMemcpyDeviceToHost, st));
+  }
   ILLUME_CUDA_TRY(cudaStreamSynchronize(st));
   ILLUME_CUDA_TRY(cudaGetLastError());
+  stack_overflow = false;
+  for (int e = 0; e < nengines; ++e) stack_overflow = stack_overflow || drops[e] != 0;
   samples_done += spp;
   next_sample += spp;
   if (stats) {
@@ -225,7 +236,7 @@ int Renderer::render_device(bool accumulate, illume_render_stats* stats) {
     stats->kernel_launches = (int64_t)npasses * Engine::launches_per_pass(p.max_depth, p.estimator == ILLUME_ESTIMATOR_NEE);
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
     stats->h2d_bytes = 4 * sizeof(int);
-    stats->d2h_bytes = 16;
+    stats->d2h_bytes = 16 + sizeof(int) * (size_t)nengines;
   }
   return ILLUME_OK;
 }

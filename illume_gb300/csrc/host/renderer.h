@@ -38,6 +38,9 @@ struct Renderer {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   long long samples_done = 0;   // samples accumulated since the last clear
   int next_sample = 0;          // first sample of the next progressive call
+  // set by render_device when a traversal of the call found its stack full (the kernels'
+  // defect flag, kCounterStackDrops): the image is complete but may lack hits
+  bool stack_overflow = false;
 
   ~Renderer();
   int init(std::string* err);

@@ -363,7 +363,7 @@ int Scene::build_host(std::string* err) {
       return ILLUME_ERR_UNSUPPORTED;
     }
   bvhs.assign(nm, MeshBvh{});
-  const int nthreads = std::max(1, std::min<int>(nm, (int)std::thread::hardware_concurrency()));
+  const int nthreads = std::max(1, std::min<int>(nm, build_threads()));
   std::vector<std::thread> pool;
   std::atomic<int> next{0};
   auto work = [&]() {

@@ -37,6 +37,13 @@ struct Context {
   int sm_count = 0;
   int l2_bytes = 0;
   std::atomic<long long> launches{0};
+  // illume_render_noalloc's set-up on this context: the device address of its fixed
+  // scratch array, the driver context it was looked up in, and grid sizes per kernel
+  // (trace by BVH kind and variant, shade by variant; 0 = not yet computed)
+  void* noalloc_scratch = nullptr;
+  void* noalloc_cu_ctx = nullptr;
+  int noalloc_grid_trace[4][5] = {};
+  int noalloc_grid_shade[5] = {};
 };
 
 // Device allocation charged against the context's budget.

@@ -370,6 +370,10 @@ int Server::retire(ServerEngine& se, std::vector<ServerJob*>* done) {
     ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays[k], reinterpret_cast<const char*>(e.w.jobs + r) + offsetof(JobDesc, rays), 8,
                                     cudaMemcpyDeviceToHost, st));
   }
+  // the table's traversal-overflow flag (kept across passes): every job it retires from
+  // then on reports it
+  int drops = 0;
+  ILLUME_CUDA_TRY(cudaMemcpyAsync(&drops, e.w.counters + kCounterStackDrops, sizeof(int), cudaMemcpyDeviceToHost, st));
   ILLUME_CUDA_TRY(cudaStreamSynchronize(st));
   for (size_t k = 0; k < rows_done.size(); ++k) {
     const int r = rows_done[k];
@@ -378,6 +382,9 @@ int Server::retire(ServerEngine& se, std::vector<ServerJob*>* done) {
     j->stats.rays = (int64_t)rays[k];
     j->stats.paths = (int64_t)p.spp * p.width * p.height;
     j->stats.d2h_bytes = (int64_t)(j->mean.size() * sizeof(float) + j->rgb8.size());
+    if (drops)
+      j->error = "a BVH traversal stack of the job's table overflowed: the image is written, but rays may have "
+                 "missed hits";
     j->sum32.release();
     j->comp32.release();
     j->sum64.release();
@@ -554,6 +561,7 @@ int Server::poll(int64_t id, float* mean, uint8_t* rgb8, illume_render_stats* st
   if (mean) memcpy(mean, j->mean.data(), sizeof(float) * j->mean.size());
   if (rgb8) memcpy(rgb8, j->rgb8.data(), j->rgb8.size());
   if (stats) *stats = j->stats;
+  if (!j->error.empty()) { set_error(j->error); return ILLUME_ERR_TRAVERSAL; }
   return ILLUME_OK;
 }
 

@@ -88,8 +88,11 @@ struct WaveBuffers {
 // counters[]: [0..1] queue sizes by parity, [2 + 16 * parity + class] event counts,
 // [kCounterPaths] paths of the pass, [kCounterPixels] pixels of the pass, [42] slot
 // overflow flag, [44 + parity] trace ray-fetch counters, [46 + parity] shadow-ray counts,
-// [48 + parity] shadow-ray fetch counters.
+// [48 + parity] shadow-ray fetch counters, [kCounterStackDrops] set when a traversal
+// found its stack full (kept across passes; cleared when the engine is made and read by
+// the renderer after each render).
 static constexpr int kCounterPaths = 40;
+static constexpr int kCounterStackDrops = 50;
 static constexpr int kCounterPixels = 41;
 static constexpr int kCounterWords = 64;
 

@@ -12,7 +12,10 @@
 // library reserves that array until the process exits. Host code cannot use the
 // array's name as a device address, so the first call on each device, with that device
 // current, asks the runtime for the array's address (cudaGetSymbolAddress) and caches
-// it; make that first call before any stream capture. The kernels are the same ones
+// it in the illume_context, with the launch grid sizes; make that first call before any
+// stream capture. A later call that finds another driver context current on the device
+// (the caller reset the device, which also invalidates every handle made before it)
+// looks the address up again. The kernels are the same ones
 // illume_render_device launches, pointed at slices of the array, one sample of every
 // pixel per pass, FP32 accumulation straight into the caller's output buffer.
 //
@@ -26,6 +29,7 @@
 
 #include "launch.h"
 #include "../host/handles.h"
+#include "../host/renderer.h"
 
 namespace illume {
 
@@ -37,7 +41,24 @@ static constexpr size_t kNoAllocScratchBytes = kNoAllocMaxPaths * kNoAllocPerPat
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[256];
+
+// The driver context current on the calling thread (cuCtxGetCurrent, reached through the
+// runtime so that the library does not link the driver library itself); null if the
+// entry point is unavailable.
+static void* current_driver_context() {
+  typedef int (*CtxGetCurrent)(void**);
+  static CtxGetCurrent fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<CtxGetCurrent>(f);
+  }();
+  void* c = nullptr;
+  if (!fn || fn(&c) != 0) return nullptr;
+  return c;
+}
 
 // Clears what must start at zero (counters, ray and visit totals, the output sums) and
 // writes the one-row job table.
@@ -68,47 +89,59 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
   if (!ctx || !scene || !params || !d_sum) { set_error("null argument"); return ILLUME_ERR_INVALID; }
   if (scene->s.ctx != &ctx->c) { set_error("scene was not uploaded with this context"); return ILLUME_ERR_INVALID; }
   const illume_render_params& p = *params;
+  // the checks every render takes (sizes, kinds, variants, the medium-field limit of the
+  // queued rays), then the limits of this entry point
+  std::string err;
+  const int chk = check_render_params(p, scene->s, &err);
+  if (chk != ILLUME_OK) { set_error("illume_render_noalloc: " + err); return chk; }
   const long long npix = (long long)p.width * p.height;
-  if (p.width <= 0 || p.height <= 0 || npix > (long long)kNoAllocMaxPaths) {
+  if (npix > (long long)kNoAllocMaxPaths) {
     set_error("illume_render_noalloc: image of " + std::to_string(npix) + " pixels exceeds the fixed scratch limit of " +
               std::to_string(kNoAllocMaxPaths) + " pixels (use illume_render_device)");
     return ILLUME_ERR_INVALID;
   }
-  if (p.spp < 0 || p.max_depth < 0) { set_error("negative spp or depth"); return ILLUME_ERR_INVALID; }
   if (p.accum_mode != ILLUME_ACCUM_FP32) { set_error("illume_render_noalloc accumulates in FP32 only"); return ILLUME_ERR_INVALID; }
   if (p.estimator != ILLUME_ESTIMATOR_REFERENCE) {
     set_error("illume_render_noalloc runs the reference estimator only (no shadow-ray scratch)");
     return ILLUME_ERR_UNSUPPORTED;
   }
-  if (p.intersector != ILLUME_ISECT_MT && p.intersector != ILLUME_ISECT_WATERTIGHT) { set_error("unknown intersector"); return ILLUME_ERR_INVALID; }
-  if (p.bvh_kind != ILLUME_BVH_BINARY && p.bvh_kind != ILLUME_BVH_WIDE8 && p.bvh_kind != ILLUME_BVH_WIDE4) {
-    set_error("unknown BVH kind");
-    return ILLUME_ERR_INVALID;
+  if (p.samples_per_pass > 1 || p.engines > 1) {
+    set_error("illume_render_noalloc renders one sample per pass on one engine (samples_per_pass and engines must be 0 or 1)");
+    return ILLUME_ERR_UNSUPPORTED;
   }
+  const RenderKnobs k = render_knobs(p);
   const int dev = ctx->c.device;
-  if (dev < 0 || dev >= 256) { set_error("device index out of range"); return ILLUME_ERR_INVALID; }
   ILLUME_CUDA_TRY(cudaSetDevice(dev));
   void* base = nullptr;
+  int grid_trace = 0, grid_shade = 0;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    void* cu_ctx = current_driver_context();
+    if (!ctx->c.noalloc_scratch || cu_ctx != ctx->c.noalloc_cu_ctx) {
       void* ptr = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
       if (e != cudaSuccess || !ptr) {
         set_error(std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
         return ILLUME_ERR_CUDA;
       }
-      g_noalloc_ptr[dev] = ptr;
+      ctx->c.noalloc_scratch = ptr;
+      ctx->c.noalloc_cu_ctx = cu_ctx;
     }
-    base = g_noalloc_ptr[dev];
+    base = ctx->c.noalloc_scratch;
+    int& gt = ctx->c.noalloc_grid_trace[k.bvh_kind & 3][k.trace_variant % 5];
+    if (!gt) gt = kernel_grid_blocks(trace_kernel_ptr(k.bvh_kind, k.trace_variant), 128, dev);
+    int& gs = ctx->c.noalloc_grid_shade[k.shade_variant % 5];
+    if (!gs) gs = kernel_grid_blocks(shade_kernel_ptr(k.shade_variant), 128, dev);
+    grid_trace = gt;
+    grid_shade = gs;
   }
   const int cap = (int)npix;
   unsigned char* cur = static_cast<unsigned char*>(base);
   WaveBuffers w{};
-  for (int k = 0; k < 2; ++k) {
-    w.q_orig[k] = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
-    w.q_dir[k] = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
-    w.q_thr[k] = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
+  for (int q = 0; q < 2; ++q) {
+    w.q_orig[q] = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
+    w.q_dir[q] = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
+    w.q_thr[q] = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
   }
   w.hit = reinterpret_cast<float4*>(carve(cur, sizeof(float4) * cap));
   w.hit_geom = reinterpret_cast<int*>(carve(cur, sizeof(int) * cap));
@@ -133,14 +166,8 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
   row.sample_end = p.sample_begin + p.spp;
   row.per_pass = 1;
   row.nsamples = p.spp > 0 ? 1 : 0;
-  RenderKnobs k{};
-  k.isect = p.intersector;
-  k.bvh_kind = p.bvh_kind == ILLUME_BVH_WIDE4 ? BVH_WIDE4 : p.bvh_kind;
-  k.trace_variant = 0;
   cudaStream_t st = ctx->c.stream;
   const int sms = ctx->c.sm_count > 0 ? ctx->c.sm_count : 1;
-  const int grid_trace = kernel_grid_blocks(trace_kernel_ptr(k.bvh_kind, 0), 128, dev);
-  const int grid_shade = kernel_grid_blocks(shade_kernel_ptr(0), 128, dev);
   const int grid_small = std::max(1, std::min((cap + 255) / 256, sms * 8));
   k_noalloc_begin<<<grid_small, 256, 0, st>>>(w.counters, w.rays, w.visits, w.jobs, row, d_sum, cap);
   for (int s = 0; s < p.spp; ++s) {

@@ -105,8 +105,10 @@ __device__ __forceinline__ float tri_wt(V3 v0, V3 v1, V3 v2, const TraceRay& r, 
 
 struct MeshBest { float t; int prim; float u, v; };
 
-// Visit counters of the instrumented trace kernel (node fetches, triangle tests).
-struct VisitCount { unsigned nodes = 0, tris = 0; };
+// Visit counters of the instrumented trace kernel (node fetches, triangle tests), and
+// whether a push found the traversal stack full (the entry is dropped, so the ray may
+// miss a hit; scene upload rejects trees deep enough for that, so it is a defect flag).
+struct VisitCount { unsigned nodes = 0, tris = 0; bool dropped = false; };
 
 __device__ __forceinline__ void test_triangle(const float4* tv, int isect, const TraceRay& r, MeshBest& b) {
   const float4 a = __ldg(tv), bb = __ldg(tv + 1), c = __ldg(tv + 2);
@@ -196,6 +198,7 @@ __device__ __forceinline__ void traverse_bvh2(const DevMesh& m, const TraceRay& 
       const bool swap = te1 < te0;
       node = swap ? inner1 : inner0;
       if (sp < kStack) stack[sp++] = swap ? inner0 : inner1;
+      else vc.dropped = true;
       continue;
     }
     if (inner0 >= 0) { node = inner0; continue; }
@@ -238,7 +241,10 @@ __device__ __forceinline__ void ww_round(const DevMesh& m, const TraceRay& r, in
     if (c0 == kEmpty) { c0 = c1; c1 = kEmpty; }
     if (c0 != kEmpty) {
       cur = c0;
-      if (c1 != kEmpty && sp < kStack) stack[sp++] = c1;
+      if (c1 != kEmpty) {
+        if (sp < kStack) stack[sp++] = c1;
+        else vc.dropped = true;
+      }
     } else {
       cur = sp > 0 ? stack[--sp] : kEmpty;
     }
@@ -322,6 +328,7 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
                  near_z = r.idir.z >= 0.0f ? 32u : 80u;
   auto push = [&](int v) {
     if (sp < kStack) stack[sp++] = v;
+    else vc.dropped = true;
   };
   auto pop = [&]() -> int { return stack[--sp]; };
   do {
@@ -445,7 +452,10 @@ __device__ __forceinline__ void traverse_wide(const DevMesh& m, const TraceRay& 
       pending &= pending - 1;
       const int slot = k ^ r.oct;
       node = child_base + __popc(imask & ((1u << slot) - 1));
-      if (pending && sp < kStack) stack[sp++] = make_uint2(child_base, (imask << 8) | pending);
+      if (pending) {
+        if (sp < kStack) stack[sp++] = make_uint2(child_base, (imask << 8) | pending);
+        else vc.dropped = true;
+      }
       continue;
     }
     // pop the next pending child of a stacked group
@@ -546,7 +556,10 @@ __device__ __forceinline__ void wide_node_step(const DevMesh& m, const TraceRay&
     }
   }
   if (tmask) {
-    if (s.tri_mask && s.sp < kStack) stack[s.sp++] = make_uint2(s.tri_base, s.tri_mask | kTriGroup);
+    if (s.tri_mask) {
+      if (s.sp < kStack) stack[s.sp++] = make_uint2(s.tri_base, s.tri_mask | kTriGroup);
+      else vc.dropped = true;
+    }
     s.tri_base = tri_base;
     s.tri_mask = tmask;
   }
@@ -554,7 +567,10 @@ __device__ __forceinline__ void wide_node_step(const DevMesh& m, const TraceRay&
     const int k = __ffs(pending) - 1;
     pending &= pending - 1;
     s.fetch = child_base + __popc(imask & ((1u << (k ^ r.oct)) - 1));
-    if (pending && s.sp < kStack) stack[s.sp++] = make_uint2(child_base, (imask << 8) | pending);
+    if (pending) {
+      if (s.sp < kStack) stack[s.sp++] = make_uint2(child_base, (imask << 8) | pending);
+      else vc.dropped = true;
+    }
   } else {
     s.fetch = kNoNode;
   }
@@ -614,7 +630,10 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }
     if (ANY && h.geom != -1) break;
   }
-  if (COUNT && vcp) *vcp = vc;
+  if (vcp) {
+    if (COUNT) *vcp = vc;
+    else vcp->dropped = vc.dropped;
+  }
   return h;
 }
 

@@ -86,6 +86,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
       const unsigned longest = __reduce_max_sync(mask, (unsigned)vc.nodes);
       if (lane == __ffs(mask) - 1) my_slots += 32ull * longest;
     }
+    if (vc.dropped) atomicOr(w.counters + kCounterStackDrops, 1);
     const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
     w.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
     w.hit_geom[i] = h.geom;
@@ -220,6 +221,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_refill(WaveBuffers w, RenderKn
       slot = -1;
     }
   }
+  if (vc.dropped) atomicOr(w.counters + kCounterStackDrops, 1);
   if (COUNT) {
     unsigned long long my_nodes = vc.nodes, my_tris = vc.tris;
     for (int off = 16; off > 0; off >>= 1) {
@@ -261,9 +263,11 @@ __global__ void __launch_bounds__(128, 8) k_shadow(WaveBuffers w, RenderKnobs k,
     const float4 so = w.s_orig[i], sd = w.s_dir[i], sv = w.s_val[i];
     const int job = __float_as_int(so.w);
     const SceneView& sc = w.jobs[job].sc;
+    VisitCount vc;
     const HitRecord h =
         closest_hit<KIND, false, KIND == BVH_BINARY, KIND == BVH_BINARY, KIND != BVH_WIDE8, false, KIND == BVH_WIDE4>(
-            sc, v3(so.x, so.y, so.z), v3(sd.x, sd.y, sd.z), k.isect, stack, nullptr, sd.w);
+            sc, v3(so.x, so.y, so.z), v3(sd.x, sd.y, sd.z), k.isect, stack, &vc, sd.w);
+    if (vc.dropped) atomicOr(w.counters + kCounterStackDrops, 1);
     if (h.geom == -1) {
       float4* c = w.contrib + __float_as_int(sv.w);
       const float4 v = *c;
@@ -405,6 +409,7 @@ __global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, const SceneView
       slot = -1;
     }
   }
+  if (!HOOK && vc.dropped) atomicOr(w.counters + kCounterStackDrops, 1);
   if (COUNT) {
     unsigned long long my_nodes = vc.nodes, my_tris = vc.tris;
     for (int off = 16; off > 0; off >>= 1) {

@@ -40,7 +40,10 @@ enum illume_status {
   ILLUME_ERR_TIMEOUT = -7,     /* a bounded device wait ran out */
   ILLUME_ERR_CANCELLED = -8,   /* job cancelled */
   ILLUME_ERR_UNSUPPORTED = -9, /* feature not available in this build */
-  ILLUME_ERR_NOT_READY = -10   /* job still running (illume_job_poll) */
+  ILLUME_ERR_NOT_READY = -10,  /* job still running (illume_job_poll) */
+  ILLUME_ERR_TRAVERSAL = -11   /* a BVH traversal stack overflowed: the render's outputs are
+                                * written but rays may have missed hits (scene upload rejects
+                                * trees deep enough for this, so it reports a defect) */
 };
 
 /* ---- enumerations shared with the JSON scene format ---- */
@@ -234,6 +237,11 @@ int illume_scene_upload(illume_scene* scene, size_t* bytes);
  * boxes inside their parent's, quantised boxes containing the exact boxes) and writes a
  * one-line summary per mesh (node counts, depths) into report. */
 int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t report_len);
+/* Test hook: 64-bit FNV-1a digests of mesh `mesh`'s built layouts, in the order binary
+ * nodes, 4-wide nodes, triangle records of both, 8-wide nodes with their triangle
+ * records. Equal digests = bit-identical trees (the build's thread count, set by the
+ * environment variable ILLUME_BUILD_THREADS, does not change them). */
+int illume_scene_bvh_digest(const illume_scene* scene, int mesh, uint64_t out[4]);
 /* Process-wide cache of mesh BVH builds, keyed by mesh content (vertex and index words):
  * scenes that share a mesh build it once. Not in the reference, which caches one BVH
  * file per OBJ path (src/accel/bvh.cpp:363-439). */
@@ -291,9 +299,13 @@ int illume_renderer_profile(illume_renderer* r, int count_visits, illume_profile
  * images are rejected with ILLUME_ERR_INVALID. Renders params->spp samples (one per
  * pass, FP32 accumulation in sample order, accum_mode must be ILLUME_ACCUM_FP32) and
  * writes the per-pixel sum of radiance (3 floats per pixel) to the caller's device
- * buffer d_sum. Asynchronous on the context's stream. The first call on a device looks
- * up the array's device address; make it before any stream capture. All calls share the
- * array: calls whose GPU work overlaps race, so order them on one stream. */
+ * buffer d_sum. Asynchronous on the context's stream. Takes the parameter checks of
+ * illume_renderer_create; samples_per_pass and engines above 1 and the next-event
+ * estimator are rejected with ILLUME_ERR_UNSUPPORTED. The first call on a context looks
+ * up the array's device address and caches it with the launch sizes; make it before any
+ * stream capture. After a device reset (which invalidates every handle) the address is
+ * looked up again. All calls share the array: calls whose GPU work overlaps race, so
+ * order them on one stream. */
 #define ILLUME_NOALLOC_MAX_PIXELS 65536
 int illume_render_noalloc(illume_context* ctx, illume_scene* scene, const illume_render_params* params, float* d_sum);
 

@@ -5,8 +5,9 @@ one g++ translation unit through oracle/ref_driver.cpp with the host shim header
 oracle/ref_shim/, into oracle/_ref/libillume_ref.so. The library pins the oracle and
 generates the golden fixtures of tests/golden/. Outputs go only into oracle/_ref/.
 
-Only possible where the reference checkout exists (the build container). Returns None
-when it does not.
+Only possible where the reference checkout exists: its root is read from the
+environment variable ILLUME_REFERENCE_ROOT, else the build container's checkout path.
+Returns None when there is no checkout there.
 
 Scenes are loaded from a scratch copy of the needed OBJ files under oracle/_ref/work,
 because the reference writes a BVH cache file next to every OBJ it loads
@@ -19,7 +20,7 @@ import shutil
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+REF_ROOT = os.environ.get("ILLUME_REFERENCE_ROOT", "/root/reference")
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB_PATH = os.path.join(OUT_DIR, "libillume_ref.so")
 WORK_DIR = os.path.join(OUT_DIR, "work")

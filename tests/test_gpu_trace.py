@@ -112,3 +112,19 @@ def test_empty_and_miss(ctx):
     h = scene.trace_closest(r)
     assert h["inst"][0] == -1 and h["sphere"][0] == -1 and h["t"][0] == np.finfo(np.float32).max
     assert h["inst"][1] == 2        # back wall
+
+
+@pytest.mark.parametrize("bvh", [C.BVH_WIDE4, C.BVH_BINARY])
+def test_full_ray_sets_on_the_benchmark_mesh(ctx, bvh):
+    """2^20 seeded rays (origins in the scene box inflated 10%, directions on the sphere,
+    with axis-parallel shares and origins on mesh vertices) plus the 2^20 primary rays of
+    the 1024x1024 camera, on the 100k-triangle traversal scene: bit-exact against the
+    oracle, watertight test."""
+    from illume_gb300 import synth
+    from oracle import pyoracle
+    sd = synth.traversal_scene(tris=100_000, env_size=(16, 8), width=1024, height=1024)
+    compare(sd, ray_set(sd, 1 << 20, seed=3), ctx, bvh, C.ISECT_WATERTIGHT)
+    cam = pyoracle.OracleScene(sd).camera_rays(1024, 1024, sample=0)
+    assert len(cam) == 1 << 20
+    hits = compare(sd, rays6_to_8(cam), ctx, bvh, C.ISECT_WATERTIGHT)
+    assert hits > (1 << 18)

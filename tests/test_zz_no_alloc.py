@@ -5,8 +5,10 @@ instead of allocating, so its images must equal those of the allocating entry po
 
 Checked through the C-ABI against illume_render (same scene, parameters and Philox
 streams, FP32 accumulation in sample order) on two calls in a row, the second on a
-different scene and size so that leftovers of the first call would show; plus the size
-limit. This file is collected last.
+different scene and size so that leftovers of the first call would show; on every BVH
+layout with both triangle tests; on the golden scene with a participating medium (the
+medium index travels packed beside the job row in the queued rays); plus the size limit
+and the parameters this entry point does not take. This file is collected last.
 """
 import ctypes
 
@@ -55,6 +57,56 @@ def test_noalloc_matches_render_on_two_calls(ctx):
         assert np.isfinite(got).all()
         np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
         scene.close()
+
+
+@pytest.mark.parametrize("bvh", [C.BVH_BINARY, C.BVH_WIDE8, C.BVH_WIDE8_PERSISTENT, C.BVH_WIDE4])
+@pytest.mark.parametrize("isect", [C.ISECT_MT, C.ISECT_WATERTIGHT])
+def test_noalloc_matches_render_per_layout(ctx, bvh, isect):
+    from illume_gb300 import synth
+    from illume_gb300.api import HostScene
+    scene = HostScene.from_data(ctx, synth.traversal_scene(tris=3000, env_size=(64, 32)))
+    p = scene.default_params(2, 8)
+    p.width, p.height = 32, 32
+    p.accum_mode = C.ACCUM_FP32
+    p.bvh_kind, p.intersector = bvh, isect
+    want = reference_sums(ctx, scene, p)
+    got = noalloc_sums(ctx, scene, p)
+    np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
+    scene.close()
+
+
+def test_noalloc_matches_render_with_a_medium(ctx):
+    from conftest import golden_scene
+    from illume_gb300.api import HostScene
+    sd = golden_scene("materials")
+    assert len(sd.mediums) > 0
+    scene = HostScene.from_data(ctx, sd)
+    p = scene.default_params(4, 12)
+    p.width, p.height = 40, 30
+    p.accum_mode = C.ACCUM_FP32
+    want = reference_sums(ctx, scene, p)
+    got = noalloc_sums(ctx, scene, p)
+    np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
+    scene.close()
+
+
+def test_noalloc_rejects_what_it_does_not_take(ctx):
+    from illume_gb300 import synth
+    from illume_gb300.api import HostScene
+    import torch
+    scene = HostScene.from_data(ctx, synth.cornell_scene(8, 8))
+    out = torch.zeros(3 * 64, dtype=torch.float32, device="cuda:0")
+    L = C.lib()
+    for field, value, status in [("samples_per_pass", 4, C.ERR_UNSUPPORTED), ("engines", 2, C.ERR_UNSUPPORTED),
+                                 ("trace_variant", 9, C.ERR_INVALID), ("shade_variant", 9, C.ERR_INVALID),
+                                 ("accum_mode", C.ACCUM_FP64, C.ERR_INVALID)]:
+        p = scene.default_params(1, 4)
+        p.width, p.height = 8, 8
+        p.accum_mode = C.ACCUM_FP32
+        setattr(p, field, value)
+        st = L.illume_render_noalloc(ctx.handle, scene.handle, ctypes.byref(p), ctypes.c_void_p(out.data_ptr()))
+        assert st == status, (field, st)
+    scene.close()
 
 
 def test_noalloc_rejects_images_beyond_the_scratch_limit(ctx):
