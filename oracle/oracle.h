@@ -606,6 +606,7 @@ struct RenderParams {
   uint32_t seed, job;
   int isect;      // ISECT_MT / ISECT_WATERTIGHT
   int exact_hg;   // 0 = reference HG sampler, 1 = exact
+  int nee;        // EXTENSION: 1 = next-event estimation with MIS (needs the scene's light tables)
 };
 
 struct CameraSetup { float pixel_size, left, top; };
@@ -781,11 +782,343 @@ static inline ScatterOut<R> scatter(const Material& mat, V3<R> d, V3<R> N, V3<R>
   }
 }
 
+// ---- EXTENSION: next-event estimation with multiple importance sampling ----
+//
+// The library's opt-in estimator (the reference finds light only by BSDF sampling,
+// src/renderer.cu:183-386). At a lambert, rough conductor or rough dielectric reflection
+// vertex in air that is not the path's last, one light is sampled from a separate
+// Philox stream (counter slot 0x40000000 | bounce): the environment (probability 1/2
+// when emissive mesh triangles exist too; a row by its weight, then a texel of the row,
+// uniform within the texel; density luminance x cos(elevation), floored at 1e-4 of the
+// largest texel weight) or an emissive mesh triangle (chosen by world-space area x the
+// emitter's luminance, uniform point). Choices go through Walker alias tables built by
+// Vose's method. The sample's contribution, weighted by the power heuristic against the
+// BSDF's own density, is added when the shadow ray finds nothing closer than the light.
+// A BSDF-sampled continuation that then escapes or reaches an emissive mesh triangle is
+// weighted by the power heuristic against the light density; after delta or
+// transmissive interactions, in media and for emissive spheres the weight is 1.
+
+struct AliasSlot { float prob; int alias; };
+
+// Vose's alias method (Vose, IEEE TSE 1991): slots whose scaled weight is below 1 take
+// the rest of their probability from a slot above 1, both lists worked from the back.
+// Slots left at the end keep themselves with probability 1. Zero total weight: every
+// slot keeps itself.
+static inline void alias_build(const double* w, size_t n, AliasSlot* out) {
+  double total = 0.0;
+  for (size_t i = 0; i < n; ++i) total += std::max(w[i], 0.0);
+  for (size_t i = 0; i < n; ++i) out[i] = AliasSlot{1.0f, (int)i};
+  if (!(total > 0.0) || n == 0) return;
+  std::vector<double> q(n);
+  std::vector<size_t> lo, hi;
+  for (size_t i = 0; i < n; ++i) {
+    q[i] = std::max(w[i], 0.0) * (double)n / total;
+    if (q[i] < 1.0) lo.push_back(i); else hi.push_back(i);
+  }
+  while (!lo.empty() && !hi.empty()) {
+    const size_t a = lo.back(), b = hi.back();
+    lo.pop_back();
+    out[a] = AliasSlot{(float)q[a], (int)b};
+    q[b] = (q[b] + q[a]) - 1.0;
+    if (q[b] < 1.0) { hi.pop_back(); lo.push_back(b); }
+  }
+  for (size_t i : hi) out[i] = AliasSlot{1.0f, (int)i};
+  for (size_t i : lo) out[i] = AliasSlot{1.0f, (int)i};
+}
+
+// Slot chosen by u in [0, 1); frac = the rest of u's randomness, uniform given the slot.
+static inline int alias_pick(const AliasSlot* t, int n, float u, float& frac) {
+  const float x = u * (float)n;
+  const int i = std::min(std::max((int)x, 0), n - 1);
+  const float f = fminf(fmaxf(x - (float)i, 0.0f), 0.99999994f);
+  if (f < t[i].prob) {
+    frac = fminf(f / t[i].prob, 0.99999994f);
+    return i;
+  }
+  frac = fminf((f - t[i].prob) / (1.0f - t[i].prob), 0.99999994f);
+  return t[i].alias;
+}
+
+struct LightTables {
+  int env_w = 0, env_h = 0;
+  std::vector<float> env_func;            // texel weights, row-major
+  std::vector<AliasSlot> env_rows, env_cols;
+  float env_integral = 0.0f;              // mean texel weight
+  float env_prob = 0.0f;                  // probability of choosing the environment
+  struct Tri { float v0[3], area, e1[3], psel, e2[3]; int inst; };
+  std::vector<Tri> tris;                  // world-space emissive triangles
+  std::vector<AliasSlot> tri_alias;
+  std::vector<int> inst_base;             // per instance: its first light triangle, -1 if none
+};
+
+static inline float luminance_f(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+
+static inline LightTables build_light_tables(const Scene& sc) {
+  LightTables L;
+  // environment
+  const int id = sc.env_tex;
+  if (id >= 0 && id < (int)sc.textures.size()) {
+    const Texture& t = sc.textures[id];
+    int w = 0, h = 0;
+    std::vector<float> lum;
+    if (t.type == TEX_BITMAP && t.scale[0] == 1.0f && t.scale[1] == 1.0f && t.width > 0 && t.height > 0) {
+      w = t.width;
+      h = t.height;
+      const float s = t.hdr ? 1.0f : 1.0f / 255.0f;
+      lum.resize((size_t)w * h);
+      for (size_t i = 0; i < lum.size(); ++i) lum[i] = s * luminance_f(t.texels[4 * i], t.texels[4 * i + 1], t.texels[4 * i + 2]);
+    } else if (t.type == TEX_CONSTANT) {
+      w = h = 1;
+      lum.assign(1, luminance_f(t.c[0], t.c[1], t.c[2]));
+    }
+    if (w > 0) {
+      std::vector<double> f((size_t)w * h);
+      double fmax = 0.0;
+      for (int y = 0; y < h; ++y) {
+        const double c = cos((0.5 - (y + 0.5) / h) * kPi);
+        for (int x = 0; x < w; ++x) {
+          f[(size_t)y * w + x] = std::max(0.0, (double)lum[(size_t)y * w + x]) * c;
+          fmax = std::max(fmax, f[(size_t)y * w + x]);
+        }
+      }
+      if (fmax > 0.0) {
+        for (int y = 0; y < h; ++y) {
+          const double c = cos((0.5 - (y + 0.5) / h) * kPi);
+          for (int x = 0; x < w; ++x) f[(size_t)y * w + x] = std::max(f[(size_t)y * w + x], 1e-4 * fmax * c);
+        }
+        L.env_w = w;
+        L.env_h = h;
+        L.env_cols.resize((size_t)w * h);
+        L.env_rows.resize(h);
+        L.env_func.resize((size_t)w * h);
+        std::vector<double> rows(h);
+        double total = 0.0;
+        for (int y = 0; y < h; ++y) {
+          alias_build(&f[(size_t)y * w], w, &L.env_cols[(size_t)y * w]);
+          double r = 0.0;
+          for (int x = 0; x < w; ++x) r += f[(size_t)y * w + x];
+          rows[y] = r;
+          total += r;
+        }
+        alias_build(rows.data(), h, L.env_rows.data());
+        for (size_t i = 0; i < f.size(); ++i) L.env_func[i] = (float)f[i];
+        L.env_integral = (float)(total / ((double)w * h));
+      }
+    }
+  }
+  // emissive mesh triangles, world space
+  L.inst_base.assign(sc.instances.size(), -1);
+  std::vector<double> weight;
+  for (int i = 0; i < (int)sc.instances.size(); ++i) {
+    const Instance& in = sc.instances[i];
+    const Material& mat = sc.materials[in.material];
+    if (mat.type != MAT_EMISSIVE) continue;
+    float col[3] = {1.0f, 1.0f, 1.0f};
+    if (mat.albedo_tex >= 0 && mat.albedo_tex < (int)sc.textures.size() && sc.textures[mat.albedo_tex].type == TEX_CONSTANT)
+      for (int c = 0; c < 3; ++c) col[c] = sc.textures[mat.albedo_tex].c[c];
+    const double lw = std::max(1e-6, (double)luminance_f(col[0], col[1], col[2]));
+    const Mesh& m = sc.meshes[in.mesh];
+    L.inst_base[i] = (int)L.tris.size();
+    for (int t = 0; t < m.num_tris; ++t) {
+      double v[3][3];
+      for (int k = 0; k < 3; ++k) {
+        const float* p = m.positions + 3 * (size_t)m.tris[3 * t + k];
+        for (int r = 0; r < 3; ++r)
+          v[k][r] = (double)in.mat.m[r][0] * p[0] + (double)in.mat.m[r][1] * p[1] + (double)in.mat.m[r][2] * p[2] +
+                    in.mat.m[r][3];
+      }
+      const double e1[3] = {v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2]};
+      const double e2[3] = {v[2][0] - v[0][0], v[2][1] - v[0][1], v[2][2] - v[0][2]};
+      const double cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2],
+                   cz = e1[0] * e2[1] - e1[1] * e2[0];
+      const double area = 0.5 * sqrt(cx * cx + cy * cy + cz * cz);
+      LightTables::Tri T;
+      for (int r = 0; r < 3; ++r) { T.v0[r] = (float)v[0][r]; T.e1[r] = (float)e1[r]; T.e2[r] = (float)e2[r]; }
+      T.area = (float)area;
+      T.psel = 0.0f;
+      T.inst = i;
+      L.tris.push_back(T);
+      weight.push_back(area * lw);
+    }
+  }
+  double total = 0.0;
+  for (double x : weight) total += x;
+  if (!(total > 0.0)) {
+    L.tris.clear();
+    for (int& b : L.inst_base) b = -1;
+  } else {
+    L.tri_alias.resize(weight.size());
+    alias_build(weight.data(), weight.size(), L.tri_alias.data());
+    for (size_t k = 0; k < weight.size(); ++k) L.tris[k].psel = (float)(weight[k] / total);
+  }
+  const bool env = L.env_w > 0, tri = !L.tri_alias.empty();
+  L.env_prob = env && tri ? 0.5f : (env ? 1.0f : 0.0f);
+  return L;
+}
+
+static const float kTwoPiSqF = 19.7392088021787172f;   // 2 pi^2
+
+template <class R> static inline R power_heuristic(R a, R b) {
+  const R a2 = a * a, b2 = b * b;
+  return a2 + b2 > (R)0 ? a2 / (a2 + b2) : (R)0;
+}
+
+// Environment radiance of direction d, the miss lookup of src/renderer.cu:378-386.
+template <class R> static inline V3<R> env_radiance(const Scene& sc, V3<R> d) {
+  if (sc.env_tex < 0) return v3<R>(0, 0, 0);
+  const R u = (R)((double)(m_atan2(d.z, d.x) * (R)0.5f) * kInvPi + 0.5);
+  const R v = (R)(0.5 - (double)m_asin(d.y) * kInvPi);
+  return tex_eval<R>(sc, sc.env_tex, u, v);
+}
+
+// Solid-angle density (with the choice probability) of the environment toward d.
+template <class R> static inline R env_light_pdf(const LightTables& L, V3<R> d) {
+  if (L.env_w == 0) return (R)0;
+  const R u = m_atan2(d.z, d.x) * ((R)0.5f * (R)(float)kInvPi) + (R)0.5f;
+  const R v = (R)0.5f - m_asin(m_min(m_max(d.y, (R)-1.0f), (R)1.0f)) * (R)(float)kInvPi;
+  const int x = std::min(std::max((int)(u * (R)L.env_w), 0), L.env_w - 1);
+  const int y = std::min(std::max((int)(v * (R)L.env_h), 0), L.env_h - 1);
+  const R ce = m_sqrt(m_max((R)1.0f - d.y * d.y, (R)0.0f));
+  if (ce < (R)1e-6f) return (R)0;
+  const R puv = (R)L.env_func[(size_t)y * L.env_w + x] / (R)L.env_integral;
+  return (R)L.env_prob * puv / ((R)kTwoPiSqF * ce);
+}
+
+// Solid-angle density of reaching light triangle l at distance t with cosine cos_l.
+template <class R> static inline R tri_light_pdf(const LightTables& L, int l, R t, R cos_l) {
+  if (l < 0 || m_abs(cos_l) < (R)1e-7f) return (R)0;
+  const R area = (R)L.tris[l].area, psel = (R)L.tris[l].psel;
+  if (!(area > (R)0)) return (R)0;
+  return ((R)1.0f - (R)L.env_prob) * psel * t * t / (area * m_abs(cos_l));
+}
+
+template <class R> struct LightSampleO { V3<R> dir; R dist; V3<R> Le; R pdf; bool ok; };
+
+// u0 picks the kind and the triangle, (u1, u2) the point.
+template <class R>
+static inline LightSampleO<R> sample_light(const Scene& sc, const LightTables& L, V3<R> p, R u0, R u1, R u2) {
+  LightSampleO<R> s;
+  s.ok = false;
+  s.pdf = 0;
+  s.dist = (R)FLT_MAX;
+  s.Le = v3<R>(0, 0, 0);
+  s.dir = v3<R>(0, 0, 1);
+  if (u0 < (R)L.env_prob) {
+    float ry, rx;
+    const int y = alias_pick(L.env_rows.data(), L.env_h, (float)u2, ry);
+    const int x = alias_pick(L.env_cols.data() + (size_t)y * L.env_w, L.env_w, (float)u1, rx);
+    const R u = ((R)x + (R)rx) / (R)L.env_w, v = ((R)y + (R)ry) / (R)L.env_h;
+    const R phi = (u - (R)0.5f) * (R)6.28318530717958648f;
+    const R elev = ((R)0.5f - v) * (R)3.14159265358979324f;
+    const R ce = m_cos(elev);
+    if (ce < (R)1e-6f) return s;
+    s.dir = v3<R>(ce * m_cos(phi), m_sin(elev), ce * m_sin(phi));
+    const R puv = (R)L.env_func[(size_t)y * L.env_w + x] / (R)L.env_integral;
+    s.pdf = (R)L.env_prob * puv / ((R)kTwoPiSqF * ce);
+    s.Le = env_radiance<R>(sc, s.dir);
+    s.ok = s.pdf > (R)0;
+    return s;
+  }
+  if (L.tris.empty()) return s;
+  const R ut = (u0 - (R)L.env_prob) / ((R)1.0f - (R)L.env_prob);
+  float rest;
+  const int l = alias_pick(L.tri_alias.data(), (int)L.tris.size(), fminf(fmaxf((float)ut, 0.0f), 0.99999994f), rest);
+  const LightTables::Tri& T = L.tris[l];
+  const V3<R> a = v3<R>(T.v0[0], T.v0[1], T.v0[2]), e1 = v3<R>(T.e1[0], T.e1[1], T.e1[2]),
+              e2 = v3<R>(T.e2[0], T.e2[1], T.e2[2]);
+  const R su = m_sqrt(u1);
+  const R b1 = (R)1.0f - su, b2 = u2 * su;
+  const V3<R> q = add(a, add(mul(e1, b1), mul(e2, b2)));
+  const V3<R> to = sub(q, p);
+  const R d2 = dot(to, to);
+  if (!(d2 > (R)0)) return s;
+  const R dist = m_sqrt(d2);
+  s.dir = mul(to, (R)1.0f / dist);
+  s.dist = dist;
+  const V3<R> n = cross(e1, e2);
+  const R nl = m_sqrt(dot(n, n));
+  if (!(nl > (R)0)) return s;
+  const R cos_l = dot(n, s.dir) / nl;
+  s.pdf = tri_light_pdf<R>(L, l, dist, cos_l);
+  // emitted radiance: the emitter's albedo at the point, texcoords as in shading
+  const Instance& in = sc.instances[T.inst];
+  const Mesh& m = sc.meshes[in.mesh];
+  const int prim = l - L.inst_base[T.inst];
+  R uv0 = b1, uv1 = b2;
+  if (m.texcoords) {
+    const int* tri = m.tris + 3 * prim;
+    const float* tc = m.texcoords;
+    const R w0 = (R)1.0f - b1 - b2;
+    uv0 = (tc[2 * tri[0]] * w0 + tc[2 * tri[1]] * b1) + tc[2 * tri[2]] * b2;
+    uv1 = (tc[2 * tri[0] + 1] * w0 + tc[2 * tri[1] + 1] * b1) + tc[2 * tri[2] + 1] * b2;
+  }
+  s.Le = tex_eval<R>(sc, sc.materials[in.material].albedo_tex, uv0, uv1);
+  s.ok = s.pdf > (R)0;
+  return s;
+}
+
+// f x cos toward wl and the density the material's own sampling gives wl (lambert,
+// rough conductor, rough dielectric reflection); false for other lobes or no value.
+template <class R>
+static inline bool bsdf_eval_cos(const Material& mat, V3<R> d, V3<R> N, V3<R> albedo, R roughness, V3<R> wl, V3<R>& fcos,
+                                 R& pdf) {
+  const V3<R> norm_o = mul(N, dot(N, d) > (R)0 ? (R)-1.0f : (R)1.0f);
+  if (mat.type == MAT_DIFFUSE) {
+    const R c = dot(wl, norm_o);
+    if (c <= (R)0) return false;
+    fcos = mul(albedo, c * (R)(float)kInvPi);
+    pdf = c * (R)(float)kInvPi;
+    return true;
+  }
+  if (mat.type != MAT_ROUGHCONDUCTOR && mat.type != MAT_ROUGHREFLECTIVE) return false;
+  const V3<R> wi = mul(d, (R)-1.0f);
+  const R wiDotN = dot(wi, N), woDotN = dot(wl, N);
+  if (mat.type == MAT_ROUGHCONDUCTOR && wiDotN <= (R)0) return false;
+  if (wiDotN * woDotN <= (R)0) return false;
+  V3<R> m = add(wi, wl);
+  const R ml = m_sqrt(dot(m, m));
+  if (!(ml > (R)0)) return false;
+  m = mul(m, (R)1.0f / ml);
+  if (dot(m, N) < (R)0) m = mul(m, (R)-1.0f);
+  const bool ggx = mat.distribution == DIST_GGX;
+  const R a = ggx ? roughness : roughness * ((R)1.2f - (R)0.2f * m_sqrt(m_abs(wiDotN)));
+  const R D = ggx ? D_ggx(m, N, a) : D_beckmann(m, N, a);
+  const R G = ggx ? G_ggx(wi, wl, m, N, a) : G_beckmann(wi, wl, m, a);
+  const R woDotM = m_abs(dot(wl, m));
+  if (!(woDotM > (R)0) || !(D > (R)0)) return false;
+  pdf = D * m_abs(dot(m, N)) / ((R)4.0f * woDotM);
+  const R base = D * G / ((R)4.0f * m_abs(wiDotN));
+  if (mat.type == MAT_ROUGHCONDUCTOR) {
+    fcos = v3<R>(fresnel_conductor((R)mat.eta[0], (R)mat.k[0], wiDotN) * base,
+                 fresnel_conductor((R)mat.eta[1], (R)mat.k[1], wiDotN) * base,
+                 fresnel_conductor((R)mat.eta[2], (R)mat.k[2], wiDotN) * base);
+  } else {
+    R cosT = 0;
+    const R F = fresnel_dielectric(dot(wi, m), (R)mat.ior, cosT);
+    fcos = mul(albedo, F * base);
+  }
+  return std::isfinite((double)pdf) && pdf > (R)0;
+}
+
+// Density of the material's own sampling for the direction it just sampled.
+template <class R> static inline R bsdf_sampled_pdf(const Material& mat, const ScatterOut<R>& s, V3<R> d, V3<R> N) {
+  if (s.status != SCATTER_REFLECT) return (R)0;
+  if (mat.type == MAT_DIFFUSE) {
+    const V3<R> norm_o = mul(N, dot(N, d) > (R)0 ? (R)-1.0f : (R)1.0f);
+    return m_max(dot(normalize(s.dir), norm_o), (R)0) * (R)(float)kInvPi;
+  }
+  if (mat.type == MAT_ROUGHCONDUCTOR || mat.type == MAT_ROUGHREFLECTIVE) {
+    const R woDotM = m_abs(dot(normalize(s.dir), s.m));
+    return woDotM > (R)0 ? s.pdf_m / ((R)4.0f * woDotM) : (R)0;
+  }
+  return (R)0;
+}
+
 struct PathResult { double L[3]; int rays; };
 
 template <class R>
 static inline PathResult trace_path(const Scene& sc, const RenderParams& p, const CameraSetup& cs, int pixel,
-                                    uint32_t sample) {
+                                    uint32_t sample, const LightTables* lights = nullptr) {
   PathResult res{{0, 0, 0}, 0};
   philox::Stream rng;
   rng.init((uint32_t)pixel, sample, 0, p.seed, p.job);
@@ -793,7 +1126,13 @@ static inline PathResult trace_path(const Scene& sc, const RenderParams& p, cons
   V3<R> color = v3<R>(1, 1, 1);
   int medium = -1;
   const R bias = (R)p.ray_bias;
-  auto accumulate = [&](V3<R> c) { res.L[0] = (double)c.x; res.L[1] = (double)c.y; res.L[2] = (double)c.z; };
+  const bool nee = p.nee != 0 && lights != nullptr;
+  // radiance in the path's arithmetic: the reference estimator sets it once; with
+  // next-event estimation the light samples and the final emission add up in order
+  V3<R> Lsum = v3<R>(0, 0, 0);
+  auto finish = [&]() { res.L[0] = (double)Lsum.x; res.L[1] = (double)Lsum.y; res.L[2] = (double)Lsum.z; return res; };
+  auto accumulate = [&](V3<R> c) { Lsum = nee ? add(Lsum, c) : c; };
+  R pdf_prev = 0;   // density of the BSDF sample that led to this vertex (0: weight 1)
   for (int j = 0; j < p.max_depth; ++j) {
     res.rays++;
     rng.init((uint32_t)pixel, sample, (uint32_t)(j + 1), p.seed, p.job);
@@ -809,7 +1148,8 @@ static inline PathResult trace_path(const Scene& sc, const RenderParams& p, cons
         color = mulv(color, v3<R>(m_exp((R)-1.0f * scatter_dist * (R)md.absorption[0]),
                                   m_exp((R)-1.0f * scatter_dist * (R)md.absorption[1]),
                                   m_exp((R)-1.0f * scatter_dist * (R)md.absorption[2])));
-        if ((double)length2(color) < 1e-4) return res;
+        pdf_prev = 0;
+        if ((double)length2(color) < 1e-4) return finish();
         continue;
       }
       color = mulv(color, v3<R>(m_exp((R)-1.0f * h.t * (R)md.absorption[0]),
@@ -818,28 +1158,64 @@ static inline PathResult trace_path(const Scene& sc, const RenderParams& p, cons
     }
     if (!h.hit) {
       // miss: environment lookup, src/renderer.cu:378-386
-      const R u = (R)((double)(m_atan2(ray.d.z, ray.d.x) * (R)0.5f) * kInvPi + 0.5);
-      const R v = (R)(0.5 - (double)m_asin(ray.d.y) * kInvPi);
-      const V3<R> env = sc.env_tex >= 0 ? tex_eval<R>(sc, sc.env_tex, u, v) : v3<R>(0, 0, 0);
-      accumulate(mulv(color, env));
-      return res;
+      V3<R> Le = mulv(color, env_radiance<R>(sc, ray.d));
+      if (nee && pdf_prev > (R)0) Le = mul(Le, power_heuristic<R>(pdf_prev, env_light_pdf<R>(*lights, ray.d)));
+      accumulate(Le);
+      return finish();
     }
     const Material& mat = sc.materials[h.material];
     const V3<R> albedo = tex_eval<R>(sc, mat.albedo_tex, h.uv[0], h.uv[1]);
     const R roughness = tex_eval<R>(sc, mat.roughness_tex, h.uv[0], h.uv[1]).x;
     if (mat.type == MAT_EMISSIVE) {  // :192-198
-      accumulate(mulv(color, albedo));
-      return res;
+      V3<R> Le = mulv(color, albedo);
+      if (nee && pdf_prev > (R)0 && h.inst >= 0 && !lights->tris.empty()) {
+        const int base = lights->inst_base[h.inst];
+        if (base >= 0) {
+          const int l = base + h.prim;
+          const LightTables::Tri& T = lights->tris[l];
+          const V3<R> ln = cross(v3<R>(T.e1[0], T.e1[1], T.e1[2]), v3<R>(T.e2[0], T.e2[1], T.e2[2]));
+          const R lnl = m_sqrt(dot(ln, ln));
+          const R cos_l = lnl > (R)0 ? dot(ln, ray.d) / lnl : (R)0;
+          Le = mul(Le, power_heuristic<R>(pdf_prev, tri_light_pdf<R>(*lights, l, h.t, cos_l)));
+        }
+      }
+      accumulate(Le);
+      return finish();
+    }
+    if (j + 1 >= p.max_depth) return finish();   // every closest-hit query is used
+    if (nee && (medium < 0 || !sc.mediums[medium].active) &&
+        (mat.type == MAT_DIFFUSE || mat.type == MAT_ROUGHCONDUCTOR || mat.type == MAT_ROUGHREFLECTIVE)) {
+      philox::Stream lr;
+      lr.init((uint32_t)pixel, sample, 0x40000000u | (uint32_t)(j + 1), p.seed, p.job);
+      const R u0 = (R)lr.next(), u1 = (R)lr.next(), u2 = (R)lr.next();
+      const V3<R> ph = add(ray.o, mul(ray.d, h.t));
+      const LightSampleO<R> ls = sample_light<R>(sc, *lights, ph, u0, u1, u2);
+      V3<R> fcos;
+      R pdf_b = 0;
+      if (ls.ok && bsdf_eval_cos<R>(mat, ray.d, h.normal, albedo, roughness, ls.dir, fcos, pdf_b)) {
+        const V3<R> Cn = mul(mulv(mulv(color, fcos), ls.Le), power_heuristic<R>(ls.pdf, pdf_b) / ls.pdf);
+        if (std::isfinite((double)(Cn.x + Cn.y + Cn.z)) && (Cn.x > (R)0 || Cn.y > (R)0 || Cn.z > (R)0)) {
+          const V3<R> norm_o = mul(h.normal, dot(h.normal, ray.d) > (R)0 ? (R)-1.0f : (R)1.0f);
+          const V3<R> org = add(ph, mul(norm_o, bias));
+          const R tmax = ls.dist == (R)FLT_MAX ? (R)FLT_MAX : ls.dist * ((R)1.0f - (R)1e-4f) - bias;
+          if (tmax > (R)0) {
+            res.rays++;   // the shadow ray is a closest-hit query too
+            const Hit<R> o = closest_hit<R>(sc, Ray<R>{org, ls.dir}, p.isect);
+            if (!(o.hit && o.t < tmax)) accumulate(Cn);
+          }
+        }
+      }
     }
     ScatterOut<R> s = scatter<R>(mat, ray.d, h.normal, albedo, roughness, [&]() { return (R)rng.next(); });
-    if (s.status == SCATTER_KILLED) return res;
+    if (s.status == SCATTER_KILLED) return finish();
     if (s.medium != MEDIUM_UNCHANGED) medium = s.medium;
     color = mulv(color, s.weight);
+    pdf_prev = nee ? bsdf_sampled_pdf<R>(mat, s, ray.d, h.normal) : (R)0;
     const V3<R> new_origin = add(add(ray.o, mul(ray.d, h.t)), mul(s.offset_dir, s.offset_sign * bias));
     const V3<R> new_dir = s.dir;
     ray = Ray<R>{new_origin, normalize(new_dir)};
   }
-  return res;
+  return finish();
 }
 
 // ---- tonemap: src/tonemapper.cu:32-76 and src/renderer.cu:426-441 ----

@@ -171,6 +171,7 @@ typedef struct {
   int32_t num_pixels;       // 0 = every pixel of the image
   const int32_t* pixels;    // pixel indices (y * width + x) when num_pixels > 0
   int32_t nthreads;         // 0 = OpenMP default
+  int32_t nee;              // 1 = next-event estimation with MIS (EXTENSION)
 } oracle_render_args;
 
 void* oracle_scene_create(const illume_scene_desc* desc) { return scene_from_desc(desc); }
@@ -265,8 +266,10 @@ int64_t oracle_render(void* sp, const oracle_render_args* a, double* out_sum, do
   const Scene& sc = *(const Scene*)sp;
   RenderParams p;
   p.width = a->width; p.height = a->height; p.max_depth = a->max_depth; p.ray_bias = a->ray_bias;
-  p.seed = a->seed; p.job = a->job; p.isect = a->isect; p.exact_hg = a->exact_hg;
+  p.seed = a->seed; p.job = a->job; p.isect = a->isect; p.exact_hg = a->exact_hg; p.nee = a->nee;
   const CameraSetup cs = camera_setup(sc.camera, a->width, a->height);
+  LightTables lights;
+  if (a->nee) lights = build_light_tables(sc);
   const int np = a->num_pixels > 0 ? a->num_pixels : a->width * a->height;
   if (a->nthreads > 0) omp_set_num_threads(a->nthreads);
   std::atomic<int64_t> rays{0};
@@ -277,8 +280,8 @@ int64_t oracle_render(void* sp, const oracle_render_args* a, double* out_sum, do
     int64_t local = 0;
     for (int k = 0; k < a->spp; ++k) {
       const uint32_t sample = (uint32_t)(a->sample_begin + k);
-      const PathResult r = a->precision == 64 ? trace_path<double>(sc, p, cs, pixel, sample)
-                                              : trace_path<float>(sc, p, cs, pixel, sample);
+      const PathResult r = a->precision == 64 ? trace_path<double>(sc, p, cs, pixel, sample, &lights)
+                                              : trace_path<float>(sc, p, cs, pixel, sample, &lights);
       local += r.rays;
       for (int c = 0; c < 3; ++c) { s[c] += r.L[c]; s2[c] += r.L[c] * r.L[c]; }
     }
@@ -289,6 +292,24 @@ int64_t oracle_render(void* sp, const oracle_render_args* a, double* out_sum, do
     }
   }
   return rays.load();
+}
+
+// Alias table of n weights (EXTENSION: the next-event estimator's light choice).
+void oracle_alias_build(const double* w, int n, float* prob, int* alias) {
+  std::vector<AliasSlot> t(n > 0 ? n : 0);
+  alias_build(w, (size_t)(n > 0 ? n : 0), t.data());
+  for (int i = 0; i < n; ++i) { prob[i] = t[i].prob; alias[i] = t[i].alias; }
+}
+
+// The scene's light tables (EXTENSION): sizes, then the environment's texel weights,
+// row and column tables, and the triangle table with each triangle's choice probability.
+void oracle_light_info(void* sp, int* env_wh, float* env_integral_prob, int* num_tri) {
+  const LightTables L = build_light_tables(*(const Scene*)sp);
+  env_wh[0] = L.env_w;
+  env_wh[1] = L.env_h;
+  env_integral_prob[0] = L.env_integral;
+  env_integral_prob[1] = L.env_prob;
+  *num_tri = (int)L.tris.size();
 }
 
 void oracle_tonemap_image(const float* sum, int n, float samples, int op, unsigned char* out) {

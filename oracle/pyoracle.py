@@ -36,7 +36,7 @@ class RenderArgs(ctypes.Structure):
     _fields_ = [("width", c_int32), ("height", c_int32), ("max_depth", c_int32), ("ray_bias", c_float),
                 ("seed", c_uint32), ("job", c_uint32), ("isect", c_int32), ("exact_hg", c_int32),
                 ("spp", c_int32), ("sample_begin", c_int32), ("precision", c_int32), ("num_pixels", c_int32),
-                ("pixels", POINTER(c_int32)), ("nthreads", c_int32)]
+                ("pixels", POINTER(c_int32)), ("nthreads", c_int32), ("nee", c_int32)]
 
 
 _LIB = None
@@ -88,6 +88,8 @@ def lib():
         L.oracle_sphere_intersect.restype = c_int
         L.oracle_sphere_intersect.argtypes = [fp, c_float, fp, fp, fp, fp, fp]
         L.oracle_tonemap_eval.argtypes = [c_int, fp, fp]
+        L.oracle_alias_build.argtypes = [POINTER(c_double), c_int, fp, POINTER(c_int32)]
+        L.oracle_light_info.argtypes = [c_void_p, POINTER(c_int32), fp, POINTER(c_int32)]
         _LIB = L
     return _LIB
 
@@ -123,14 +125,16 @@ class OracleScene:
         return out
 
     def render(self, width, height, spp, max_depth, ray_bias=None, seed=0, job=0, isect=C.ISECT_WATERTIGHT,
-               exact_hg=0, sample_begin=0, precision=32, pixels=None, nthreads=0):
-        """Per-pixel sum and sum of squares of per-sample radiance (float64), and rays traced."""
+               exact_hg=0, sample_begin=0, precision=32, pixels=None, nthreads=0, nee=0):
+        """Per-pixel sum and sum of squares of per-sample radiance (float64), and rays traced
+        (nee=1: the next-event estimator; shadow rays count as rays)."""
         a = RenderArgs()
         a.width, a.height, a.max_depth = width, height, max_depth
         a.ray_bias = self.scene.ray_bias if ray_bias is None else ray_bias
         a.seed, a.job, a.isect, a.exact_hg = seed, job, isect, exact_hg
         a.spp, a.sample_begin, a.precision = spp, sample_begin, precision
         a.nthreads = nthreads
+        a.nee = nee
         pix = None
         if pixels is not None:
             pix = np.ascontiguousarray(pixels, dtype=np.int32)
@@ -142,6 +146,14 @@ class OracleScene:
         rays = lib().oracle_render(self.handle, ctypes.byref(a), s.ctypes.data_as(POINTER(c_double)),
                                    s2.ctypes.data_as(POINTER(c_double)))
         return s, s2, int(rays)
+
+    def light_info(self):
+        """(env_w, env_h, env_integral, env_prob, number of emissive triangles)."""
+        wh = (c_int32 * 2)()
+        fp2 = np.zeros(2, np.float32)
+        nt = c_int32()
+        lib().oracle_light_info(self.handle, wh, _fp(fp2), ctypes.byref(nt))
+        return int(wh[0]), int(wh[1]), float(fp2[0]), float(fp2[1]), int(nt.value)
 
     def texture_eval(self, tex, u, v):
         out = np.zeros(3, np.float32)
@@ -174,3 +186,13 @@ def bsdf_batch(material_type: int, distribution: int, inputs: np.ndarray, precis
     y = np.zeros_like(x)
     lib().oracle_bsdf_batch(material_type, distribution, _fp(x), x.shape[0], _fp(y), precision)
     return y
+
+
+def alias_table(weights):
+    """The oracle's alias table of the weights: (probabilities, aliases)."""
+    w = np.ascontiguousarray(weights, dtype=np.float64)
+    n = w.size
+    prob = np.zeros(n, np.float32)
+    alias = np.zeros(n, np.int32)
+    lib().oracle_alias_build(w.ctypes.data_as(POINTER(c_double)), n, _fp(prob), alias.ctypes.data_as(POINTER(c_int32)))
+    return prob, alias

@@ -1,10 +1,12 @@
 """Generates the golden fixtures of tests/golden/ from the reference renderer itself.
 
 Run in the build container, where the reference sources exist:
-    PYTHONPATH=. python tests/golden/make_golden.py
+    PYTHONPATH=. python tests/golden/make_golden.py [scene names]
+(with only "textured", only that scene's fixture is written; the others stay as they are)
 
-1. Writes the test scenes of tests/golden/scenes/ (JSON in the reference's scene format
-   and OBJ meshes; all authored here, none copied from the reference).
+1. Writes the test scenes of tests/golden/scenes/ (JSON in the reference's scene format,
+   OBJ meshes, and .hdr / .png bitmap textures; all authored here, none copied from the
+   reference).
 2. Runs the reference's own code, built for the host by oracle/build_ref.py, on seeded
    inputs and on those scenes, and stores its outputs:
      ref_components.npz   sampling, Fresnel, microfacet, intersection and tonemap functions
@@ -101,6 +103,60 @@ def write_obj_files():
             f.write("vn %.6f %.6f %.6f\n" % v)
         for a, b, c in faces:
             f.write(f"f {a + 1}/{a + 1}/{a + 1} {b + 1}/{b + 1}/{b + 1} {c + 1}/{c + 1}/{c + 1}\n")
+
+
+def write_rgbe(path, rgb):
+    """Radiance .hdr, flat (not run-length encoded) RGBE scanlines, top row first."""
+    h, w, _ = rgb.shape
+    out = bytearray(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n" + f"-Y {h} +X {w}\n".encode())
+    for y in range(h):
+        for x in range(w):
+            r, g, b = (float(v) for v in rgb[y, x])
+            m = max(r, g, b)
+            if m < 1e-32:
+                out += bytes(4)
+                continue
+            f, e = math.frexp(m)
+            sc = f * 256.0 / m
+            out += bytes([int(r * sc), int(g * sc), int(b * sc), e + 128])
+    with open(path, "wb") as f:
+        f.write(bytes(out))
+
+
+def write_png(path, pix, color_type):
+    """8-bit PNG (color type 0 gray, 2 RGB or 6 RGBA), filter 0 on every row."""
+    import struct
+    import zlib
+    h, w = pix.shape[:2]
+    raw = b"".join(b"\x00" + pix[y].astype(np.uint8).tobytes() for y in range(h))
+
+    def chunk(tag, data):
+        c = struct.pack(">I", len(data)) + tag + data
+        return c + struct.pack(">I", zlib.crc32(tag + data) & 0xffffffff)
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, color_type, 0, 0, 0))
+    png += chunk(b"IDAT", zlib.compress(raw, 9)) + chunk(b"IEND", b"")
+    with open(path, "wb") as f:
+        f.write(png)
+
+
+def write_texture_files():
+    """Bitmap textures of the textured scene, seeded: an equirectangular sky with texel
+    noise and a sharp sun lobe (a wrong uv or filter weight changes every escaped ray),
+    an HDR albedo, and LDR albedo / roughness images in three PNG colour types."""
+    rng = np.random.default_rng(77)
+    W, H = 64, 32
+    y = (np.arange(H) + 0.5) / H
+    base = 0.25 + 0.9 * (1.0 - y)[:, None, None] * np.array([0.6, 0.75, 1.0])
+    sky = base * (0.6 + 0.8 * rng.random((H, W, 3)))
+    sun_x, sun_y = 41.3, 9.6
+    xx, yy = np.meshgrid(np.arange(W) + 0.5, np.arange(H) + 0.5)
+    lobe = 40.0 * np.exp(-((xx - sun_x) ** 2 + (yy - sun_y) ** 2) / (2 * 1.2 ** 2))
+    sky = sky + lobe[:, :, None] * np.array([1.0, 0.9, 0.7])
+    write_rgbe(os.path.join(SCENE_DIR, "sky.hdr"), sky)
+    write_rgbe(os.path.join(SCENE_DIR, "tiles.hdr"), 0.05 + 0.9 * rng.random((16, 16, 3)))
+    write_png(os.path.join(SCENE_DIR, "grid.png"), rng.integers(0, 256, size=(8, 8, 3)), 2)
+    write_png(os.path.join(SCENE_DIR, "dots.png"), rng.integers(0, 256, size=(6, 10, 4)), 6)
+    write_png(os.path.join(SCENE_DIR, "rough.png"), rng.integers(10, 120, size=(4, 8)), 0)
 
 
 def tf(translation=(0, 0, 0), scale=(1, 1, 1), rotation=(0, 0, 0)):
@@ -220,7 +276,35 @@ def write_scene_files():
                    "fov": 50.0, "depth_of_field": 8.0, "aperture_radius": 0.05},
         "render_settings": {"resolution": [48, 40], "ray_bias": 0.001, "tonemapper": "Reinhard"},
     }
-    for name, sc in (("box", box), ("materials", materials), ("mesh", mesh)):
+    textured = {
+        "environment_map": {"type": "bitmap", "file": "sky.hdr"},
+        "materials": [
+            {"name": "floor", "type": "lambert", "albedo": {"type": "bitmap", "file": "tiles.hdr", "scale": [3.0, 3.0]}},
+            {"name": "crate", "type": "lambert", "albedo": {"type": "bitmap", "file": "grid.png", "scale": [2.0, 2.0]}},
+            {"name": "dotted", "type": "lambert", "albedo": {"type": "bitmap", "file": "dots.png"}},
+            {"name": "brushed", "type": "roughconductor", "material": "Au",
+             "roughness": {"type": "bitmap", "file": "rough.png", "scale": [2.0, 1.0]}},
+            {"name": "mirror", "type": "reflective", "albedo": [0.95, 0.95, 0.95]},
+            {"name": "tiledplastic", "type": "plastic", "ior": 1.5,
+             "albedo": {"type": "bitmap", "file": "tiles.hdr", "scale": [1.5, 0.75]}},
+        ],
+        "meshes": [{"file": "quad.obj", "name": "quad", "has_texcoords": True},
+                   {"file": "box.obj", "name": "box", "has_texcoords": True}],
+        "primitives": [
+            {"type": "mesh_instance", "mesh": "quad", "material": "floor",
+             "transform": tf((0, 0, 0), (14, 14, 14), (90, 0, 0))},
+            {"type": "mesh_instance", "mesh": "box", "material": "crate",
+             "transform": tf((-3.2, 0.75, 1.0), (1.5, 1.5, 1.5), (0, 25, 0))},
+            {"type": "sphere", "center": [-1.0, 1.0, -0.5], "radius": 1.0, "material": "dotted"},
+            {"type": "sphere", "center": [1.3, 1.0, 0.5], "radius": 1.0, "material": "brushed"},
+            {"type": "sphere", "center": [3.6, 1.2, 1.5], "radius": 1.2, "material": "mirror"},
+            {"type": "sphere", "center": [0.4, 0.6, -2.4], "radius": 0.6, "material": "tiledplastic"},
+        ],
+        "camera": {"transform": {"translation": [0.0, 2.2, -9.0], "lookat": [0.0, 1.4, 0.0]},
+                   "fov": 60.0, "depth_of_field": 1.0, "aperture_radius": 0.0},
+        "render_settings": {"resolution": [64, 48], "ray_bias": 0.001},
+    }
+    for name, sc in (("box", box), ("materials", materials), ("mesh", mesh), ("textured", textured)):
         with open(os.path.join(SCENE_DIR, name + ".json"), "w") as f:
             json.dump(sc, f, indent=1)
 
@@ -252,7 +336,7 @@ def seeded_rays(sd, n, seed):
 def gen_scene(name, pyref, golden_io, work):
     from oracle import build_ref
     for f in os.listdir(SCENE_DIR):
-        if f.endswith(".obj") or f.endswith(".json"):
+        if f.endswith((".obj", ".json", ".hdr", ".png")):
             shutil.copyfile(os.path.join(SCENE_DIR, f), os.path.join(work, f))
     rs = pyref.RefScene(name + ".json", work)
     sd = rs.export()
@@ -443,6 +527,7 @@ def gen_json(pyref):
 
 def main():
     write_obj_files()
+    write_texture_files()
     write_scene_files()
     from oracle import build_ref, pyref
     import golden_io
@@ -452,9 +537,13 @@ def main():
     build_ref.build()
     work = os.path.join(build_ref.WORK_DIR, "golden")
     os.makedirs(work, exist_ok=True)
+    names = sys.argv[1:] or ["box", "materials", "mesh", "textured"]
+    if names == ["textured"]:
+        gen_scene("textured", pyref, golden_io, work)
+        return
     gen_components(pyref)
     gen_json(pyref)
-    for name in ("box", "materials", "mesh"):
+    for name in names:
         gen_scene(name, pyref, golden_io, work)
 
 

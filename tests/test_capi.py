@@ -36,7 +36,7 @@ def load_host(path, base=SCENES):
     return st, h
 
 
-@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+@pytest.mark.parametrize("name", ["box", "materials", "mesh", "textured"])
 def test_host_only_scene_and_bvh_invariants(native_lib, name):
     st, h = load_host(os.path.join(SCENES, name + ".json"))
     assert st == C.OK, native_lib.illume_last_error()

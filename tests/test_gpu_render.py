@@ -31,7 +31,7 @@ def render(ctx, sd, w, h, spp, depth, **kw):
     return out
 
 
-@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+@pytest.mark.parametrize("name", ["box", "materials", "mesh", "textured"])
 @pytest.mark.parametrize("bvh", [C.BVH_BINARY, C.BVH_WIDE8, C.BVH_WIDE8_PERSISTENT, C.BVH_WIDE4])
 def test_matches_reference_render(ctx, name, bvh):
     z = golden(f"ref_scene_{name}.npz")
@@ -47,7 +47,7 @@ def test_matches_reference_render(ctx, name, bvh):
     assert (out["rgb8"] == z["render_rgb8"]).all(1).mean() >= 0.98
 
 
-@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+@pytest.mark.parametrize("name", ["box", "materials", "mesh", "textured"])
 def test_matches_oracle_watertight(ctx, name):
     from oracle import pyoracle
     sd = golden_scene(name)

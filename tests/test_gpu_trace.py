@@ -74,7 +74,7 @@ def compare(sd, rays8, ctx, bvh, isect):
     return int((want["inst"] >= 0).sum() + (want["sphere"] >= 0).sum())
 
 
-@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+@pytest.mark.parametrize("name", ["box", "materials", "mesh", "textured"])
 @pytest.mark.parametrize("bvh,isect", KINDS)
 def test_golden_scenes(ctx, name, bvh, isect):
     sd = golden_scene(name)

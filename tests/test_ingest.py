@@ -27,7 +27,7 @@ def host_scene_from_json(text, base=None):
 CAM = {"transform": {"translation": [0, 0, -5]}, "fov": 40, "depth_of_field": 1, "aperture_radius": 0}
 
 
-@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+@pytest.mark.parametrize("name", ["box", "materials", "mesh", "textured"])
 def test_scene_files_parse_like_the_reference(native_lib, name):
     sd = host_scene_from_json(open(os.path.join(SCENES, name + ".json")).read(), SCENES)
     ref = golden_scene(name)
@@ -200,3 +200,23 @@ def test_obj_variants(native_lib, tmp_path):
     sd = host_scene_from_json(json.dumps(sc), str(tmp_path))
     assert sd.meshes[0].normals is not None
     assert np.allclose(np.linalg.norm(sd.meshes[0].normals, axis=1), 1.0)
+
+
+def test_bitmap_texels_and_environment_like_the_reference(native_lib):
+    """The textured scene's .hdr (flat RGBE) and .png (gray, RGB, RGBA) bitmaps decode to
+    the texels the reference's stb_image path gives (src/imageio.cpp, 4 channels), and
+    the equirectangular environment evaluates identically over the whole uv square
+    (bilinear HDR filtering with wrap addressing, src/texture.cu:146-152)."""
+    from oracle import pyoracle
+    sd = host_scene_from_json(open(os.path.join(SCENES, "textured.json")).read(), SCENES)
+    ref = golden_scene("textured")
+    bitmaps = lambda s: [t for t in s.textures if t.texels is not None]
+    A, B = bitmaps(sd), bitmaps(ref)
+    assert len(A) >= 4 and len(B) >= 4
+    key = lambda t: (t.texels.shape, t.hdr, t.texels.tobytes())
+    assert sorted(map(key, A)) == sorted(map(key, B))
+    osa, osb = pyoracle.OracleScene(sd), pyoracle.OracleScene(ref)
+    rng = np.random.default_rng(5)
+    uvs = (rng.random((512, 2)) * 1.6 - 0.3).astype(np.float32)
+    for u, v in uvs:
+        assert np.array_equal(osa.texture_eval(sd.env_tex, u, v), osb.texture_eval(ref.env_tex, u, v))

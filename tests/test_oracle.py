@@ -138,7 +138,7 @@ def test_tonemap_operators(oracle_lib):
         assert (ulp_diff(out, z[f"tone{op}"]) <= 2).all(), op
 
 
-@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+@pytest.mark.parametrize("name", ["box", "materials", "mesh", "textured"])
 def test_camera_rays_bit_exact(oracle_lib, name):
     from oracle import pyoracle
     z = golden(f"ref_scene_{name}.npz")
@@ -147,7 +147,7 @@ def test_camera_rays_bit_exact(oracle_lib, name):
     assert np.array_equal(os_.camera_rays(W, H, sample=5, seed=0), z["camera_rays"])
 
 
-@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+@pytest.mark.parametrize("name", ["box", "materials", "mesh", "textured"])
 def test_closest_hits_match_reference(oracle_lib, name):
     from oracle import pyoracle
     z = golden(f"ref_scene_{name}.npz")
@@ -164,7 +164,7 @@ def test_closest_hits_match_reference(oracle_lib, name):
     assert (h["t"][hit] == z["hit_t"][hit]).mean() >= 0.999
 
 
-@pytest.mark.parametrize("name", ["box", "materials", "mesh"])
+@pytest.mark.parametrize("name", ["box", "materials", "mesh", "textured"])
 def test_render_matches_reference_integrator(oracle_lib, name):
     """Same Philox streams: the oracle's FP32 path equals the reference's path by path."""
     from oracle import pyoracle
