@@ -42,8 +42,8 @@ struct Context {
   // (trace by BVH kind and variant, shade by variant; 0 = not yet computed)
   void* noalloc_scratch = nullptr;
   void* noalloc_cu_ctx = nullptr;
-  int noalloc_grid_trace[4][5] = {};
-  int noalloc_grid_shade[5] = {};
+  int noalloc_grid_trace[4][8] = {};
+  int noalloc_grid_shade[8] = {};
 };
 
 // Device allocation charged against the context's budget.

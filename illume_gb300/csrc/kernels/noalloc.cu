@@ -128,9 +128,9 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
       ctx->c.noalloc_cu_ctx = cu_ctx;
     }
     base = ctx->c.noalloc_scratch;
-    int& gt = ctx->c.noalloc_grid_trace[k.bvh_kind & 3][k.trace_variant % 5];
+    int& gt = ctx->c.noalloc_grid_trace[k.bvh_kind & 3][k.trace_variant & 7];
     if (!gt) gt = kernel_grid_blocks(trace_kernel_ptr(k.bvh_kind, k.trace_variant), 128, dev);
-    int& gs = ctx->c.noalloc_grid_shade[k.shade_variant % 5];
+    int& gs = ctx->c.noalloc_grid_shade[k.shade_variant & 7];
     if (!gs) gs = kernel_grid_blocks(shade_kernel_ptr(k.shade_variant), 128, dev);
     grid_trace = gt;
     grid_shade = gs;

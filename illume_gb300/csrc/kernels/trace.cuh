@@ -37,10 +37,23 @@ __device__ __forceinline__ float safe_rcp(float d) {
   return 1.0f / (fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d));
 }
 
+// The same reciprocal from the hardware approximation (rcp.approx.ftz.f32, at most about
+// one ulp off; the clamp keeps the input normal). Used only for box tests: a relative
+// error e on a ray's reciprocal direction scales each axis's slab distances by (1 + e),
+// so entry and exit distances of different axes move apart by at most twice that, far
+// inside the ~8 ulp exit widening (kExitSlack), and no box that contains a hit is culled.
+__device__ __forceinline__ float fast_rcp(float d) {
+  const float c = fabsf(d) > 1e-20f ? d : copysignf(1e-20f, d);
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(c));
+  return r;
+}
+
+template <bool FR = false>
 __device__ __forceinline__ void setup_ray(TraceRay& r, V3 o, V3 d, int isect) {
   r.o = o;
   r.d = d;
-  r.idir = v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+  r.idir = FR ? v3(fast_rcp(d.x), fast_rcp(d.y), fast_rcp(d.z)) : v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
   r.oi = v3(o.x * r.idir.x, o.y * r.idir.y, o.z * r.idir.z);
   r.oct = (d.x < 0.0f ? 4 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 1 : 0);
   if (isect == ISECT_WATERTIGHT) {
@@ -589,8 +602,9 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 // tmax: only hits closer than tmax count (shadow rays). ANY: return at the first hit
 // found closer than tmax (occlusion; with the binary and 4-wide layouts).
 // PS, NF: options of the 4-wide traversal (traverse_bvh4_ww).
+// FR: box-test reciprocals from the hardware approximation (fast_rcp).
 template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false, bool ANY = false, bool PS = false,
-          bool NF = false>
+          bool NF = false, bool FR = false>
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
                                                  VisitCount* vcp = nullptr, float tmax = FLT_MAX) {
   VisitCount vc;
@@ -614,13 +628,13 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
   // world-space probe for instance boxes
   TraceRay wr;
   wr.o = o; wr.d = d;
-  wr.idir = v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
+  wr.idir = FR ? v3(fast_rcp(d.x), fast_rcp(d.y), fast_rcp(d.z)) : v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
   for (int i = 0; i < sc.num_instances; ++i) {
     const DevInstance& in = sc.instances[i];
     float te;
     if (!box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) continue;
     TraceRay r;
-    setup_ray(r, xform(in.inv, o, 1.0f), xform(in.inv, d, 0.0f), isect);
+    setup_ray<FR>(r, xform(in.inv, o, 1.0f), xform(in.inv, d, 0.0f), isect);
     MeshBest b{h.t, -1, 0.0f, 0.0f};
     const DevMesh& m = sc.meshes[in.mesh];
     if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);

@@ -44,7 +44,8 @@ __device__ __forceinline__ int event_class(const WaveBuffers& w, const JobDesc& 
 // shared counter (counters[44 + parity]) instead of a fixed grid stride, so that warps
 // whose rays finish early take over the remaining work.
 // PS, NF (4-wide only): see traverse_bvh4_ww.
-template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false, bool PS = false, bool NF = false>
+template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false, bool PS = false, bool NF = false,
+          bool FR = false>
 __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
   const int parity = bounce & 1;
   const int n = w.counters[parity];
@@ -77,8 +78,8 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
     const SceneView& sc = J.sc;
     VisitCount vc;
     const HitRecord h =
-        closest_hit<KIND, COUNT, OPT, WW, false, PS, NF>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect, stack,
-                                                     &vc);
+        closest_hit<KIND, COUNT, OPT, WW, false, PS, NF, FR>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect,
+                                                         stack, &vc);
     if (COUNT) {
       my_nodes += vc.nodes;
       my_tris += vc.tris;
@@ -462,6 +463,7 @@ const void* trace_kernel_ptr(int bvh_kind, int variant) {
     if (variant == 1) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, true, true>;
     if (variant == 2) return (const void*)k_trace<BVH_WIDE4, false, 8, true>;
     if (variant == 3) return (const void*)k_trace<BVH_WIDE4, false, 6, true, false, false, true>;
+    if (variant == 4) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true, true>;
     return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true>;
   }
   if (bvh_kind == BVH_WIDE8)
@@ -485,6 +487,9 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
     } else if (k.trace_variant == 3) {
       if (count_visits) k_trace<BVH_WIDE4, true, 6, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE4, false, 6, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    } else if (k.trace_variant == 4) {
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true, false, false, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
     } else {
       if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE4, false, 8, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);

@@ -171,7 +171,9 @@ typedef struct {
                                * near / far planes loaded by per-ray offsets, stack in local
                                * memory (default); 1 = four compare-swaps instead of five in
                                * the child ordering; 2 = lo / hi planes selected per child
-                               * box; 3 = at most 80 registers. Other layouts ignore it. */
+                               * box; 3 = at most 80 registers; 4 = variant 0 with box-test
+                               * reciprocals from the hardware approximation. Other layouts
+                               * ignore it. */
   int32_t shade_variant;      /* 0 = the measured best register bound (default), 1 = the
                                * compiler's choice, 2 / 3 / 4 = at most 80 / 72 / 64 registers */
   int32_t estimator;          /* illume_estimator */

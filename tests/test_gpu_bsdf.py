@@ -8,6 +8,8 @@ FP64's and directions be within 1e-5. Values (weight, D, pdf, G, F, eval): withi
 relative (to max(|ref|, 1e-3)) on >= 99.5% of the tuples whose FP64 values move by less
 than 4e-6 under a 4-ulp perturbation of the inputs, and within 5e-5 on all of them.
 """
+import json
+
 import numpy as np
 import pytest
 
@@ -90,3 +92,15 @@ def test_bsdf_against_oracle(ctx, mat, dist):
     # the FP32 formulation itself (FP32 oracle) leaves a small tail above 1e-5 on these
     assert (rel_gpu < 1e-5).mean() >= 0.995, (rel_gpu < 1e-5).mean()
     assert rel_gpu.max() < 5e-5, rel_gpu.max()
+    # reported over every live tuple, conditioned or not (printed; pytest -s shows it):
+    # the share within 1e-5 of FP64, the worst case, and the same for the FP32 oracle,
+    # whose arithmetic the kernels follow
+    alive = (f64[:, 12] > 0) & (got[:, 12] == f64[:, 12])
+    rel_all = (np.abs(got[alive][:, vals] - f64[alive][:, vals]) / ref[alive]).max(1)
+    rel_f32 = (np.abs(f32[alive][:, vals] - f64[alive][:, vals]) / ref[alive]).max(1)
+    print("BSDF_STATS", json.dumps({"material": int(mat), "distribution": int(dist), "live": int(alive.sum()),
+                                    "stable": int(stable.sum()),
+                                    "gpu_within_1e-5_all_live": round(float((rel_all < 1e-5).mean()), 4),
+                                    "gpu_max_rel_all_live": float(rel_all.max()) if alive.any() else 0.0,
+                                    "fp32_oracle_within_1e-5_all_live": round(float((rel_f32 < 1e-5).mean()), 4),
+                                    "fp32_oracle_max_rel_all_live": float(rel_f32.max()) if alive.any() else 0.0}))

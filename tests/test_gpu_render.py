@@ -93,24 +93,29 @@ def test_three_sigma_against_fp64_oracle(ctx, name):
 
 def test_three_sigma_full_cornell_frame(ctx):
     """The plain small configuration (the Cornell box of five quads with a mirror and a
-    dielectric sphere, 256x256, depth 8): every pixel's GPU mean (1024 samples) against the
-    FP64 oracle's (256 independent samples), |mu_gpu - mu_ref| <= 3 sqrt(s2_gpu/n_gpu +
-    s2_ref/n_ref). Under a Gaussian model a pixel fails with probability 0.27%; the bar is a
-    failing fraction of at most 0.5%, which over 65,536 pixels lies 5.6 binomial standard
-    deviations above the expected 177 failures (a correct renderer fails it with
-    probability below 1e-7 under that model)."""
+    dielectric sphere, 256x256, depth 8): every pixel's GPU mean against the FP64
+    oracle's, 1024 independent samples each, |mu_gpu - mu_ref| <= 3 sqrt(s2_gpu/n_gpu +
+    s2_ref/n_ref) on all three channels. Under a Gaussian model a channel fails with
+    probability 0.27%; the caustics of the small light through the spheres make the
+    per-pixel distributions heavy tailed, so the bar is set from two independent oracle
+    renders of this frame at 1024 samples each, which fail on 0.34% of pixels (0.20% of
+    channels): at most 0.5% of pixels may fail, 3.2 binomial standard deviations above
+    that rate over 65,536 pixels. (Unequal sample counts are avoided: the side with
+    fewer samples misses rare caustic paths and understates its variance, and 1024
+    against 256 samples fails 3.8% of pixels even between two oracle renders.)"""
     from illume_gb300 import synth
     from oracle import pyoracle
     w = h = 256
+    n = 1024
     sd = synth.cornell_scene(w, h)
-    out = render(ctx, sd, w, h, 1024, 8, accum_mode=C.ACCUM_FP64, seed=31)
-    s, s2, _ = pyoracle.OracleScene(sd).render(w, h, 256, 8, seed=4242, isect=C.ISECT_WATERTIGHT, precision=64)
-    ok = three_sigma(out["sum"], out["sumsq"], 1024, s, s2, 256).all(1)
-    n = ok.size
-    fails = int(n - ok.sum())
-    p0 = 0.0027
-    z = (fails - n * p0) / np.sqrt(n * p0 * (1 - p0))
-    assert fails / n <= 0.005, (fails, n, z)
+    out = render(ctx, sd, w, h, n, 8, accum_mode=C.ACCUM_FP64, seed=31)
+    s, s2, _ = pyoracle.OracleScene(sd).render(w, h, n, 8, seed=4242, isect=C.ISECT_WATERTIGHT, precision=64)
+    ok = three_sigma(out["sum"], out["sumsq"], n, s, s2, n).all(1)
+    npx = ok.size
+    fails = int(npx - ok.sum())
+    p0 = 0.0034
+    z = (fails - npx * p0) / np.sqrt(npx * p0 * (1 - p0))
+    assert fails / npx <= 0.005, (fails, npx, z)
 
 
 def test_exact_hg_matches_the_oracle(ctx):
