@@ -65,9 +65,17 @@ def parse():
     ap.add_argument("--shade-variant", type=int, default=0,
                     help="shade kernel: 0 measured best register bound (default), 1 compiler's choice, "
                          "2 / 3 / 4 at most 80 / 72 / 64 registers")
+    ap.add_argument("--queue-slots", type=int, default=0,
+                    help="path regeneration: rays in flight per engine (0: every path of a pass starts at once)")
+    ap.add_argument("--regen-threshold", type=float, default=1.0,
+                    help="path regeneration: refill when the next queue holds at most this share of the slots")
     ap.add_argument("--engines", type=int, default=0,
                     help="engines taking turns on a step's passes (0: the library's choice)")
     ap.add_argument("--tris", type=int, default=100_000)
+    ap.add_argument("--scene", default="traversal", choices=["traversal", "sss", "instanced"],
+                    help="traversal workload's scene: the headline 100k-triangle scene (default), the "
+                         "700k-triangle subsurface scene, or the 2M-triangle instanced scene (BVH layout "
+                         "comparisons where the BVH outgrows the caches)")
     ap.add_argument("--res", type=int, default=1024)
     ap.add_argument("--depth", type=int, default=25)
     ap.add_argument("--sss-res", type=int, nargs=2, default=[96, 72],
@@ -155,7 +163,23 @@ def measured_peaks():
 
 def build_scene(args):
     from illume_gb300 import synth
+    if args.scene == "sss":
+        return synth.sss_scene(700_000, seed=3, width=args.res, height=args.res)
+    if args.scene == "instanced":
+        sd = synth.instanced_scene(16, 125_000, seed=5)
+        sd.width = sd.height = args.res
+        return sd
     return synth.traversal_scene(tris=args.tris, seed=1, width=args.res, height=args.res)
+
+
+def workload_name(args):
+    if args.scene == "sss":
+        return (f"subsurface scene: 700k-tri displaced dielectric (ior 1.3) around a medium in the Cornell box, "
+                f"{args.res}x{args.res}, depth {args.depth}")
+    if args.scene == "instanced":
+        return (f"instanced scene: 16 displaced 125k-tri meshes (2M tris), mixed materials, 2048x1024 env, "
+                f"{args.res}x{args.res}, depth {args.depth}")
+    return WORKLOAD
 
 
 def cpu_baseline(sd, args, seconds):
@@ -252,6 +276,8 @@ def run_ours(args):
     p.trace_variant = args.trace_variant
     p.shade_variant = args.shade_variant
     p.engines = args.engines
+    p.queue_slots = args.queue_slots
+    p.regen_threshold = args.regen_threshold
     r = Renderer(ctx, scene, params=p)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{dev}")   # > 129 MB L2
 
@@ -378,8 +404,11 @@ def run_ours(args):
             "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(dev_ms_max / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "mode": "plain wavefront" + (", passes of %d samples on %d engines taking "
-                       "turns" % (pass_spp, n_eng) if n_eng > 1 else ""), "bvh": args.bvh, "intersector": "watertight",
+            "config": {"workload": workload_name(args), "mode": "plain wavefront" + (", passes of %d samples on %d engines taking "
+                       "turns" % (pass_spp, n_eng) if n_eng > 1 else "") + (
+                           ", paths regenerated into %d queue slots per engine (threshold %.2f)" %
+                           (args.queue_slots, args.regen_threshold) if args.queue_slots > 0 else ""),
+                       "bvh": args.bvh, "intersector": "watertight",
                        "estimator": args.estimator, "trace_variant": args.trace_variant,
                        "spp_per_step": args.spp_per_step, "paths_per_step": npix * args.spp_per_step,
                        "triangles": sd.num_triangles(), "resolution": [args.res, args.res], "max_depth": args.depth,

@@ -36,7 +36,8 @@ ISECT_MT, ISECT_WATERTIGHT = range(2)
 BVH_BINARY, BVH_WIDE8, BVH_WIDE8_PERSISTENT, BVH_WIDE4 = range(4)
 ACCUM_FP32, ACCUM_KAHAN, ACCUM_FP64 = range(3)
 ESTIMATOR_REFERENCE, ESTIMATOR_NEE = range(2)
-SERVER_PATH_CAPACITY, SERVER_PASSES_PER_STEP, SERVER_AUTOTUNE, SERVER_TRACE_VARIANT, SERVER_LANES = range(5)
+(SERVER_PATH_CAPACITY, SERVER_PASSES_PER_STEP, SERVER_AUTOTUNE, SERVER_TRACE_VARIANT, SERVER_LANES,
+ SERVER_QUEUE_SLOTS, SERVER_REGEN_THRESHOLD) = range(7)
 
 _pi32 = POINTER(c_int32)
 _pf = POINTER(c_float)
@@ -79,7 +80,7 @@ class RenderParams(ctypes.Structure):
         ("seed", c_uint32), ("job", c_uint32), ("accum_mode", c_int32), ("intersector", c_int32),
         ("bvh_kind", c_int32), ("exact_hg", c_int32), ("samples_per_pass", c_int32),
         ("camera", _pf), ("trace_variant", c_int32), ("shade_variant", c_int32), ("estimator", c_int32),
-        ("engines", c_int32),
+        ("engines", c_int32), ("queue_slots", c_int32), ("regen_threshold", c_float),
     ]
 
 
@@ -103,7 +104,7 @@ class ServerStats(ctypes.Structure):
     """illume_server_stats"""
     _fields_ = [("rays", c_int64), ("passes", c_int64), ("kernel_launches", c_int64), ("jobs_done", c_int64),
                 ("device_ms", c_double), ("path_capacity", c_int64), ("trace_variant", c_int32), ("tuned", c_int32),
-                ("device_bytes", c_int64)]
+                ("device_bytes", c_int64), ("queue_slots", c_int32), ("regen_threshold", c_float)]
 
 
 class Hit(ctypes.Structure):

@@ -224,7 +224,8 @@ class Server:
         ctx._adopt(self)
         self._npix = {}
         names = {"path_capacity": C.SERVER_PATH_CAPACITY, "passes_per_step": C.SERVER_PASSES_PER_STEP,
-                 "autotune": C.SERVER_AUTOTUNE, "trace_variant": C.SERVER_TRACE_VARIANT, "lanes": C.SERVER_LANES}
+                 "autotune": C.SERVER_AUTOTUNE, "trace_variant": C.SERVER_TRACE_VARIANT, "lanes": C.SERVER_LANES,
+                 "queue_slots": C.SERVER_QUEUE_SLOTS, "regen_threshold_permille": C.SERVER_REGEN_THRESHOLD}
         for k, v in options.items():
             C.check(C.lib().illume_server_set_option(self.handle, names[k], int(v)))
 

@@ -217,6 +217,8 @@ int illume_render_params_default(const illume_scene* scene, int spp, int max_dep
   out->bvh_kind = ILLUME_BVH_WIDE4;
   out->exact_hg = 0;
   out->samples_per_pass = 0;
+  out->queue_slots = 0;
+  out->regen_threshold = 1.0f;
   return ILLUME_OK;
 }
 

@@ -37,12 +37,17 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if (p.intersector != ISECT_MT && p.intersector != ISECT_WATERTIGHT) { *err = "unknown intersector"; return ILLUME_ERR_INVALID; }
   if (p.bvh_kind < 0 || p.bvh_kind > 3) { *err = "unknown BVH kind"; return ILLUME_ERR_INVALID; }
   if (p.bvh_kind == BVH_BINARY && (p.trace_variant < 0 || p.trace_variant > 4)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
-  if (p.bvh_kind == 3 && (p.trace_variant < 0 || p.trace_variant > 4)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
+  if (p.bvh_kind == 3 && (p.trace_variant < 0 || p.trace_variant > 5)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.accum_mode < ACCUM_FP32 || p.accum_mode > ACCUM_FP64) { *err = "unknown accumulation mode"; return ILLUME_ERR_INVALID; }
   if (p.samples_per_pass < 0) { *err = "negative samples per pass"; return ILLUME_ERR_INVALID; }
   if (p.shade_variant < 0 || p.shade_variant > 4) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.engines < 0 || p.engines > 16) { *err = "engines out of range (0-16)"; return ILLUME_ERR_INVALID; }
   if (p.estimator < ILLUME_ESTIMATOR_REFERENCE || p.estimator > ILLUME_ESTIMATOR_NEE) { *err = "unknown estimator"; return ILLUME_ERR_INVALID; }
+  if (p.queue_slots < 0) { *err = "negative queue slots"; return ILLUME_ERR_INVALID; }
+  if (p.queue_slots > 0 && !(p.regen_threshold >= 0.0f && p.regen_threshold <= 1.0f)) {
+    *err = "regeneration threshold outside [0, 1]";
+    return ILLUME_ERR_INVALID;
+  }
   if ((int)scene.t_mediums.size() > kMaxMediums) { *err = "too many mediums"; return ILLUME_ERR_UNSUPPORTED; }
   // the 8-wide kernels push up to two stack entries per level (a triangle group and a
   // node group); upload bounds the binary and 4-wide trees the same way
@@ -124,7 +129,8 @@ int Renderer::init(std::string* err) {
   acc.comp32 = comp32.as<float>();
   acc.sum64 = sum64.as<double>();
   acc.sumsq = sumsq.as<double>();
-  if ((st = eng.init(ctx, 1, per_pass * npix, render_knobs(p), err)) != ILLUME_OK) return st;
+  if ((st = eng.init(ctx, 1, per_pass * npix, render_knobs(p), err, p.queue_slots, p.regen_threshold)) != ILLUME_OK)
+    return st;
   JobDesc row = job_row(*scene, p, acc);
   if (nengines > 1) row.flags |= nengines << kInterleaveShift;
   eng.mirror[0] = row;
@@ -143,12 +149,14 @@ int Renderer::init(std::string* err) {
       more.emplace_back(new Engine);
       Engine& x = *more.back();
       x.stream = s;
-      if ((st = x.init(ctx, 1, per_pass * npix, render_knobs(p), err)) != ILLUME_OK) return st;
+      if ((st = x.init(ctx, 1, per_pass * npix, render_knobs(p), err, p.queue_slots, p.regen_threshold)) != ILLUME_OK)
+        return st;
       x.mirror[0] = row;
       if ((st = x.write_row(0)) != ILLUME_OK) { *err = last_error(); return st; }
       ILLUME_CUDA_TRY(cudaStreamSynchronize(s));
     }
   }
+  iter_total.assign(nengines, 0);
   ILLUME_CUDA_TRY(cudaEventCreate(&ev0));
   ILLUME_CUDA_TRY(cudaEventCreate(&ev1));
   launch_clear_accumulators(acc, npix, ctx->stream);
@@ -212,17 +220,34 @@ int Renderer::render_device(bool accumulate, illume_render_stats* stats) {
     if ((s = eng.run(npasses, p.max_depth)) != ILLUME_OK) return s;
   }
   ILLUME_CUDA_TRY(cudaEventRecord(ev1, st));
-  std::vector<int> drops(nengines, 0);
+  // per engine: the traversal-overflow flag, the regeneration loop's iteration total and
+  // its bound flag (a word each, after the ray total)
+  std::vector<int> flags(3 * (size_t)nengines, 0);
   for (int e = 0; e < nengines; ++e) {
     ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_after[e], reinterpret_cast<const char*>(engine(e).w.jobs) + rays_off, 8,
                                     cudaMemcpyDeviceToHost, st));
-    ILLUME_CUDA_TRY(cudaMemcpyAsync(&drops[e], engine(e).w.counters + kCounterStackDrops, sizeof(int),
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&flags[3 * e], engine(e).w.counters + kCounterStackDrops, sizeof(int),
+                                    cudaMemcpyDeviceToHost, st));
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&flags[3 * e + 1], engine(e).w.counters + kCounterIterTotal, sizeof(int),
+                                    cudaMemcpyDeviceToHost, st));
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&flags[3 * e + 2], engine(e).w.counters + kCounterLoopLimit, sizeof(int),
                                     cudaMemcpyDeviceToHost, st));
   }
   ILLUME_CUDA_TRY(cudaStreamSynchronize(st));
   ILLUME_CUDA_TRY(cudaGetLastError());
   stack_overflow = false;
-  for (int e = 0; e < nengines; ++e) stack_overflow = stack_overflow || drops[e] != 0;
+  long long iters = 0;
+  bool loop_limit = false;
+  for (int e = 0; e < nengines; ++e) {
+    stack_overflow = stack_overflow || flags[3 * e] != 0;
+    iters += (long long)flags[3 * e + 1] - iter_total[e];
+    iter_total[e] = flags[3 * e + 1];
+    loop_limit = loop_limit || flags[3 * e + 2] != 0;
+  }
+  if (loop_limit) {
+    set_error("a path-regeneration loop reached its iteration bound: the pass ended before all its paths");
+    return ILLUME_ERR_TIMEOUT;
+  }
   samples_done += spp;
   next_sample += spp;
   if (stats) {
@@ -233,10 +258,12 @@ int Renderer::render_device(bool accumulate, illume_render_stats* stats) {
     stats->rays = rays;
     stats->paths = (int64_t)spp * npix;
     stats->render_ms = ms;
-    stats->kernel_launches = (int64_t)npasses * Engine::launches_per_pass(p.max_depth, p.estimator == ILLUME_ESTIMATOR_NEE);
+    const bool nee = p.estimator == ILLUME_ESTIMATOR_NEE;
+    stats->kernel_launches = eng.regen ? Engine::launches_regen(npasses, iters, nee)
+                                       : (int64_t)npasses * Engine::launches_per_pass(p.max_depth, nee);
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - wall0).count();
     stats->h2d_bytes = 4 * sizeof(int);
-    stats->d2h_bytes = 16 + sizeof(int) * (size_t)nengines;
+    stats->d2h_bytes = 16 + 3 * sizeof(int) * (size_t)nengines;
   }
   return ILLUME_OK;
 }
@@ -252,7 +279,8 @@ int Renderer::profile(bool count_visits, illume_profile* out) {
   ILLUME_CUDA_TRY(cudaMemcpyAsync(&rays_before, reinterpret_cast<const char*>(eng.w.jobs) + offsetof(JobDesc, rays), 8,
                                   cudaMemcpyDeviceToHost, st));
   std::vector<cudaEvent_t> ev;
-  const int ps = eng.run_profiled(p.max_depth, count_visits, ev);
+  int iters = 0;
+  const int ps = eng.run_profiled(p.max_depth, count_visits, ev, &iters);
   if (ps != ILLUME_OK) {
     for (auto& e : ev) if (e) cudaEventDestroy(e);
     return ps;
@@ -268,13 +296,13 @@ int Renderer::profile(bool count_visits, illume_profile* out) {
     return (double)x;
   };
   out->raygen_ms = ms(0, 1);
-  for (int b = 0; b < p.max_depth; ++b) {
+  for (int b = 0; b < iters; ++b) {
     out->trace_ms += ms(1 + 2 * b, 2 + 2 * b);
     out->shade_ms += ms(2 + 2 * b, 3 + 2 * b);
   }
-  out->accumulate_ms = ms(1 + 2 * p.max_depth, 2 + 2 * p.max_depth);
-  out->trace_launches = p.max_depth;
-  out->shade_launches = p.max_depth;
+  out->accumulate_ms = ms(1 + 2 * iters, 2 + 2 * iters);
+  out->trace_launches = iters;
+  out->shade_launches = iters;
   out->rays = (int64_t)(rays_after - rays_before);
   out->node_fetches = (int64_t)vis[0];
   out->tri_tests = (int64_t)vis[1];

@@ -41,6 +41,7 @@ struct Renderer {
   // set by render_device when a traversal of the call found its stack full (the kernels'
   // defect flag, kCounterStackDrops): the image is complete but may lack hits
   bool stack_overflow = false;
+  std::vector<int> iter_total;   // per engine: regeneration loop iterations read at the last call's end
 
   ~Renderer();
   int init(std::string* err);

@@ -49,7 +49,7 @@ int Server::new_engine(const illume_render_params& p, int key, long long cap, Se
   k.trace_variant = trace_variant >= 0 ? trace_variant : (p.bvh_kind == 2 ? 1 : 0);
   k.shade_variant = 0;
   std::string err;
-  const int st = se.eng->init(ctx, rows, (int)cap, k, &err);
+  const int st = se.eng->init(ctx, rows, (int)cap, k, &err, queue_slots, regen_threshold);
   if (st != ILLUME_OK) { set_error(err); return st; }
   // a table that joins a tuned setting takes the tuned candidate
   auto tit = tuners.find(se.base_key);
@@ -57,6 +57,10 @@ int Server::new_engine(const illume_render_params& p, int key, long long cap, Se
     for (const auto& kv : engines)
       if (kv.second.base_key == se.base_key) {
         se.eng->set_trace_variant(kv.second.eng->knobs.trace_variant);
+        if (se.eng->set_regen(kv.second.eng->queue_req, kv.second.eng->regen_threshold, &err) != ILLUME_OK) {
+          set_error(err);
+          return ILLUME_ERR_CUDA;
+        }
         break;
       }
   }
@@ -400,11 +404,13 @@ int Server::retire(ServerEngine& se, std::vector<ServerJob*>* done) {
   return ILLUME_OK;
 }
 
-// Applies candidate `idx` (path slots per table, trace kernel variant) to every table of
-// a trace-kernel setting; fails without change if a running job does not fit the slots.
+// Applies candidate `idx` (path slots per table, trace kernel variant, path
+// regeneration) to every table of a trace-kernel setting; fails without change if a
+// running job does not fit the slots.
 int Server::apply_candidate(int base_key, int idx) {
   const Tuner& t = tuners[base_key];
-  const int cap = t.candidates[idx].first;
+  const Tuner::Candidate& c = t.candidates[idx];
+  const int cap = c.cap;
   for (const auto& kv : engines) {
     if (kv.second.base_key != base_key) continue;
     for (int r = 0; r < kv.second.eng->rows; ++r)
@@ -416,7 +422,8 @@ int Server::apply_candidate(int base_key, int idx) {
     std::string err;
     int st = e.resize(cap, &err);
     if (st != ILLUME_OK) { set_error(err); return st; }
-    if ((st = e.set_trace_variant(t.candidates[idx].second)) != ILLUME_OK) return st;
+    if ((st = e.set_regen(c.queue_slots, c.threshold, &err)) != ILLUME_OK) { set_error(err); return st; }
+    if ((st = e.set_trace_variant(c.variant)) != ILLUME_OK) return st;
   }
   return ILLUME_OK;
 }
@@ -442,10 +449,16 @@ void Server::tune(int base_key, double rays, double ms) {
     const std::vector<int> variants = kind == BVH_BINARY ? std::vector<int>{0, 3} : std::vector<int>{0, 1};
     // the tables' present size first: its windows need no reallocation
     const int other = current == (1 << 24) ? 1 << 25 : 1 << 24;
-    for (int cap : {current == (1 << 24) ? 1 << 24 : 1 << 25, other}) {
+    const int first = current == (1 << 24) ? 1 << 24 : 1 << 25;
+    for (int cap : {first, other}) {
       if (budget && reserved + engines_bytes() - held + (size_t)ntables * cap * kBytesPerPath > budget) continue;
-      for (int v : variants) t.candidates.push_back({cap, v});
+      for (int v : variants) t.candidates.push_back({cap, v, queue_slots, regen_threshold});
     }
+    // path regeneration at the first size: a quarter of the slots in flight, refilled
+    // every iteration or once the queue is down to a quarter (fewer bytes than the
+    // candidates above, so no budget check)
+    if (queue_slots == 0)
+      for (float thr : {1.0f, 0.25f}) t.candidates.push_back({first, variants[0], first / 4, thr});
     t.rate.assign(t.candidates.size(), 0.0);
     t.state = 1;
     t.idx = -1;
@@ -474,8 +487,11 @@ void Server::tune(int base_key, double rays, double ms) {
 // feeds the autotuner.
 int Server::finish_in_flight(std::vector<ServerJob*>* done) {
   if (in_flight.empty()) return ILLUME_OK;
-  for (Launched& l : in_flight)
+  for (Launched& l : in_flight) {
     ILLUME_CUDA_TRY(cudaMemcpyAsync(&l.total, l.se->eng->w.rays, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    ILLUME_CUDA_TRY(cudaMemcpyAsync(&l.iter_total, l.se->eng->w.counters + kCounterIterTotal, sizeof(int),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+  }
   ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   float ms = 0.0f;
   cudaEventElapsedTime(&ms, ev0, ev1);
@@ -485,6 +501,15 @@ int Server::finish_in_flight(std::vector<ServerJob*>* done) {
   for (Launched& l : in_flight) {
     const double rays = (double)(l.total - l.se->rays_seen);
     l.se->rays_seen = l.total;
+    if (l.se->eng->regen) {
+      // launches of the regeneration loops, known once the passes are done
+      const long long iters = (long long)l.iter_total - l.se->iters_seen;
+      const long long nl = Engine::launches_regen(l.k, iters, false);
+      totals.kernel_launches += nl;
+      for (int r = 0; r < l.se->eng->rows; ++r)
+        if (l.se->row_job[r]) jobs[l.se->row_job[r]]->stats.kernel_launches += nl;
+    }
+    l.se->iters_seen = l.iter_total;
     totals.rays += (int64_t)rays;
     rays_by_key[l.se->base_key] += rays;
     if ((st = retire(*l.se, done)) != ILLUME_OK) return st;
@@ -527,7 +552,8 @@ int Server::step(int* running_out) {
     }
     if (depth == 0 && e.paths_in_pass() == 0) continue;
     k = std::max(k, 1);
-    const int per_pass_launches = Engine::launches_per_pass(depth, e.any_nee());
+    // (under regeneration the launches are counted when the passes are done)
+    const int per_pass_launches = e.regen ? 0 : Engine::launches_per_pass(depth, e.any_nee());
     ILLUME_CUDA_TRY(cudaStreamWaitEvent(e.stream, ev0, 0));   // after admission's clears
     if ((st = e.run(k, depth)) != ILLUME_OK) return st;
     ILLUME_CUDA_TRY(cudaEventRecord(se.lane->done, e.stream));
@@ -535,7 +561,7 @@ int Server::step(int* running_out) {
     for (int r : active) jobs[se.row_job[r]]->stats.kernel_launches += (int64_t)k * per_pass_launches;
     totals.passes += k;
     totals.kernel_launches += (int64_t)k * per_pass_launches;
-    in_flight.push_back({&se, k, 0});
+    in_flight.push_back({&se, k, 0, 0});
   }
   ILLUME_CUDA_TRY(cudaEventRecord(ev1, ctx->stream));
   const double t = now_ms();
@@ -610,6 +636,14 @@ int Server::set_option(int option, int64_t value) {
       if (value < 1 || value > kMaxLanes) { set_error("lanes out of range"); return ILLUME_ERR_INVALID; }
       lanes = (int)value;
       return ILLUME_OK;
+    case ILLUME_SERVER_QUEUE_SLOTS:
+      if (value < 0 || value > (1 << 30)) { set_error("queue slots out of range"); return ILLUME_ERR_INVALID; }
+      queue_slots = (int)value;
+      return ILLUME_OK;
+    case ILLUME_SERVER_REGEN_THRESHOLD:
+      if (value < 0 || value > 1000) { set_error("regeneration threshold out of range (0-1000)"); return ILLUME_ERR_INVALID; }
+      regen_threshold = (float)value / 1000.0f;
+      return ILLUME_OK;
     default:
       set_error("unknown server option");
       return ILLUME_ERR_INVALID;
@@ -621,9 +655,15 @@ void Server::get_stats(illume_server_stats* out) const {
   out->path_capacity = 0;
   out->trace_variant = -1;
   out->tuned = 0;
+  out->queue_slots = 0;
+  out->regen_threshold = 0.0f;
   for (const auto& kv : engines) {
     out->path_capacity = std::max<int64_t>(out->path_capacity, kv.second.eng->cap);
     out->trace_variant = kv.second.eng->knobs.trace_variant;
+    if (kv.second.eng->regen) {
+      out->queue_slots = kv.second.eng->qcap;
+      out->regen_threshold = kv.second.eng->regen_threshold;
+    }
   }
   for (const auto& kv : tuners) out->tuned |= kv.second.state == 2;
   out->device_bytes = (int64_t)(engines_bytes() + reserved);

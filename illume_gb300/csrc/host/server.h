@@ -68,6 +68,7 @@ struct ServerEngine {
   int base_key = 0;                      // trace-kernel setting (engine_key)
   std::vector<int64_t> row_job;          // job id per row, 0 = free
   unsigned long long rays_seen = 0;      // engine ray total at the last read
+  int iters_seen = 0;                    // regeneration loop iterations at the last read
 };
 
 // Autotuner state of one trace-kernel setting (all its tables move together).
@@ -75,7 +76,8 @@ struct Tuner {
   int state = 0;                         // 0 not started, 1 measuring, 2 done
   int idx = 0, steps = 0;
   double rays = 0, ms = 0;
-  std::vector<std::pair<int, int>> candidates;   // (path slots per table, trace variant)
+  struct Candidate { int cap, variant, queue_slots; float threshold; };
+  std::vector<Candidate> candidates;             // path slots per table, trace variant, regeneration
   std::vector<double> rate;                      // rays per ms of each candidate
 };
 
@@ -88,6 +90,8 @@ struct Server {
   int autotune = 0;
   int trace_variant = -1;     // -1 = per-layout default
   int lanes = 4;              // job tables per trace-kernel setting
+  int queue_slots = 0;        // path regeneration: rays in flight per table (0 = off)
+  float regen_threshold = 1.0f;
   size_t reserved = 0;        // job footprints
   int64_t next_id = 1;
   std::map<int64_t, std::unique_ptr<ServerJob>> jobs;
@@ -97,7 +101,7 @@ struct Server {
   illume_server_stats totals{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // the passes of the last step, still running on the device when step() returned
-  struct Launched { ServerEngine* se; int k; unsigned long long total; };
+  struct Launched { ServerEngine* se; int k; unsigned long long total; int iter_total; };
   std::vector<Launched> in_flight;
 
   ~Server();

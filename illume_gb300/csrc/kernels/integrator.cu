@@ -125,38 +125,104 @@ __device__ __forceinline__ int tiled_pixel(int q, int w, int h) {
   return th * 4 * w + (r - right);
 }
 
+// Starts path i of the pass (0 <= i < the pass's paths) at position q of queue `par`.
+__device__ __forceinline__ void start_path(const WaveBuffers& w, int i, int q, int par) {
+  const int j = find_row(w.job_path_base, w.njobs, i);
+  const JobDesc& J = w.jobs[j];
+  const int npix = J.npix;
+  const int s = (i - J.path_base) / npix;
+  const CameraView& cam = J.cam;
+  // path i (in tile order) is this pixel's; its slot g keys the radiance
+  const int pixel = tiled_pixel(i - J.path_base - s * npix, cam.width, cam.height);
+  const int g = J.path_base + s * npix + pixel;
+  const int sample = J.sample_base + s;
+  RngStream rng;
+  rng.init((uint32_t)pixel, (uint32_t)sample, 0u, J.seed, J.job);
+  const int x = pixel % cam.width, y = pixel / cam.width;
+  const float left_edge = cam.left + cam.pixel_size * (float)x;
+  const float top_edge = cam.top - cam.pixel_size * (float)y;
+  const float r_x = left_edge + cam.pixel_size * rng.next();
+  const float r_y = top_edge - cam.pixel_size * rng.next();
+  V3 pos = v3(0.0f, 0.0f, 0.0f);
+  if (cam.aperture > FLT_EPSILON) {
+    const float u1 = rng.next(), u2 = rng.next();
+    pos = mul(sample_circle(u1, u2), cam.aperture);
+  }
+  const V3 origin = xform(cam.m, pos, 1.0f);
+  const V3 image_pos = xform(cam.m, v3(r_x, r_y, cam.dof), 1.0f);
+  const V3 dir = normalize(sub(image_pos, origin));
+  w.q_orig[par][q] = make_float4(origin.x, origin.y, origin.z, __int_as_float(g));
+  w.q_dir[par][q] = make_float4(dir.x, dir.y, dir.z, pack_job_medium(j, -1));
+  w.q_thr[par][q] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+  if (w.q_bounce[par]) w.q_bounce[par][q] = 0;
+  w.contrib[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
 __global__ void __launch_bounds__(256) k_raygen(WaveBuffers w) {
   const int total = w.counters[kCounterPaths];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-    const int j = find_row(w.job_path_base, w.njobs, i);
-    const JobDesc& J = w.jobs[j];
-    const int npix = J.npix;
-    const int s = (i - J.path_base) / npix;
-    const CameraView& cam = J.cam;
-    // queue position i holds the path of this pixel; its slot g keys the radiance
-    const int pixel = tiled_pixel(i - J.path_base - s * npix, cam.width, cam.height);
-    const int g = J.path_base + s * npix + pixel;
-    const int sample = J.sample_base + s;
-    RngStream rng;
-    rng.init((uint32_t)pixel, (uint32_t)sample, 0u, J.seed, J.job);
-    const int x = pixel % cam.width, y = pixel / cam.width;
-    const float left_edge = cam.left + cam.pixel_size * (float)x;
-    const float top_edge = cam.top - cam.pixel_size * (float)y;
-    const float r_x = left_edge + cam.pixel_size * rng.next();
-    const float r_y = top_edge - cam.pixel_size * rng.next();
-    V3 pos = v3(0.0f, 0.0f, 0.0f);
-    if (cam.aperture > FLT_EPSILON) {
-      const float u1 = rng.next(), u2 = rng.next();
-      pos = mul(sample_circle(u1, u2), cam.aperture);
-    }
-    const V3 origin = xform(cam.m, pos, 1.0f);
-    const V3 image_pos = xform(cam.m, v3(r_x, r_y, cam.dof), 1.0f);
-    const V3 dir = normalize(sub(image_pos, origin));
-    w.q_orig[0][i] = make_float4(origin.x, origin.y, origin.z, __int_as_float(g));
-    w.q_dir[0][i] = make_float4(dir.x, dir.y, dir.z, pack_job_medium(j, -1));
-    w.q_thr[0][i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    w.contrib[g] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) start_path(w, i, i, 0);
+}
+
+// ---- path regeneration (see launch.h) ----
+
+// The first batch: min(qcap, paths) paths into queue 0, iteration 0.
+__global__ void k_regen_start(WaveBuffers w) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const int total = w.counters[kCounterPaths];
+  const int n = total < w.qcap ? total : w.qcap;
+  w.counters[kCounterRegenN] = n;
+  w.counters[kCounterRegenFirst] = 0;
+  w.counters[kCounterRegenQ] = 0;
+  w.counters[0] = n;
+  w.counters[kCounterGen] = n;
+  w.counters[kCounterIter] = 0;
+  w.counters[kCounterMore] = 1;
+}
+
+// Camera rays of the batch the last plan chose, appended to the queue of the current
+// iteration.
+__global__ void __launch_bounds__(256) k_regen(WaveBuffers w) {
+  const int n = w.counters[kCounterRegenN], first = w.counters[kCounterRegenFirst], q0 = w.counters[kCounterRegenQ];
+  const int par = w.counters[kCounterIter] & 1;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    start_path(w, first + k, q0 + k, par);
+}
+
+// After an iteration's shading: the next batch of new paths and the loop condition. A
+// refill starts at least (1 - threshold) x qcap paths (or all that are left), and a queue
+// of at most qcap rays empties within `depth` iterations, so the loop needs fewer than
+// (paths / ((1 - threshold) qcap) + 2) (depth + 1) iterations; past twice that bound it
+// stops and raises counters[kCounterLoopLimit].
+__global__ void k_regen_plan(WaveBuffers w, cudaGraphConditionalHandle cond, int use_cond, int depth,
+                             float threshold) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const int it = w.counters[kCounterIter];
+  const int np = (it & 1) ^ 1;
+  const int total = w.counters[kCounterPaths], gen = w.counters[kCounterGen];
+  const int nq = w.counters[np];
+  int n = 0;
+  if (gen < total && (float)nq <= threshold * (float)w.qcap) {
+    n = w.qcap - nq;
+    if (n > total - gen) n = total - gen;
+    if (n < 0) n = 0;
   }
+  w.counters[kCounterRegenN] = n;
+  w.counters[kCounterRegenFirst] = gen;
+  w.counters[kCounterRegenQ] = nq;
+  w.counters[np] = nq + n;
+  w.counters[kCounterGen] = gen + n;
+  w.counters[kCounterIter] = it + 1;
+  w.counters[kCounterIterTotal] += 1;
+  bool more = nq + n > 0 || gen + n < total;
+  float fill = (1.0f - threshold) * (float)w.qcap;
+  if (fill < 1.0f) fill = 1.0f;
+  const long long bound = 2 * ((long long)((float)total / fill) + 2) * (long long)(depth + 1) + 16;
+  if (more && (long long)it + 1 >= bound) {
+    more = false;
+    w.counters[kCounterLoopLimit] = 1;
+  }
+  w.counters[kCounterMore] = more ? 1 : 0;
+  if (use_cond) cudaGraphSetConditional(cond, more ? 1u : 0u);
 }
 
 // A path's radiance: the reference estimator ends a path at its one contribution, so
@@ -181,8 +247,9 @@ struct BounceRng {
 // NEE: the instance with the next-event estimator compiled in (launched only when a job
 // of the pass uses it; its extra registers stay out of the reference path).
 template <int MINB, bool NEE>
-__global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) {
-  const int parity = bounce & 1;
+__global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce_arg) {
+  const int it = pass_iteration(w, bounce_arg);
+  const int parity = it & 1;
   const int* counts = ev_counts2(w, parity);
   __shared__ int prefix[EV_COUNT + 1];
   // block-level aggregation of the counters every warp would otherwise hit with its own
@@ -213,11 +280,13 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) 
     int myjob = -1;
     float4 no = make_float4(0, 0, 0, 0), nd = no, nt = no;
     float4 so = no, sd = no, sv = no;
+    int bounce = it;   // this ray's bounce (per ray under path regeneration)
     const unsigned live = __ballot_sync(0xffffffffu, gi < total);
     if (gi < total) {
       int cls = 0;
       while (cls + 1 < EV_COUNT && gi >= prefix[cls + 1]) ++cls;
-      const int i = w.evq[(size_t)cls * w.cap + (gi - prefix[cls])];
+      const int i = w.evq[(size_t)cls * w.qcap + (gi - prefix[cls])];
+      bounce = ray_bounce(w, parity, i, it);
       const float4 qo = w.q_orig[parity][i];
       const float4 qd = w.q_dir[parity][i];
       const float4 qt = w.q_thr[parity][i];
@@ -412,6 +481,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce) 
       w.q_orig[parity ^ 1][j] = no;
       w.q_dir[parity ^ 1][j] = nd;
       w.q_thr[parity ^ 1][j] = nt;
+      if (w.q_bounce[parity ^ 1]) w.q_bounce[parity ^ 1][j] = bounce + 1;
     }
   }
   __syncthreads();
@@ -601,6 +671,12 @@ void launch_plan(const WaveBuffers& w, cudaStream_t st) {
   k_plan<<<1, threads > 32 ? threads : 32, 0, st>>>(w);
 }
 void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st) { k_raygen<<<grid, 256, 0, st>>>(w); }
+void launch_regen_start(const WaveBuffers& w, cudaStream_t st) { k_regen_start<<<1, 32, 0, st>>>(w); }
+void launch_regen(const WaveBuffers& w, int grid, cudaStream_t st) { k_regen<<<grid, 256, 0, st>>>(w); }
+void launch_regen_plan(const WaveBuffers& w, cudaGraphConditionalHandle cond, bool use_cond, int depth, float threshold,
+                       cudaStream_t st) {
+  k_regen_plan<<<1, 32, 0, st>>>(w, cond, use_cond ? 1 : 0, depth, threshold);
+}
 void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st, bool nee) {
   const void* fn = shade_kernel_ptr(k.shade_variant, nee);
   void* args[] = {const_cast<WaveBuffers*>(&w), &bounce};

@@ -81,8 +81,12 @@ struct WaveBuffers {
   JobDesc* jobs;
   int* job_path_base;    // njobs + 1 prefix sums of the pass's paths (k_plan)
   int* job_pixel_base;   // njobs + 1 prefix sums of the pass's pixels (k_plan)
+  // Path regeneration: the bounce of each queued ray, by queue parity. Null: every ray of
+  // a queue is at the pass's bounce (the queues hold all the pass's paths at once).
+  int* q_bounce[2];
   int njobs;
-  int cap;               // path slots
+  int cap;               // path slots of one pass (per-path radiance)
+  int qcap;              // queue slots (rays in flight); equal to cap without regeneration
 };
 
 // counters[]: [0..1] queue sizes by parity, [2 + 16 * parity + class] event counts,
@@ -93,8 +97,30 @@ struct WaveBuffers {
 // the renderer after each render).
 static constexpr int kCounterPaths = 40;
 static constexpr int kCounterStackDrops = 50;
+// Path regeneration (a pass whose paths outnumber the queue slots): paths started so
+// far, the loop's iteration, the next batch of new paths (count, first path, first queue
+// position), whether the loop goes on, a flag set when its iteration bound ended a pass
+// (kept across passes, like the stack-overflow flag) and the loop's iterations since the
+// engine was made.
+static constexpr int kCounterGen = 51;
+static constexpr int kCounterIter = 52;
+static constexpr int kCounterRegenN = 53;
+static constexpr int kCounterRegenFirst = 54;
+static constexpr int kCounterRegenQ = 55;
+static constexpr int kCounterMore = 56;
+static constexpr int kCounterLoopLimit = 57;
+static constexpr int kCounterIterTotal = 58;
 static constexpr int kCounterPixels = 41;
 static constexpr int kCounterWords = 64;
+
+// Iteration of a stage launched with `bounce` (-1 under path regeneration: read from the
+// counters), and the bounce of queued ray i.
+__device__ __forceinline__ int pass_iteration(const WaveBuffers& w, int bounce) {
+  return bounce >= 0 ? bounce : w.counters[kCounterIter];
+}
+__device__ __forceinline__ int ray_bounce(const WaveBuffers& w, int parity, int i, int it) {
+  return w.q_bounce[parity] ? w.q_bounce[parity][i] : it;
+}
 
 // Settings shared by every job of a table (they select kernel instances).
 struct RenderKnobs {
@@ -108,6 +134,19 @@ int kernel_grid_blocks(const void* fn, int block, int device);
 
 void launch_plan(const WaveBuffers& w, cudaStream_t st);
 void launch_raygen(const WaveBuffers& w, int grid, cudaStream_t st);
+// Path regeneration. A pass runs as a loop of iterations (trace, shade, [shadow], plan of
+// the next new paths, their camera rays) over queues of qcap rays, new paths entering
+// the queue as earlier ones end, until every path of the pass has ended. The stages take
+// bounce = -1 and read the iteration from the counters. regen_start: the first
+// min(qcap, paths) paths; regen_plan: after an iteration's shading, starts new paths when
+// the next queue holds at most threshold x qcap rays (filling it to qcap), and sets the
+// loop's condition (through `cond` when launched inside a graph's while node, else only
+// counters[kCounterMore]); the loop ends early, raising counters[kCounterLoopLimit], at
+// an iteration bound derived from the paths, qcap, threshold and `depth`.
+void launch_regen_start(const WaveBuffers& w, cudaStream_t st);
+void launch_regen(const WaveBuffers& w, int grid, cudaStream_t st);
+void launch_regen_plan(const WaveBuffers& w, cudaGraphConditionalHandle cond, bool use_cond, int depth, float threshold,
+                       cudaStream_t st);
 void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st,
                   bool count_visits = false);
 void launch_shade(const WaveBuffers& w, const RenderKnobs& k, int bounce, int grid, cudaStream_t st, bool nee = false);

@@ -105,8 +105,9 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
     set_error("illume_render_noalloc runs the reference estimator only (no shadow-ray scratch)");
     return ILLUME_ERR_UNSUPPORTED;
   }
-  if (p.samples_per_pass > 1 || p.engines > 1) {
-    set_error("illume_render_noalloc renders one sample per pass on one engine (samples_per_pass and engines must be 0 or 1)");
+  if (p.samples_per_pass > 1 || p.engines > 1 || p.queue_slots > 0) {
+    set_error("illume_render_noalloc renders one sample per pass on one engine without path regeneration "
+              "(samples_per_pass and engines must be 0 or 1, queue_slots 0)");
     return ILLUME_ERR_UNSUPPORTED;
   }
   const RenderKnobs k = render_knobs(p);
@@ -158,6 +159,7 @@ extern "C" int illume_render_noalloc(illume_context* ctx, illume_scene* scene, c
     return ILLUME_ERR_INVALID;
   }
   w.cap = cap;
+  w.qcap = cap;
   w.njobs = 1;
   Accumulators acc{};
   acc.sum32 = d_sum;

@@ -603,8 +603,11 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 // found closer than tmax (occlusion; with the binary and 4-wide layouts).
 // PS, NF: options of the 4-wide traversal (traverse_bvh4_ww).
 // FR: box-test reciprocals from the hardware approximation (fast_rcp).
+// SI: instances visited nearest box entry first (scenes of 2 to kSortedInstances
+// instances), stopping at the first box that starts beyond the best hit; see below.
+static constexpr int kSortedInstances = 16;
 template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false, bool ANY = false, bool PS = false,
-          bool NF = false, bool FR = false>
+          bool NF = false, bool FR = false, bool SI = false>
 __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d, int isect, void* stack_mem,
                                                  VisitCount* vcp = nullptr, float tmax = FLT_MAX) {
   VisitCount vc;
@@ -629,20 +632,56 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
   TraceRay wr;
   wr.o = o; wr.d = d;
   wr.idir = FR ? v3(fast_rcp(d.x), fast_rcp(d.y), fast_rcp(d.z)) : v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
-  for (int i = 0; i < sc.num_instances; ++i) {
+  // One instance's triangles. The walk keeps the index-order result whatever the order
+  // of visits: a hit at the best distance replaces the best when it comes from an
+  // instance of lower index (its mesh best starts with prim INT_MAX, so an equal t wins),
+  // never when the best is a sphere or an instance of lower index (prim -1).
+  auto visit = [&](int i) {
     const DevInstance& in = sc.instances[i];
-    float te;
-    if (!box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) continue;
     TraceRay r;
     setup_ray<FR>(r, xform(in.inv, o, 1.0f), xform(in.inv, d, 0.0f), isect);
-    MeshBest b{h.t, -1, 0.0f, 0.0f};
+    const int seed = h.geom > i ? INT_MAX : -1;
+    MeshBest b{h.t, seed, 0.0f, 0.0f};
     const DevMesh& m = sc.meshes[in.mesh];
     if (KIND == BVH_WIDE8) traverse_wide<COUNT>(m, r, isect, b, reinterpret_cast<uint2*>(stack_mem), vc);
     else if (KIND == BVH_WIDE4) traverse_bvh4_ww<COUNT, ANY, PS, NF>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else if (WW) traverse_bvh2_ww<COUNT, FMA, ANY>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else traverse_bvh2<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
-    if (b.prim >= 0) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }
-    if (ANY && h.geom != -1) break;
+    if (b.prim >= 0 && b.prim != INT_MAX) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }
+  };
+  if (SI && sc.num_instances > 1 && sc.num_instances <= kSortedInstances) {
+    // the boxes the ray enters, then nearest entry first (equal entries by index)
+    float key[kSortedInstances];
+    int idx[kSortedInstances];
+    int n = 0;
+    for (int i = 0; i < sc.num_instances; ++i) {
+      const DevInstance& in = sc.instances[i];
+      float te;
+      if (!box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) continue;
+      key[n] = te;
+      idx[n] = i;
+      ++n;
+    }
+    for (int k = 0; k < n; ++k) {
+      int m = k;
+      for (int j = k + 1; j < n; ++j)
+        if (key[j] < key[m] || (key[j] == key[m] && idx[j] < idx[m])) m = j;
+      const float km = key[m];
+      const int im = idx[m];
+      key[m] = key[k];
+      idx[m] = idx[k];
+      if (!(km <= h.t * kExitSlack)) break;   // this box and every later one start beyond the best hit
+      visit(im);
+      if (ANY && h.geom != -1) break;
+    }
+  } else {
+    for (int i = 0; i < sc.num_instances; ++i) {
+      const DevInstance& in = sc.instances[i];
+      float te;
+      if (!box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) continue;
+      visit(i);
+      if (ANY && h.geom != -1) break;
+    }
   }
   if (vcp) {
     if (COUNT) *vcp = vc;

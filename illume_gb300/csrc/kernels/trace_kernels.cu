@@ -45,9 +45,10 @@ __device__ __forceinline__ int event_class(const WaveBuffers& w, const JobDesc& 
 // whose rays finish early take over the remaining work.
 // PS, NF (4-wide only): see traverse_bvh4_ww.
 template <int KIND, bool COUNT, int MINB = 1, bool OPT = false, bool WW = false, bool PS = false, bool NF = false,
-          bool FR = false>
+          bool FR = false, bool SI = false>
 __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs k, int bounce) {
-  const int parity = bounce & 1;
+  const int it = pass_iteration(w, bounce);
+  const int parity = it & 1;
   const int n = w.counters[parity];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     w.counters[parity ^ 1] = 0;
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
     const SceneView& sc = J.sc;
     VisitCount vc;
     const HitRecord h =
-        closest_hit<KIND, COUNT, OPT, WW, false, PS, NF, FR>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect,
+        closest_hit<KIND, COUNT, OPT, WW, false, PS, NF, FR, SI>(sc, v3(qo.x, qo.y, qo.z), v3(qd.x, qd.y, qd.z), k.isect,
                                                          stack, &vc);
     if (COUNT) {
       my_nodes += vc.nodes;
@@ -88,11 +89,12 @@ __global__ void __launch_bounds__(128, MINB) k_trace(WaveBuffers w, RenderKnobs 
       if (lane == __ffs(mask) - 1) my_slots += 32ull * longest;
     }
     if (vc.dropped) atomicOr(w.counters + kCounterStackDrops, 1);
-    const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
+    const int cls = event_class(w, J, sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1,
+                                ray_bounce(w, parity, i, it));
     w.hit[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
     w.hit_geom[i] = h.geom;
     const int pos = warp_append_keyed(mask, cls, counts);
-    w.evq[(size_t)cls * w.cap + pos] = i;
+    w.evq[(size_t)cls * w.qcap + pos] = i;
   }
   if (COUNT) {
     for (int off = 16; off > 0; off >>= 1) {
@@ -118,7 +120,8 @@ enum { RF_IDLE = 0, RF_INSTANCE = 1, RF_TRAVERSE = 2, RF_FINISH = 3 };
 template <bool COUNT>
 __global__ void __launch_bounds__(128, 8) k_trace_refill(WaveBuffers w, RenderKnobs k, int bounce) {
   const unsigned FULL = 0xffffffffu;
-  const int parity = bounce & 1;
+  const int it = pass_iteration(w, bounce);
+  const int parity = it & 1;
   const int n = w.counters[parity];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     w.counters[parity ^ 1] = 0;
@@ -213,11 +216,12 @@ __global__ void __launch_bounds__(128, 8) k_trace_refill(WaveBuffers w, RenderKn
       const JobDesc& J = w.jobs[job];
       const float4 qo = w.q_orig[parity][slot], qd = w.q_dir[parity][slot];
       const int packed = __float_as_int(qd.w);
-      const int cls = event_class(w, J, J.sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1, bounce);
+      const int cls = event_class(w, J, J.sc, h, __float_as_int(qo.w), (packed & ((1 << kMediumBits) - 1)) - 1,
+                                  ray_bounce(w, parity, slot, it));
       w.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
       w.hit_geom[slot] = h.geom;
       const int pos = warp_append_keyed(fin, cls, counts);
-      w.evq[(size_t)cls * w.cap + pos] = slot;
+      w.evq[(size_t)cls * w.qcap + pos] = slot;
       phase = RF_IDLE;
       slot = -1;
     }
@@ -242,7 +246,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_refill(WaveBuffers w, RenderKn
 // warps take 32 rays at a time from a counter (counters[48 + parity]).
 template <int KIND>
 __global__ void __launch_bounds__(128, 8) k_shadow(WaveBuffers w, RenderKnobs k, int bounce) {
-  const int parity = bounce & 1;
+  const int parity = pass_iteration(w, bounce) & 1;
   const int n = w.counters[46 + parity];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     w.counters[46 + (parity ^ 1)] = 0;
@@ -292,7 +296,8 @@ template <bool COUNT, bool HOOK>
 __global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, const SceneView* hook_view, RenderKnobs k, int bounce,
                                                   const float4* hook_rays, int hook_n, illume_hit* hook_out) {
   const unsigned FULL = 0xffffffffu;
-  const int parity = bounce & 1;
+  const int it = HOOK ? 0 : pass_iteration(w, bounce);
+  const int parity = it & 1;
   const int n = HOOK ? hook_n : w.counters[parity];
   if (!HOOK && blockIdx.x == 0 && threadIdx.x == 0) w.counters[parity ^ 1] = 0;
   int* counts = HOOK ? nullptr : ev_counts(w, parity);
@@ -400,11 +405,11 @@ __global__ void __launch_bounds__(128) k_trace_sm(WaveBuffers w, const SceneView
         out.pad[0] = out.pad[1] = 0;
         hook_out[slot] = out;
       } else {
-        const int cls = event_class(w, *jp, *scp, h, g, medium, bounce);
+        const int cls = event_class(w, *jp, *scp, h, g, medium, ray_bounce(w, parity, slot, it));
         w.hit[slot] = make_float4(h.t, h.u, h.v, __int_as_float(h.prim));
         w.hit_geom[slot] = h.geom;
         const int pos = warp_append_keyed(fin, cls, counts);
-        w.evq[(size_t)cls * w.cap + pos] = slot;
+        w.evq[(size_t)cls * w.qcap + pos] = slot;
       }
       phase = PH_IDLE;
       slot = -1;
@@ -464,6 +469,7 @@ const void* trace_kernel_ptr(int bvh_kind, int variant) {
     if (variant == 2) return (const void*)k_trace<BVH_WIDE4, false, 8, true>;
     if (variant == 3) return (const void*)k_trace<BVH_WIDE4, false, 6, true, false, false, true>;
     if (variant == 4) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true, true>;
+    if (variant == 5) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true, true, true>;
     return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true>;
   }
   if (bvh_kind == BVH_WIDE8)
@@ -490,6 +496,9 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
     } else if (k.trace_variant == 4) {
       if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE4, false, 8, true, false, false, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    } else if (k.trace_variant == 5) {
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true, false, false, true, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
     } else {
       if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE4, false, 8, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define ILLUME_ABI_VERSION 2
+#define ILLUME_ABI_VERSION 3
 
 enum illume_status {
   ILLUME_OK = 0,
@@ -172,8 +172,9 @@ typedef struct {
                                * memory (default); 1 = four compare-swaps instead of five in
                                * the child ordering; 2 = lo / hi planes selected per child
                                * box; 3 = at most 80 registers; 4 = variant 0 with box-test
-                               * reciprocals from the hardware approximation. Other layouts
-                               * ignore it. */
+                               * reciprocals from the hardware approximation; 5 = variant 4
+                               * with the instances a ray enters visited nearest first
+                               * (scenes of 2 to 16 instances). Other layouts ignore it. */
   int32_t shade_variant;      /* 0 = the measured best register bound (default), 1 = the
                                * compiler's choice, 2 / 3 / 4 = at most 80 / 72 / 64 registers */
   int32_t estimator;          /* illume_estimator */
@@ -184,6 +185,16 @@ typedef struct {
                                * samples per pass.
                                * The image does not depend on it. The server ignores it
                                * (ILLUME_SERVER_LANES). */
+  /* Path regeneration (no counterpart in the reference, whose passes hold one sample of
+   * every pixel): with queue_slots > 0 and below a pass's paths, the wavefront queues hold
+   * queue_slots rays, and each pass runs as a loop on the device (one graph launch: a
+   * while node) in which new paths of the pass enter the queue as earlier ones end,
+   * whenever the next queue holds at most regen_threshold x queue_slots rays (0 <=
+   * regen_threshold <= 1; 1 = refill every iteration). 0 = every path of a pass starts
+   * at once (the default). The image does not depend on either. A loop that reaches its
+   * iteration bound (never expected) makes the render return ILLUME_ERR_TIMEOUT. */
+  int32_t queue_slots;
+  float regen_threshold;
 } illume_render_params;
 
 typedef struct {
@@ -302,8 +313,8 @@ int illume_renderer_profile(illume_renderer* r, int count_visits, illume_profile
  * pass, FP32 accumulation in sample order, accum_mode must be ILLUME_ACCUM_FP32) and
  * writes the per-pixel sum of radiance (3 floats per pixel) to the caller's device
  * buffer d_sum. Asynchronous on the context's stream. Takes the parameter checks of
- * illume_renderer_create; samples_per_pass and engines above 1 and the next-event
- * estimator are rejected with ILLUME_ERR_UNSUPPORTED. The first call on a context looks
+ * illume_renderer_create; samples_per_pass and engines above 1, queue_slots above 0 and
+ * the next-event estimator are rejected with ILLUME_ERR_UNSUPPORTED. The first call on a context looks
  * up the array's device address and caches it with the launch sizes; make it before any
  * stream capture. After a device reset (which invalidates every handle) the address is
  * looked up again. All calls share the array: calls whose GPU work overlaps race, so
@@ -372,10 +383,17 @@ typedef enum {
   ILLUME_SERVER_PASSES_PER_STEP = 1,  /* passes per illume_server_step (default 1) */
   ILLUME_SERVER_AUTOTUNE = 2,         /* 1 = choose path slots and trace kernel from measured throughput */
   ILLUME_SERVER_TRACE_VARIANT = 3,    /* trace kernel variant (-1 = default) */
-  ILLUME_SERVER_LANES = 4             /* job tables per trace-kernel setting, each on its own
+  ILLUME_SERVER_LANES = 4,            /* job tables per trace-kernel setting, each on its own
                                        * stream, whose passes overlap (1-16, default 4;
                                        * illume_render_batch uses 16); a table
                                        * is created only when every existing one has work */
+  ILLUME_SERVER_QUEUE_SLOTS = 5,      /* path regeneration in every table: rays in flight
+                                       * (0 = off, the default; see
+                                       * illume_render_params.queue_slots) */
+  ILLUME_SERVER_REGEN_THRESHOLD = 6   /* its refill threshold in thousandths (0-1000,
+                                       * default 1000). The autotuner also tries
+                                       * regeneration at a quarter of the path slots with
+                                       * thresholds 1 and 1/4. */
 } illume_server_option;
 int illume_server_set_option(illume_server* s, int option, int64_t value);
 
@@ -389,6 +407,8 @@ typedef struct {
   int32_t trace_variant;      /* trace kernel variant in use */
   int32_t tuned;              /* 1 once the autotuner has chosen */
   int64_t device_bytes;       /* bytes the server holds on the device */
+  int32_t queue_slots;        /* path regeneration in use: rays in flight per table (0 = off) */
+  float regen_threshold;      /* and its refill threshold */
 } illume_server_stats;
 int illume_server_get_stats(const illume_server* s, illume_server_stats* out);
 

@@ -48,12 +48,15 @@ def alone(ctx, sc, p):
 @pytest.mark.parametrize("bvh", [C.BVH_WIDE4, C.BVH_BINARY])
 def test_same_alone_and_in_the_mix(ctx, scenes, bvh):
     """Every server setting (slots, passes per step, each trace kernel variant of the
-    layout) gives each job the image it gets alone with the default settings."""
+    layout, path regeneration) gives each job the image it gets alone with the default
+    settings."""
     from illume_gb300.api import Server
     jobs = job_list(scenes, bvh)
     ref = [alone(ctx, sc, p) for sc, p in jobs]
     variants = [{"trace_variant": v} for v in ((1, 2, 3, 4) if bvh == C.BVH_BINARY else (1, 2, 3))]
-    for opts in [{}, {"path_capacity": 40000}, {"passes_per_step": 4}, {"lanes": 1}, {"lanes": 3}] + variants:
+    regen = [{"queue_slots": 5000}, {"queue_slots": 20000, "regen_threshold_permille": 300},
+             {"path_capacity": 40000, "queue_slots": 9000, "regen_threshold_permille": 0, "lanes": 2}]
+    for opts in [{}, {"path_capacity": 40000}, {"passes_per_step": 4}, {"lanes": 1}, {"lanes": 3}] + variants + regen:
         srv = Server(ctx, **opts)
         ids = [srv.submit(sc, p) for sc, p in jobs]
         srv.run()

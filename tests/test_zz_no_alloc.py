@@ -98,6 +98,7 @@ def test_noalloc_rejects_what_it_does_not_take(ctx):
     out = torch.zeros(3 * 64, dtype=torch.float32, device="cuda:0")
     L = C.lib()
     for field, value, status in [("samples_per_pass", 4, C.ERR_UNSUPPORTED), ("engines", 2, C.ERR_UNSUPPORTED),
+                                 ("queue_slots", 1024, C.ERR_UNSUPPORTED),
                                  ("trace_variant", 9, C.ERR_INVALID), ("shade_variant", 9, C.ERR_INVALID),
                                  ("accum_mode", C.ACCUM_FP64, C.ERR_INVALID)]:
         p = scene.default_params(1, 4)
