@@ -37,7 +37,7 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if (p.intersector != ISECT_MT && p.intersector != ISECT_WATERTIGHT) { *err = "unknown intersector"; return ILLUME_ERR_INVALID; }
   if (p.bvh_kind < 0 || p.bvh_kind > 3) { *err = "unknown BVH kind"; return ILLUME_ERR_INVALID; }
   if (p.bvh_kind == BVH_BINARY && (p.trace_variant < 0 || p.trace_variant > 4)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
-  if (p.bvh_kind == 3 && (p.trace_variant < 0 || p.trace_variant > 5)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
+  if (p.bvh_kind == 3 && (p.trace_variant < 0 || p.trace_variant > 4)) { *err = "unknown trace kernel variant"; return ILLUME_ERR_INVALID; }
   if (p.accum_mode < ACCUM_FP32 || p.accum_mode > ACCUM_FP64) { *err = "unknown accumulation mode"; return ILLUME_ERR_INVALID; }
   if (p.samples_per_pass < 0) { *err = "negative samples per pass"; return ILLUME_ERR_INVALID; }
   if (p.shade_variant < 0 || p.shade_variant > 4) { *err = "unknown shade kernel variant"; return ILLUME_ERR_INVALID; }
@@ -62,7 +62,9 @@ RenderKnobs render_knobs(const illume_render_params& p) {
   RenderKnobs k{};
   k.isect = p.intersector;
   k.bvh_kind = p.bvh_kind == 2 ? BVH_WIDE8 : (p.bvh_kind == 3 ? BVH_WIDE4 : p.bvh_kind);
-  k.trace_variant = p.bvh_kind == 2 ? 1 : (p.bvh_kind == BVH_BINARY || p.bvh_kind == 3 ? p.trace_variant : 0);
+  k.trace_variant = p.bvh_kind == 2 ? 1
+                    : (p.bvh_kind == 1 ? (p.trace_variant == 2 ? 2 : 0)
+                                       : (p.bvh_kind == BVH_BINARY || p.bvh_kind == 3 ? p.trace_variant : 0));
   k.shade_variant = p.shade_variant;
   return k;
 }

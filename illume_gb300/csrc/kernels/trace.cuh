@@ -412,6 +412,14 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
 // ---- 8-wide quantised BVH ----
 __device__ __forceinline__ float exp2i(uint8_t biased) { return __int_as_float((int)biased << 23); }
 
+// Byte k (0-3, known at compile time in the unrolled loops) of `word` as a float, exact:
+// a byte permute builds 2^23 + q (the byte in the low mantissa bits under the exponent
+// of 2^23) and one subtraction removes 2^23. Integer-to-float conversions run at a
+// fraction of the rate of these two instructions.
+__device__ __forceinline__ float byte_as_float(uint32_t word, int k) {
+  return __int_as_float((int)__byte_perm(word, 0x4B000000u, 0x7650u | (unsigned)k)) - 8388608.0f;
+}
+
 template <bool COUNT>
 __device__ __forceinline__ void traverse_wide(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
                                               uint2* stack, VisitCount& vc) {
@@ -443,9 +451,10 @@ __device__ __forceinline__ void traverse_wide(const DevMesh& m, const TraceRay& 
       const uint32_t me = (meta[w] >> sh) & 0xff;
       const bool inner = (imask >> s) & 1;
       if (!inner && me == 0) continue;
-      const float lx = (float)((qlx[w] >> sh) & 0xff), hx = (float)((qhx[w] >> sh) & 0xff);
-      const float ly = (float)((qly[w] >> sh) & 0xff), hy = (float)((qhy[w] >> sh) & 0xff);
-      const float lz = (float)((qlz[w] >> sh) & 0xff), hz = (float)((qhz[w] >> sh) & 0xff);
+      const int kb = s & 3;
+      const float lx = byte_as_float(qlx[w], kb), hx = byte_as_float(qhx[w], kb);
+      const float ly = byte_as_float(qly[w], kb), hy = byte_as_float(qhy[w], kb);
+      const float lz = byte_as_float(qlz[w], kb), hz = byte_as_float(qhz[w], kb);
       const float nx = r.idir.x >= 0.0f ? lx : hx, fx = r.idir.x >= 0.0f ? hx : lx;
       const float ny = r.idir.y >= 0.0f ? ly : hy, fy = r.idir.y >= 0.0f ? hy : ly;
       const float nz = r.idir.z >= 0.0f ? lz : hz, fz = r.idir.z >= 0.0f ? hz : lz;
@@ -551,12 +560,13 @@ __device__ __forceinline__ void wide_node_step(const DevMesh& m, const TraceRay&
     const int w = s8 >> 2, sh = (s8 & 3) * 8;
     const uint32_t me = (__float_as_uint(w ? q1.w : q1.z) >> sh) & 0xff;
     const bool inner = (imask >> s8) & 1;
-    const float lx = (float)((__float_as_uint(w ? q2.y : q2.x) >> sh) & 0xff);
-    const float ly = (float)((__float_as_uint(w ? q2.w : q2.z) >> sh) & 0xff);
-    const float lz = (float)((__float_as_uint(w ? q3.y : q3.x) >> sh) & 0xff);
-    const float hx = (float)((__float_as_uint(w ? q3.w : q3.z) >> sh) & 0xff);
-    const float hy = (float)((__float_as_uint(w ? q4.y : q4.x) >> sh) & 0xff);
-    const float hz = (float)((__float_as_uint(w ? q4.w : q4.z) >> sh) & 0xff);
+    const int kb = s8 & 3;
+    const float lx = byte_as_float(__float_as_uint(w ? q2.y : q2.x), kb);
+    const float ly = byte_as_float(__float_as_uint(w ? q2.w : q2.z), kb);
+    const float lz = byte_as_float(__float_as_uint(w ? q3.y : q3.x), kb);
+    const float hx = byte_as_float(__float_as_uint(w ? q3.w : q3.z), kb);
+    const float hy = byte_as_float(__float_as_uint(w ? q4.y : q4.x), kb);
+    const float hz = byte_as_float(__float_as_uint(w ? q4.w : q4.z), kb);
     const float nx = r.idir.x >= 0.0f ? lx : hx, fx = r.idir.x >= 0.0f ? hx : lx;
     const float ny = r.idir.y >= 0.0f ? ly : hy, fy = r.idir.y >= 0.0f ? hy : ly;
     const float nz = r.idir.z >= 0.0f ? lz : hz, fz = r.idir.z >= 0.0f ? hz : lz;
@@ -603,8 +613,9 @@ __device__ __forceinline__ void wide_tri_step(const DevMesh& m, const TraceRay& 
 // found closer than tmax (occlusion; with the binary and 4-wide layouts).
 // PS, NF: options of the 4-wide traversal (traverse_bvh4_ww).
 // FR: box-test reciprocals from the hardware approximation (fast_rcp).
-// SI: instances visited nearest box entry first (scenes of 2 to kSortedInstances
-// instances), stopping at the first box that starts beyond the best hit; see below.
+// SI: instances visited nearest box entry first (scenes of 3 to kSortedInstances
+// instances; with two the index order costs less than sorting), stopping at the first
+// box that starts beyond the best hit; see below.
 static constexpr int kSortedInstances = 16;
 template <int KIND, bool COUNT = false, bool FMA = false, bool WW = false, bool ANY = false, bool PS = false,
           bool NF = false, bool FR = false, bool SI = false>
@@ -632,11 +643,43 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
   TraceRay wr;
   wr.o = o; wr.d = d;
   wr.idir = FR ? v3(fast_rcp(d.x), fast_rcp(d.y), fast_rcp(d.z)) : v3(safe_rcp(d.x), safe_rcp(d.y), safe_rcp(d.z));
-  // One instance's triangles. The walk keeps the index-order result whatever the order
-  // of visits: a hit at the best distance replaces the best when it comes from an
-  // instance of lower index (its mesh best starts with prim INT_MAX, so an equal t wins),
-  // never when the best is a sphere or an instance of lower index (prim -1).
-  auto visit = [&](int i) {
+  // Instances in index order, or (SI) the boxes the ray enters sorted by entry distance
+  // (equal entries by index), stopping at the first box that starts beyond the best hit.
+  // The walk keeps the index-order result whatever the order of visits: a hit at the
+  // best distance replaces the best when it comes from an instance of lower index (its
+  // mesh best starts with prim INT_MAX, so an equal t wins), never when the best is a
+  // sphere or an instance of lower index (prim -1).
+  const bool sorted = SI && sc.num_instances > 2 && sc.num_instances <= kSortedInstances;
+  float key[SI ? kSortedInstances : 1];
+  int idx[SI ? kSortedInstances : 1];
+  int count = sc.num_instances;
+  if (sorted) {
+    count = 0;
+    for (int i = 0; i < sc.num_instances; ++i) {
+      const DevInstance& in = sc.instances[i];
+      float te;
+      if (!box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) continue;
+      key[count] = te;
+      idx[count] = i;
+      ++count;
+    }
+  }
+  for (int k = 0; k < count; ++k) {
+    int i = k;
+    if (sorted) {
+      int m = k;
+      for (int j = k + 1; j < count; ++j)
+        if (key[j] < key[m] || (key[j] == key[m] && idx[j] < idx[m])) m = j;
+      const float km = key[m];
+      i = idx[m];
+      key[m] = key[k];
+      idx[m] = idx[k];
+      if (!(km <= h.t * kExitSlack)) break;   // this box and every later one start beyond the best hit
+    } else {
+      const DevInstance& in = sc.instances[i];
+      float te;
+      if (!box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) continue;
+    }
     const DevInstance& in = sc.instances[i];
     TraceRay r;
     setup_ray<FR>(r, xform(in.inv, o, 1.0f), xform(in.inv, d, 0.0f), isect);
@@ -648,40 +691,7 @@ __device__ __forceinline__ HitRecord closest_hit(const SceneView& sc, V3 o, V3 d
     else if (WW) traverse_bvh2_ww<COUNT, FMA, ANY>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     else traverse_bvh2<COUNT, FMA>(m, r, isect, b, reinterpret_cast<int*>(stack_mem), vc);
     if (b.prim >= 0 && b.prim != INT_MAX) { h.t = b.t; h.u = b.u; h.v = b.v; h.prim = b.prim; h.geom = i; }
-  };
-  if (SI && sc.num_instances > 1 && sc.num_instances <= kSortedInstances) {
-    // the boxes the ray enters, then nearest entry first (equal entries by index)
-    float key[kSortedInstances];
-    int idx[kSortedInstances];
-    int n = 0;
-    for (int i = 0; i < sc.num_instances; ++i) {
-      const DevInstance& in = sc.instances[i];
-      float te;
-      if (!box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) continue;
-      key[n] = te;
-      idx[n] = i;
-      ++n;
-    }
-    for (int k = 0; k < n; ++k) {
-      int m = k;
-      for (int j = k + 1; j < n; ++j)
-        if (key[j] < key[m] || (key[j] == key[m] && idx[j] < idx[m])) m = j;
-      const float km = key[m];
-      const int im = idx[m];
-      key[m] = key[k];
-      idx[m] = idx[k];
-      if (!(km <= h.t * kExitSlack)) break;   // this box and every later one start beyond the best hit
-      visit(im);
-      if (ANY && h.geom != -1) break;
-    }
-  } else {
-    for (int i = 0; i < sc.num_instances; ++i) {
-      const DevInstance& in = sc.instances[i];
-      float te;
-      if (!box_hit(in.lo[0], in.lo[1], in.lo[2], in.hi[0], in.hi[1], in.hi[2], wr, h.t, te)) continue;
-      visit(i);
-      if (ANY && h.geom != -1) break;
-    }
+    if (ANY && h.geom != -1) break;
   }
   if (vcp) {
     if (COUNT) *vcp = vc;

@@ -468,12 +468,13 @@ const void* trace_kernel_ptr(int bvh_kind, int variant) {
     if (variant == 1) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, true, true>;
     if (variant == 2) return (const void*)k_trace<BVH_WIDE4, false, 8, true>;
     if (variant == 3) return (const void*)k_trace<BVH_WIDE4, false, 6, true, false, false, true>;
-    if (variant == 4) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true, true>;
-    if (variant == 5) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true, true, true>;
-    return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true>;
+    if (variant == 4) return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true>;
+    return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true, true, true>;
   }
-  if (bvh_kind == BVH_WIDE8)
+  if (bvh_kind == BVH_WIDE8) {
+    if (variant == 2) return (const void*)k_trace<BVH_WIDE8, false, 8>;
     return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
+  }
   if (variant == 1) return (const void*)k_trace<BVH_BINARY, false>;
   if (variant == 2) return (const void*)k_trace<BVH_BINARY, false, 8>;
   if (variant == 3) return (const void*)k_trace<BVH_BINARY, false, 8, true>;
@@ -494,14 +495,11 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
       if (count_visits) k_trace<BVH_WIDE4, true, 6, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE4, false, 6, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
     } else if (k.trace_variant == 4) {
-      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
-      else k_trace<BVH_WIDE4, false, 8, true, false, false, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
-    } else if (k.trace_variant == 5) {
-      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
-      else k_trace<BVH_WIDE4, false, 8, true, false, false, true, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
-    } else {
       if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE4, false, 8, true, false, false, true><<<grid, 128, 0, st>>>(w, k, bounce);
+    } else {
+      if (count_visits) k_trace<BVH_WIDE4, true, 8, true, false, false, true, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE4, false, 8, true, false, false, true, true, true><<<grid, 128, 0, st>>>(w, k, bounce);
     }
     return;
   }
@@ -509,6 +507,9 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
     if (k.trace_variant == 1) {
       if (count_visits) k_trace_sm<true, false><<<grid, 128, 0, st>>>(w, nullptr, k, bounce, nullptr, 0, nullptr);
       else k_trace_sm<false, false><<<grid, 128, 0, st>>>(w, nullptr, k, bounce, nullptr, 0, nullptr);
+    } else if (k.trace_variant == 2) {
+      if (count_visits) k_trace<BVH_WIDE8, true, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE8, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
     } else {
       if (count_visits) k_trace<BVH_WIDE8, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE8, false><<<grid, 128, 0, st>>>(w, k, bounce);

@@ -171,10 +171,14 @@ typedef struct {
                                * near / far planes loaded by per-ray offsets, stack in local
                                * memory (default); 1 = four compare-swaps instead of five in
                                * the child ordering; 2 = lo / hi planes selected per child
-                               * box; 3 = at most 80 registers; 4 = variant 0 with box-test
-                               * reciprocals from the hardware approximation; 5 = variant 4
-                               * with the instances a ray enters visited nearest first
-                               * (scenes of 2 to 16 instances). Other layouts ignore it. */
+                               * box; 3 = at most 80 registers; 4 = variant 0 with exact
+                               * box-test reciprocals and the instances walked in index
+                               * order (variant 0 takes the hardware's approximate
+                               * reciprocal and, in scenes of 3 to 16 instances, visits
+                               * the instances a ray enters nearest box entry first).
+                               * 8-wide (ILLUME_BVH_WIDE8): 2 = at most 64 registers
+                               * (others: the compiler's choice). The persistent 8-wide
+                               * layout ignores it. */
   int32_t shade_variant;      /* 0 = the measured best register bound (default), 1 = the
                                * compiler's choice, 2 / 3 / 4 = at most 80 / 72 / 64 registers */
   int32_t estimator;          /* illume_estimator */

@@ -7,9 +7,10 @@ sample, bounce) and its job, and each pixel's samples are still summed in sample
 so the image must be bit-identical to the render without regeneration, for every queue
 size and threshold, accumulation mode, estimator, engine count and progressive call.
 
-Sorted instance walk (4-wide trace variant 5): the instances a ray enters are visited
-nearest box entry first; ties between instances still go to the lower index, so images
-must equal the index-order walk's, including scenes whose instances coincide."""
+Sorted instance walk (the default 4-wide trace kernel; variant 4 walks in index order):
+the instances a ray enters are visited nearest box entry first; ties between instances
+still go to the lower index, so images must equal the index-order walk's, including
+scenes whose instances coincide."""
 import numpy as np
 import pytest
 
@@ -139,7 +140,7 @@ def test_sorted_instance_walk_gives_the_same_image(ctx, name):
         sd = _coincident_instances()
     w, h = 40, 32
     kw = dict(accum_mode=C.ACCUM_FP64, bvh_kind=C.BVH_WIDE4)
-    ref = render(ctx, sd, w, h, 8, 10, trace_variant=0, **kw)
-    got = render(ctx, sd, w, h, 8, 10, trace_variant=5, **kw)
+    ref = render(ctx, sd, w, h, 8, 10, trace_variant=4, **kw)
+    got = render(ctx, sd, w, h, 8, 10, trace_variant=0, **kw)
     assert np.array_equal(got["sum"], ref["sum"], equal_nan=True)
     assert got["stats"][0].rays == ref["stats"][0].rays
