@@ -130,10 +130,18 @@ __device__ __forceinline__ void start_path(const WaveBuffers& w, int i, int q, i
   const int j = find_row(w.job_path_base, w.njobs, i);
   const JobDesc& J = w.jobs[j];
   const int npix = J.npix;
-  const int s = (i - J.path_base) / npix;
   const CameraView& cam = J.cam;
   // path i (in tile order) is this pixel's; its slot g keys the radiance
-  const int pixel = tiled_pixel(i - J.path_base - s * npix, cam.width, cam.height);
+  const int rel = i - J.path_base;
+  int s, pixel;
+  if (w.ray_order) {
+    const int ns = J.nsamples > 0 ? J.nsamples : 1;
+    s = rel % ns;
+    pixel = tiled_pixel(rel / ns, cam.width, cam.height);
+  } else {
+    s = rel / npix;
+    pixel = tiled_pixel(rel - s * npix, cam.width, cam.height);
+  }
   const int g = J.path_base + s * npix + pixel;
   const int sample = J.sample_base + s;
   RngStream rng;

@@ -85,6 +85,7 @@ struct WaveBuffers {
   // a queue is at the pass's bounce (the queues hold all the pass's paths at once).
   int* q_bounce[2];
   int njobs;
+  int ray_order;         // camera rays in the queue: 0 = per sample, pixels in 8x4 tiles; 1 = the pass's samples of a pixel together, pixels in tiles
   int cap;               // path slots of one pass (per-path radiance)
   int qcap;              // queue slots (rays in flight); equal to cap without regeneration
 };

@@ -412,13 +412,15 @@ __device__ __forceinline__ void traverse_bvh4_ww(const DevMesh& m, const TraceRa
 // ---- 8-wide quantised BVH ----
 __device__ __forceinline__ float exp2i(uint8_t biased) { return __int_as_float((int)biased << 23); }
 
-// Byte k (0-3, known at compile time in the unrolled loops) of `word` as a float, exact:
-// a byte permute builds 2^23 + q (the byte in the low mantissa bits under the exponent
-// of 2^23) and one subtraction removes 2^23. Integer-to-float conversions run at a
-// fraction of the rate of these two instructions.
+// Byte k (0-3) of `word` as a float, exact. PB: a byte permute builds 2^23 + q (the byte
+// in the low mantissa bits under the exponent of 2^23) and one subtraction removes 2^23;
+// otherwise a shift, a mask and an integer-to-float conversion.
+template <bool PB>
 __device__ __forceinline__ float byte_as_float(uint32_t word, int k) {
-  return __int_as_float((int)__byte_perm(word, 0x4B000000u, 0x7650u | (unsigned)k)) - 8388608.0f;
+  if (PB) return __int_as_float((int)__byte_perm(word, 0x4B000000u, 0x7650u | (unsigned)k)) - 8388608.0f;
+  return (float)((word >> (8 * k)) & 0xffu);
 }
+static constexpr bool kBytePermute = false;   // the conversion measured faster (see the design notes)
 
 template <bool COUNT>
 __device__ __forceinline__ void traverse_wide(const DevMesh& m, const TraceRay& r, int isect, MeshBest& best,
@@ -452,9 +454,9 @@ __device__ __forceinline__ void traverse_wide(const DevMesh& m, const TraceRay& 
       const bool inner = (imask >> s) & 1;
       if (!inner && me == 0) continue;
       const int kb = s & 3;
-      const float lx = byte_as_float(qlx[w], kb), hx = byte_as_float(qhx[w], kb);
-      const float ly = byte_as_float(qly[w], kb), hy = byte_as_float(qhy[w], kb);
-      const float lz = byte_as_float(qlz[w], kb), hz = byte_as_float(qhz[w], kb);
+      const float lx = byte_as_float<kBytePermute>(qlx[w], kb), hx = byte_as_float<kBytePermute>(qhx[w], kb);
+      const float ly = byte_as_float<kBytePermute>(qly[w], kb), hy = byte_as_float<kBytePermute>(qhy[w], kb);
+      const float lz = byte_as_float<kBytePermute>(qlz[w], kb), hz = byte_as_float<kBytePermute>(qhz[w], kb);
       const float nx = r.idir.x >= 0.0f ? lx : hx, fx = r.idir.x >= 0.0f ? hx : lx;
       const float ny = r.idir.y >= 0.0f ? ly : hy, fy = r.idir.y >= 0.0f ? hy : ly;
       const float nz = r.idir.z >= 0.0f ? lz : hz, fz = r.idir.z >= 0.0f ? hz : lz;
@@ -561,12 +563,12 @@ __device__ __forceinline__ void wide_node_step(const DevMesh& m, const TraceRay&
     const uint32_t me = (__float_as_uint(w ? q1.w : q1.z) >> sh) & 0xff;
     const bool inner = (imask >> s8) & 1;
     const int kb = s8 & 3;
-    const float lx = byte_as_float(__float_as_uint(w ? q2.y : q2.x), kb);
-    const float ly = byte_as_float(__float_as_uint(w ? q2.w : q2.z), kb);
-    const float lz = byte_as_float(__float_as_uint(w ? q3.y : q3.x), kb);
-    const float hx = byte_as_float(__float_as_uint(w ? q3.w : q3.z), kb);
-    const float hy = byte_as_float(__float_as_uint(w ? q4.y : q4.x), kb);
-    const float hz = byte_as_float(__float_as_uint(w ? q4.w : q4.z), kb);
+    const float lx = byte_as_float<kBytePermute>(__float_as_uint(w ? q2.y : q2.x), kb);
+    const float ly = byte_as_float<kBytePermute>(__float_as_uint(w ? q2.w : q2.z), kb);
+    const float lz = byte_as_float<kBytePermute>(__float_as_uint(w ? q3.y : q3.x), kb);
+    const float hx = byte_as_float<kBytePermute>(__float_as_uint(w ? q3.w : q3.z), kb);
+    const float hy = byte_as_float<kBytePermute>(__float_as_uint(w ? q4.y : q4.x), kb);
+    const float hz = byte_as_float<kBytePermute>(__float_as_uint(w ? q4.w : q4.z), kb);
     const float nx = r.idir.x >= 0.0f ? lx : hx, fx = r.idir.x >= 0.0f ? hx : lx;
     const float ny = r.idir.y >= 0.0f ? ly : hy, fy = r.idir.y >= 0.0f ? hy : ly;
     const float nz = r.idir.z >= 0.0f ? lz : hz, fz = r.idir.z >= 0.0f ? hz : lz;
