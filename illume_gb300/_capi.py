@@ -80,7 +80,7 @@ class RenderParams(ctypes.Structure):
         ("seed", c_uint32), ("job", c_uint32), ("accum_mode", c_int32), ("intersector", c_int32),
         ("bvh_kind", c_int32), ("exact_hg", c_int32), ("samples_per_pass", c_int32),
         ("camera", _pf), ("trace_variant", c_int32), ("shade_variant", c_int32), ("estimator", c_int32),
-        ("engines", c_int32), ("queue_slots", c_int32), ("regen_threshold", c_float),
+        ("engines", c_int32), ("queue_slots", c_int32), ("regen_threshold", c_float), ("ray_group", c_int32),
     ]
 
 

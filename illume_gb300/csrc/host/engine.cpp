@@ -131,10 +131,7 @@ void Engine::point() {
   w.job_path_base = path_base.as<int>();
   w.job_pixel_base = pixel_base.as<int>();
   w.njobs = rows;
-  {
-    const char* e = getenv("ILLUME_RAY_ORDER");
-    w.ray_order = e && atoi(e) == 1 ? 1 : 0;
-  }
+  w.ray_group = ray_group;
   w.cap = cap;
   w.qcap = qcap;
   for (int k = 0; k < 2; ++k) w.q_bounce[k] = regen ? q_bounce[k].as<int>() : nullptr;

@@ -25,6 +25,7 @@ struct Engine {
   // and new paths enter as earlier ones end (threshold: the next queue's fill, as a share
   // of qcap, at or below which new paths are started); otherwise qcap = cap.
   int queue_req = 0, qcap = 0;
+  int ray_group = kDefaultRayGroup;   // samples of a pixel together in the camera-ray queue
   float regen_threshold = 1.0f;
   bool regen = false;
   RenderKnobs knobs{};

@@ -44,6 +44,7 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if (p.engines < 0 || p.engines > 16) { *err = "engines out of range (0-16)"; return ILLUME_ERR_INVALID; }
   if (p.estimator < ILLUME_ESTIMATOR_REFERENCE || p.estimator > ILLUME_ESTIMATOR_NEE) { *err = "unknown estimator"; return ILLUME_ERR_INVALID; }
   if (p.queue_slots < 0) { *err = "negative queue slots"; return ILLUME_ERR_INVALID; }
+  if (p.ray_group < 0) { *err = "negative ray group"; return ILLUME_ERR_INVALID; }
   if (p.queue_slots > 0 && !(p.regen_threshold >= 0.0f && p.regen_threshold <= 1.0f)) {
     *err = "regeneration threshold outside [0, 1]";
     return ILLUME_ERR_INVALID;
@@ -131,6 +132,7 @@ int Renderer::init(std::string* err) {
   acc.comp32 = comp32.as<float>();
   acc.sum64 = sum64.as<double>();
   acc.sumsq = sumsq.as<double>();
+  eng.ray_group = p.ray_group > 0 ? p.ray_group : kDefaultRayGroup;
   if ((st = eng.init(ctx, 1, per_pass * npix, render_knobs(p), err, p.queue_slots, p.regen_threshold)) != ILLUME_OK)
     return st;
   JobDesc row = job_row(*scene, p, acc);
@@ -151,6 +153,7 @@ int Renderer::init(std::string* err) {
       more.emplace_back(new Engine);
       Engine& x = *more.back();
       x.stream = s;
+      x.ray_group = eng.ray_group;
       if ((st = x.init(ctx, 1, per_pass * npix, render_knobs(p), err, p.queue_slots, p.regen_threshold)) != ILLUME_OK)
         return st;
       x.mirror[0] = row;

@@ -132,16 +132,16 @@ __device__ __forceinline__ void start_path(const WaveBuffers& w, int i, int q, i
   const int npix = J.npix;
   const CameraView& cam = J.cam;
   // path i (in tile order) is this pixel's; its slot g keys the radiance
+  // the pass's samples come in groups of k; a group's paths are queued pixel by pixel
+  // (pixels in tile order) with the group's k samples of a pixel next to each other
   const int rel = i - J.path_base;
-  int s, pixel;
-  if (w.ray_order) {
-    const int ns = J.nsamples > 0 ? J.nsamples : 1;
-    s = rel % ns;
-    pixel = tiled_pixel(rel / ns, cam.width, cam.height);
-  } else {
-    s = rel / npix;
-    pixel = tiled_pixel(rel - s * npix, cam.width, cam.height);
-  }
+  const int ns = J.nsamples > 0 ? J.nsamples : 1;
+  const int k = w.ray_group > 1 ? (w.ray_group < ns ? w.ray_group : ns) : 1;
+  const int grp = rel / (k * npix);
+  const int kk = (grp + 1) * k <= ns ? k : ns - grp * k;   // the last group may be smaller
+  const int within = rel - grp * k * npix;
+  const int s = grp * k + within % kk;
+  const int pixel = tiled_pixel(within / kk, cam.width, cam.height);
   const int g = J.path_base + s * npix + pixel;
   const int sample = J.sample_base + s;
   RngStream rng;

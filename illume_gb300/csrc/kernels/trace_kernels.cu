@@ -472,8 +472,8 @@ const void* trace_kernel_ptr(int bvh_kind, int variant) {
     return (const void*)k_trace<BVH_WIDE4, false, 8, true, false, false, true, true, true>;
   }
   if (bvh_kind == BVH_WIDE8) {
-    if (variant == 2) return (const void*)k_trace<BVH_WIDE8, false, 8>;
-    return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false>;
+    if (variant == 2) return (const void*)k_trace<BVH_WIDE8, false>;
+    return variant == 1 ? (const void*)k_trace_sm<false, false> : (const void*)k_trace<BVH_WIDE8, false, 8>;
   }
   if (variant == 1) return (const void*)k_trace<BVH_BINARY, false>;
   if (variant == 2) return (const void*)k_trace<BVH_BINARY, false, 8>;
@@ -508,11 +508,11 @@ void launch_trace(const WaveBuffers& w, const RenderKnobs& k, int bounce, int gr
       if (count_visits) k_trace_sm<true, false><<<grid, 128, 0, st>>>(w, nullptr, k, bounce, nullptr, 0, nullptr);
       else k_trace_sm<false, false><<<grid, 128, 0, st>>>(w, nullptr, k, bounce, nullptr, 0, nullptr);
     } else if (k.trace_variant == 2) {
-      if (count_visits) k_trace<BVH_WIDE8, true, 8><<<grid, 128, 0, st>>>(w, k, bounce);
-      else k_trace<BVH_WIDE8, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
-    } else {
       if (count_visits) k_trace<BVH_WIDE8, true><<<grid, 128, 0, st>>>(w, k, bounce);
       else k_trace<BVH_WIDE8, false><<<grid, 128, 0, st>>>(w, k, bounce);
+    } else {
+      if (count_visits) k_trace<BVH_WIDE8, true, 8><<<grid, 128, 0, st>>>(w, k, bounce);
+      else k_trace<BVH_WIDE8, false, 8><<<grid, 128, 0, st>>>(w, k, bounce);
     }
     return;
   }

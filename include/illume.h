@@ -176,9 +176,9 @@ typedef struct {
                                * order (variant 0 takes the hardware's approximate
                                * reciprocal and, in scenes of 3 to 16 instances, visits
                                * the instances a ray enters nearest box entry first).
-                               * 8-wide (ILLUME_BVH_WIDE8): 2 = at most 64 registers
-                               * (others: the compiler's choice). The persistent 8-wide
-                               * layout ignores it. */
+                               * 8-wide (ILLUME_BVH_WIDE8): 2 = the compiler's register
+                               * choice (others: at most 64 registers). The persistent
+                               * 8-wide layout ignores it. */
   int32_t shade_variant;      /* 0 = the measured best register bound (default), 1 = the
                                * compiler's choice, 2 / 3 / 4 = at most 80 / 72 / 64 registers */
   int32_t estimator;          /* illume_estimator */
@@ -199,6 +199,12 @@ typedef struct {
    * iteration bound (never expected) makes the render return ILLUME_ERR_TIMEOUT. */
   int32_t queue_slots;
   float regen_threshold;
+  /* Order of a pass's camera rays in the queue (no counterpart in the reference): up to
+   * ray_group samples of a pixel next to each other, pixels in 8x4 tiles, so that a warp's
+   * rays start alike and stay alike for more bounces. 0 = the library's choice (16, the
+   * fastest measured), 1 = one sample of every pixel after another. The image does not
+   * depend on it. */
+  int32_t ray_group;
 } illume_render_params;
 
 typedef struct {

@@ -7,6 +7,10 @@ sample, bounce) and its job, and each pixel's samples are still summed in sample
 so the image must be bit-identical to the render without regeneration, for every queue
 size and threshold, accumulation mode, estimator, engine count and progressive call.
 
+Camera-ray order: a pass's samples of a pixel are queued next to each other in groups
+(`ray_group`); the order of the queue changes which rays share a warp, never a path's
+result.
+
 Sorted instance walk (the default 4-wide trace kernel; variant 4 walks in index order):
 the instances a ray enters are visited nearest box entry first; ties between instances
 still go to the lower index, so images must equal the index-order walk's, including
@@ -144,3 +148,18 @@ def test_sorted_instance_walk_gives_the_same_image(ctx, name):
     got = render(ctx, sd, w, h, 8, 10, trace_variant=0, **kw)
     assert np.array_equal(got["sum"], ref["sum"], equal_nan=True)
     assert got["stats"][0].rays == ref["stats"][0].rays
+
+
+@pytest.mark.parametrize("name", ["traversal", "materials"])
+def test_camera_ray_grouping_gives_the_same_image(ctx, name):
+    sd = scenes()[name]
+    w, h, spp, depth = 48, 40, 30, 12
+    # 30 samples in passes of 7: groups of 4 and 16 leave smaller last groups
+    ref = render(ctx, sd, w, h, spp, depth, accum_mode=C.ACCUM_FP64, samples_per_pass=7, ray_group=1)
+    for g in (4, 16, 32, 0):
+        got = render(ctx, sd, w, h, spp, depth, accum_mode=C.ACCUM_FP64, samples_per_pass=7, ray_group=g)
+        assert np.array_equal(got["sum"], ref["sum"], equal_nan=True), (name, g)
+        assert got["stats"][0].rays == ref["stats"][0].rays
+    got = render(ctx, sd, w, h, spp, depth, accum_mode=C.ACCUM_FP64, samples_per_pass=7, ray_group=16,
+                 queue_slots=900, regen_threshold=0.5)
+    assert np.array_equal(got["sum"], ref["sum"], equal_nan=True)
