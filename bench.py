@@ -69,6 +69,11 @@ def parse():
                     help="path regeneration: rays in flight per engine (0: every path of a pass starts at once)")
     ap.add_argument("--regen-threshold", type=float, default=1.0,
                     help="path regeneration: refill when the next queue holds at most this share of the slots")
+    ap.add_argument("--intersector", default="mt", choices=["mt", "watertight"],
+                    help="triangle test of the traversal and Cornell workloads, their CPU baseline, reference "
+                         "arm and oracle check: mt = the reference's Moller-Trumbore test "
+                         "(src/primitives/mesh.cu:445-476; the default, as the reference measures its rays), "
+                         "watertight = the library's default test")
     ap.add_argument("--engines", type=int, default=0,
                     help="engines taking turns on a step's passes (0: the library's choice)")
     ap.add_argument("--tris", type=int, default=100_000)
@@ -96,6 +101,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
+
+
+def isect_of(args):
+    from illume_gb300 import _capi as C
+    return C.ISECT_MT if args.intersector == "mt" else C.ISECT_WATERTIGHT
 
 
 def dist_env():
@@ -198,7 +208,7 @@ def cpu_baseline(sd, args, seconds):
     k = 0
     while True:
         sel = pixels[(k * chunk) % len(pixels):(k * chunk) % len(pixels) + chunk]
-        _, _, r = osc.render(W, H, 1, args.depth, pixels=sel, sample_begin=k, isect=1, precision=32)
+        _, _, r = osc.render(W, H, 1, args.depth, pixels=sel, sample_begin=k, isect=isect_of(args), precision=32)
         rays += r
         done += len(sel)
         k += 1
@@ -223,7 +233,7 @@ def run_reference(args):
     W = H = args.res
     pixels = np.arange(0, W * H, 97, dtype=np.int32)   # 10,810 paths per step
     def step(k):
-        return osc.render(W, H, 1, args.depth, pixels=pixels, sample_begin=k, isect=1, precision=32)[2]
+        return osc.render(W, H, 1, args.depth, pixels=pixels, sample_begin=k, isect=isect_of(args), precision=32)[2]
     for k in range(args.warmup):
         step(k)
     rays = 0
@@ -269,7 +279,7 @@ def run_ours(args):
     p.samples_per_pass = args.spp_per_step
     p.bvh_kind = {"binary": C.BVH_BINARY, "wide": C.BVH_WIDE8, "wide-persistent": C.BVH_WIDE8_PERSISTENT,
                   "wide4": C.BVH_WIDE4}[args.bvh]
-    p.intersector = C.ISECT_WATERTIGHT
+    p.intersector = isect_of(args)
     p.accum_mode = C.ACCUM_FP32
     p.sample_begin = rank * 1_000_000
     p.estimator = C.ESTIMATOR_NEE if args.estimator == "nee" else C.ESTIMATOR_REFERENCE
@@ -329,7 +339,7 @@ def run_ours(args):
         subset = np.arange(npix_q // 97, npix_q, npix_q // 48, dtype=np.int32)[:48]
         t0q = time.perf_counter()
         osum, _, _ = pyoracle.OracleScene(sd).render(args.res, args.res, acc_spp, args.depth, seed=p.seed, job=p.job,
-                                                      isect=C.ISECT_WATERTIGHT, precision=64, pixels=subset,
+                                                      isect=isect_of(args), precision=64, pixels=subset,
                                                       sample_begin=p.sample_begin)
         om = osum / acc_spp
         gm = g["sum"][subset] / acc_spp
@@ -408,7 +418,7 @@ def run_ours(args):
                        "turns" % (pass_spp, n_eng) if n_eng > 1 else "") + (
                            ", paths regenerated into %d queue slots per engine (threshold %.2f)" %
                            (args.queue_slots, args.regen_threshold) if args.queue_slots > 0 else ""),
-                       "bvh": args.bvh, "intersector": "watertight",
+                       "bvh": args.bvh, "intersector": args.intersector,
                        "estimator": args.estimator, "trace_variant": args.trace_variant,
                        "spp_per_step": args.spp_per_step, "paths_per_step": npix * args.spp_per_step,
                        "triangles": sd.num_triangles(), "resolution": [args.res, args.res], "max_depth": args.depth,
@@ -766,6 +776,7 @@ def run_cornell(args):
     p = scene.default_params(spp, depth)
     p.width, p.height, p.seed, p.job, p.accum_mode = W, H, 0, 0, C.ACCUM_FP32
     p.estimator = C.ESTIMATOR_NEE if args.estimator == "nee" else C.ESTIMATOR_REFERENCE
+    p.intersector = isect_of(args)
     r = Renderer(ctx, scene, params=p)
     for _ in range(args.warmup):
         r.render_device()
@@ -787,10 +798,10 @@ def run_cornell(args):
     value = rays / (dev_ms * 1e-3) / 1e6
     osc = pyoracle.OracleScene(sd)
     t0 = time.perf_counter()
-    o32, _, crays = osc.render(W, H, spp, depth, seed=0, job=0, isect=C.ISECT_WATERTIGHT, precision=32)
+    o32, _, crays = osc.render(W, H, spp, depth, seed=0, job=0, isect=isect_of(args), precision=32)
     cpu_s = time.perf_counter() - t0
     threads = os.cpu_count() or 1
-    osum, osq, _ = osc.render(W, H, spp, depth, seed=0, job=0, isect=C.ISECT_WATERTIGHT, precision=64)
+    osum, osq, _ = osc.render(W, H, spp, depth, seed=0, job=0, isect=isect_of(args), precision=64)
     om = osum / spp
     ovar = np.maximum(osq / spp - om * om, 0)
     rmse = float(np.sqrt(np.mean((gmean - om) ** 2)))
@@ -802,7 +813,7 @@ def run_cornell(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"Cornell box (5 wall quads, 130x105 light (17,12,4), mirror and glass spheres r=90), "
                                f"{W}x{H}, {spp} spp, depth {depth}, FP32 accumulation, seed 0",
-                   "estimator": args.estimator, "rays_per_render": rays // args.steps,
+                   "estimator": args.estimator, "intersector": args.intersector, "rays_per_render": rays // args.steps,
                    "l2": "scene and image fit in L2 (working set < 40 MB); not flushed"},
         # the reference estimator follows the oracle's Philox streams, so these differences
         # are arithmetic (FP32 paths that part from the FP64 ones); the next-event estimator
