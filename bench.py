@@ -74,6 +74,9 @@ def parse():
                          "arm and oracle check: mt = the reference's Moller-Trumbore test "
                          "(src/primitives/mesh.cu:445-476; the default, as the reference measures its rays), "
                          "watertight = the library's default test")
+    ap.add_argument("--bvh-builder", default="host", choices=["host", "device"],
+                    help="traversal workload: BVHs built by binned SAH on the host cores (default) or by "
+                         "locally-ordered clustering on the GPU")
     ap.add_argument("--engines", type=int, default=0,
                     help="engines taking turns on a step's passes (0: the library's choice)")
     ap.add_argument("--tris", type=int, default=100_000)
@@ -273,6 +276,7 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     sd = build_scene(args)
     ctx = Context(dev)
+    ctx.set_bvh_builder(C.BVH_BUILD_DEVICE if args.bvh_builder == "device" else C.BVH_BUILD_HOST)
     scene = HostScene.from_data(ctx, sd)
     p = scene.default_params(args.spp_per_step, args.depth)
     p.width = p.height = args.res
@@ -419,6 +423,7 @@ def run_ours(args):
                            ", paths regenerated into %d queue slots per engine (threshold %.2f)" %
                            (args.queue_slots, args.regen_threshold) if args.queue_slots > 0 else ""),
                        "bvh": args.bvh, "intersector": args.intersector,
+                       "bvh_builder": args.bvh_builder, "bvh_build_ms": round(scene.build_info()["build_ms"], 1),
                        "estimator": args.estimator, "trace_variant": args.trace_variant,
                        "spp_per_step": args.spp_per_step, "paths_per_step": npix * args.spp_per_step,
                        "triangles": sd.num_triangles(), "resolution": [args.res, args.res], "max_depth": args.depth,

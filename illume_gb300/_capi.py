@@ -34,6 +34,7 @@ DIST_BECKMANN, DIST_GGX = range(2)
 TONE_LINEAR, TONE_REINHARD, TONE_FILMIC, TONE_UNCHARTED = range(4)
 ISECT_MT, ISECT_WATERTIGHT = range(2)
 BVH_BINARY, BVH_WIDE8, BVH_WIDE8_PERSISTENT, BVH_WIDE4 = range(4)
+BVH_BUILD_HOST, BVH_BUILD_DEVICE = range(2)
 ACCUM_FP32, ACCUM_KAHAN, ACCUM_FP64 = range(3)
 ESTIMATOR_REFERENCE, ESTIMATOR_NEE = range(2)
 (SERVER_PATH_CAPACITY, SERVER_PASSES_PER_STEP, SERVER_AUTOTUNE, SERVER_TRACE_VARIANT, SERVER_LANES,
@@ -130,6 +131,8 @@ PROTOTYPES = {
     "illume_context_create": (c_int, [c_int, c_size_t, POINTER(c_void_p)]),
     "illume_context_destroy": (c_int, [c_void_p]),
     "illume_context_stream": (c_void_p, [c_void_p]),
+    "illume_context_set_bvh_builder": (c_int, [c_void_p, c_int]),
+    "illume_scene_build_info": (c_int, [c_void_p, POINTER(c_int), POINTER(c_double)]),
     "illume_scene_load_json": (c_int, [c_void_p, c_char_p, c_char_p, POINTER(c_void_p)]),
     "illume_scene_load_json_string": (c_int, [c_void_p, c_char_p, c_char_p, POINTER(c_void_p)]),
     "illume_scene_create": (c_int, [c_void_p, POINTER(SceneDesc), POINTER(c_void_p)]),

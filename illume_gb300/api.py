@@ -54,6 +54,12 @@ class Context:
     def stream(self) -> int:
         return C.lib().illume_context_stream(self.handle) or 0
 
+    def set_bvh_builder(self, builder: int) -> None:
+        """C.BVH_BUILD_HOST (binned SAH on the host cores, the default) or
+        C.BVH_BUILD_DEVICE (locally-ordered clustering on this context's GPU) for the
+        scenes made on this context from now on."""
+        C.check(C.lib().illume_context_set_bvh_builder(self.handle, builder))
+
 
 class HostScene:
     """A scene resident on the device (geometry, BVHs, materials, textures)."""
@@ -89,6 +95,18 @@ class HostScene:
         d = C.SceneDesc()
         C.check(C.lib().illume_scene_describe(self.handle, ctypes.byref(d)))
         return SceneData.from_desc(d)
+
+    def build_info(self) -> dict:
+        """Meshes whose BVHs came from the device build, and the BVH build's wall time."""
+        d, ms = ctypes.c_int(), ctypes.c_double()
+        C.check(C.lib().illume_scene_build_info(self.handle, ctypes.byref(d), ctypes.byref(ms)))
+        return {"device_meshes": d.value, "build_ms": ms.value}
+
+    def check_bvh(self) -> str:
+        """Checks every mesh's BVH invariants (raises on a violation); returns the report."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        C.check(C.lib().illume_scene_check_bvh(self.handle, buf, len(buf)))
+        return buf.value.decode()
 
     def device_bytes(self) -> int:
         n = ctypes.c_size_t()

@@ -1,4 +1,6 @@
 #include "bvh_build.h"
+#include "../kernels/bvh_device.h"
+#include "runtime.h"
 
 #include <math.h>
 #include <string.h>
@@ -219,8 +221,82 @@ int tree_depth(const std::vector<BNode>& n, int i) {
 
 }  // namespace
 
-void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, MeshBvh* out) {
-  (void)num_vertices;
+namespace {
+
+// The host tree of a device cluster tree: leaves of up to max_leaf primitives where the
+// surface-area cost says a leaf is cheaper than the subtree below it (cost of a leaf =
+// its primitives, of an inner node = 1 + the children's costs weighted by their share of
+// its box area, the same units as build_step), nodes and `order` in depth-first order
+// (root at 0, left subtree first). Cluster nodes are numbered after their children, so
+// one ascending sweep is bottom-up.
+std::vector<BNode> tree_from_clusters(const ClusterTree& ct, int max_leaf, std::vector<int>& order) {
+  const int n = ct.n, total = 2 * n - 1;
+  std::vector<int> cnt(total);
+  std::vector<char> leaf(total);
+  std::vector<double> cost(total), area(total);
+  auto box_of = [&](int id) {
+    Box b;
+    for (int a = 0; a < 3; ++a) {
+      b.lo[a] = ct.box[6 * (size_t)id + a];
+      b.hi[a] = ct.box[6 * (size_t)id + 3 + a];
+    }
+    return b;
+  };
+  for (int id = 0; id < total; ++id) {
+    area[id] = box_of(id).area();
+    if (id < n) {
+      cnt[id] = 1;
+      cost[id] = 1.0;
+      leaf[id] = 1;
+      continue;
+    }
+    const int l = ct.child[2 * (size_t)(id - n)], r = ct.child[2 * (size_t)(id - n) + 1];
+    cnt[id] = cnt[l] + cnt[r];
+    const double split = 1.0 + (area[l] * cost[l] + area[r] * cost[r]) / std::max(area[id], 1e-300);
+    leaf[id] = cnt[id] <= max_leaf && (double)cnt[id] <= split;
+    cost[id] = leaf[id] ? (double)cnt[id] : split;
+  }
+  std::vector<BNode> nodes;
+  nodes.reserve(2 * (size_t)n);
+  order.clear();
+  order.reserve(n);
+  nodes.emplace_back();
+  std::vector<std::pair<int, int>> st{{ct.root, 0}};
+  std::vector<int> sub;
+  while (!st.empty()) {
+    const int id = st.back().first, bi = st.back().second;
+    st.pop_back();
+    nodes[bi].box = box_of(id);
+    if (leaf[id]) {
+      nodes[bi].first = (int)order.size();
+      nodes[bi].count = cnt[id];
+      sub.assign(1, id);
+      while (!sub.empty()) {   // the leaf's primitives, left to right
+        const int k = sub.back();
+        sub.pop_back();
+        if (k < n) {
+          order.push_back(ct.prim[k]);
+        } else {
+          sub.push_back(ct.child[2 * (size_t)(k - n) + 1]);
+          sub.push_back(ct.child[2 * (size_t)(k - n)]);
+        }
+      }
+    } else {
+      const int l = (int)nodes.size();
+      nodes.emplace_back();
+      nodes.emplace_back();
+      nodes[bi].left = l;
+      nodes[bi].right = l + 1;
+      st.push_back({ct.child[2 * (size_t)(id - n) + 1], l + 1});
+      st.push_back({ct.child[2 * (size_t)(id - n)], l});
+    }
+  }
+  return nodes;
+}
+
+}  // namespace
+
+void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, MeshBvh* out, Context* device) {
   // padded triangle boxes
   double mlo[3] = {INFINITY, INFINITY, INFINITY}, mhi[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (int i = 0; i < T; ++i)
@@ -255,11 +331,28 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
     out->lo[a] = T ? down(mlo[a] - pad) : 0.0f;
     out->hi[a] = T ? up(mhi[a] + pad) : 0.0f;
   }
+  ClusterTree ct;
+  bool use_ct = false;
+  std::string fallback;
+  if (device && T > 0) {
+    std::vector<float> b6(6 * (size_t)T);
+    for (int i = 0; i < T; ++i)
+      for (int a = 0; a < 3; ++a) {
+        b6[6 * (size_t)i + a] = (float)boxes[i].lo[a];        // exact: the padded boxes are floats
+        b6[6 * (size_t)i + 3 + a] = (float)boxes[i].hi[a];
+      }
+    std::string err;
+    if (build_cluster_tree_device(device, b6.data(), T, &ct, &err) == ILLUME_OK) use_ct = true;
+    else fallback = err.empty() ? std::string(last_error()) : err;
+  }
+  auto binary = [&](int max_leaf, std::vector<int>& order) {
+    return use_ct ? tree_from_clusters(ct, max_leaf, order) : build_binary(boxes, order, max_leaf);
+  };
 
   // ---------------- binary layout ----------------
   auto build_binary_layout = [&]() {
     std::vector<int> order;
-    std::vector<BNode> bn = T ? build_binary(boxes, order, 4) : std::vector<BNode>();
+    std::vector<BNode> bn = T ? binary(4, order) : std::vector<BNode>();
     out->bvh2.clear();
     out->bvh2_tris.clear();
     out->bvh2_tris.reserve((size_t)T * 3);
@@ -401,7 +494,7 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
   // ---------------- 8-wide quantised layout ----------------
   auto build_wide_layout = [&]() {
     std::vector<int> order;
-    std::vector<BNode> bn = T ? build_binary(boxes, order, 3) : std::vector<BNode>();
+    std::vector<BNode> bn = T ? binary(3, order) : std::vector<BNode>();
     out->wide.clear();
     out->wide_tris.clear();
     out->wide_tris.reserve((size_t)T * 3);
@@ -527,6 +620,22 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
   std::thread wide_thread(build_wide_layout);
   build_binary_layout();
   wide_thread.join();
+  if (use_ct) {
+    if (out->stats.bvh2_depth > 60 || 3 * out->stats.bvh4_depth > 60) {
+      // deeper than the traversal stacks take (scene upload rejects it): the host's tree
+      const std::string why = "device tree too deep (binary depth " + std::to_string(out->stats.bvh2_depth) +
+                              ", 4-wide depth " + std::to_string(out->stats.bvh4_depth) + ")";
+      *out = MeshBvh{};
+      build_mesh_bvh(P, num_vertices, tris, T, out, nullptr);
+      out->stats.device_fallback = why;
+      return;
+    }
+    out->stats.device_built = 1;
+    out->stats.device_rounds = ct.iterations;
+    out->stats.device_ms = ct.device_ms;
+  } else if (device && T > 0) {
+    out->stats.device_fallback = fallback;
+  }
 }
 
 }  // namespace illume

@@ -26,6 +26,10 @@ struct BuildStats {
   int wide_nodes = 0, wide_leaves = 0, wide_depth = 0;
   int bvh4_nodes = 0, bvh4_depth = 0;
   double sah_cost = 0.0;
+  int device_built = 0;          // 1: the binary tree came from the device build
+  int device_rounds = 0;         // its clustering rounds
+  double device_ms = 0.0;        // and the wall time of its device part
+  std::string device_fallback;   // why a requested device build fell back to the host build
 };
 
 struct MeshBvh {
@@ -43,8 +47,14 @@ struct MeshBvh {
 // most 16). The result does not depend on it.
 int build_threads();
 
-// positions: 3 floats per vertex; tris: 3 ints per triangle.
-void build_mesh_bvh(const float* positions, int num_vertices, const int* tris, int num_tris, MeshBvh* out);
+struct Context;
+
+// positions: 3 floats per vertex; tris: 3 ints per triangle. With `device`, the binary
+// tree is built on that context's GPU by locally-ordered clustering (bvh_device.h) and
+// turned into leaves here; a device build that fails, or whose tree is deeper than the
+// traversal stacks allow, is replaced by the host build (stats.device_fallback says why).
+void build_mesh_bvh(const float* positions, int num_vertices, const int* tris, int num_tris, MeshBvh* out,
+                    Context* device = nullptr);
 
 // Invariants of both layouts: every triangle referenced exactly once, every triangle
 // inside its leaf box, every inner child box inside its parent's box, quantised boxes

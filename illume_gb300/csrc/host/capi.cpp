@@ -57,6 +57,13 @@ int illume_context_destroy(illume_context* ctx) {
 
 void* illume_context_stream(illume_context* ctx) { return ctx ? (void*)ctx->c.stream : nullptr; }
 
+int illume_context_set_bvh_builder(illume_context* ctx, int builder) {
+  CHECK_ARG(ctx, "null context");
+  CHECK_ARG(builder == ILLUME_BVH_BUILD_HOST || builder == ILLUME_BVH_BUILD_DEVICE, "unknown BVH builder");
+  ctx->c.bvh_builder = builder;
+  return ILLUME_OK;
+}
+
 static int finish_scene(illume_context* ctx, std::unique_ptr<illume_scene>& sc, illume_scene** out) {
   std::string err;
   if (!ctx) {
@@ -146,6 +153,15 @@ int illume_bvh_cache_clear(void) {
   return ILLUME_OK;
 }
 
+int illume_scene_build_info(const illume_scene* scene, int* device_meshes, double* build_ms) {
+  CHECK_ARG(scene, "null scene");
+  int d = 0;
+  for (const MeshBvh& b : scene->s.bvhs) d += b.stats.device_built;
+  if (device_meshes) *device_meshes = d;
+  if (build_ms) *build_ms = scene->s.build_ms;
+  return ILLUME_OK;
+}
+
 int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t report_len) {
   CHECK_ARG(scene, "null scene");
   const SceneHost& h = scene->s.host;
@@ -161,10 +177,18 @@ int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t repor
     }
     char line[256];
     snprintf(line, sizeof(line),
-             "mesh %d: %d tris, binary %d nodes depth %d, 4-wide %d nodes depth %d, wide %d nodes %d leaves depth %d\n",
+             "mesh %d: %d tris, binary %d nodes depth %d, 4-wide %d nodes depth %d, wide %d nodes %d leaves depth %d, %s",
              i, h.mesh_num_tris[i], b.stats.bvh2_nodes, b.stats.bvh2_depth, b.stats.bvh4_nodes, b.stats.bvh4_depth,
-             b.stats.wide_nodes, b.stats.wide_leaves, b.stats.wide_depth);
+             b.stats.wide_nodes, b.stats.wide_leaves, b.stats.wide_depth,
+             b.stats.device_built ? "device build" : "host build");
     rep += line;
+    if (b.stats.device_built) {
+      char d[96];
+      snprintf(d, sizeof(d), " (%d clustering rounds, %.1f ms on the device)", b.stats.device_rounds, b.stats.device_ms);
+      rep += d;
+    }
+    if (!b.stats.device_fallback.empty()) rep += " (device build replaced: " + b.stats.device_fallback + ")";
+    rep += "\n";
   }
   if (report && report_len) {
     strncpy(report, rep.c_str(), report_len - 1);

@@ -280,11 +280,13 @@ namespace {
 struct BvhKey {
   uint64_t h1, h2;
   int nv, nt;
+  int builder;   // illume_bvh_builder: the device and host builds make different trees
   bool operator<(const BvhKey& o) const {
     if (h1 != o.h1) return h1 < o.h1;
     if (h2 != o.h2) return h2 < o.h2;
     if (nv != o.nv) return nv < o.nv;
-    return nt < o.nt;
+    if (nt != o.nt) return nt < o.nt;
+    return builder < o.builder;
   }
 };
 
@@ -299,7 +301,7 @@ BvhKey mesh_key(const float* P, int nv, const int* T, int nt) {
   const uint32_t* pw = reinterpret_cast<const uint32_t*>(P);
   for (size_t i = 0; i < 3 * (size_t)nv; ++i) mix(pw[i]);
   for (size_t i = 0; i < 3 * (size_t)nt; ++i) mix((uint32_t)T[i]);
-  return BvhKey{h1, h2, nv, nt};
+  return BvhKey{h1, h2, nv, nt, 0};
 }
 
 std::mutex g_bvh_mu;
@@ -313,8 +315,9 @@ size_t bvh_bytes(const MeshBvh& b) {
          b.wide_tris.size() * sizeof(float4);
 }
 
-void build_cached(const float* P, int nv, const int* T, int nt, MeshBvh* out) {
-  const BvhKey key = mesh_key(P, nv, T, nt);
+void build_cached(const float* P, int nv, const int* T, int nt, MeshBvh* out, Context* device) {
+  BvhKey key = mesh_key(P, nv, T, nt);
+  key.builder = device ? ILLUME_BVH_BUILD_DEVICE : ILLUME_BVH_BUILD_HOST;
   {
     std::lock_guard<std::mutex> lk(g_bvh_mu);
     auto it = g_bvh_cache.find(key);
@@ -325,7 +328,9 @@ void build_cached(const float* P, int nv, const int* T, int nt, MeshBvh* out) {
     }
     ++g_bvh_misses;
   }
-  build_mesh_bvh(P, nv, T, nt, out);
+  build_mesh_bvh(P, nv, T, nt, out, device);
+  // a device build that fell back to the host tree is not kept under the device key
+  if (device && !out->stats.device_built) return;
   const size_t bytes = bvh_bytes(*out);
   std::lock_guard<std::mutex> lk(g_bvh_mu);
   if (bytes > kBvhCacheMaxBytes) return;
@@ -363,6 +368,7 @@ int Scene::build_host(std::string* err) {
       return ILLUME_ERR_UNSUPPORTED;
     }
   bvhs.assign(nm, MeshBvh{});
+  Context* device = ctx && ctx->bvh_builder == ILLUME_BVH_BUILD_DEVICE ? ctx : nullptr;
   const int nthreads = std::max(1, std::min<int>(nm, build_threads()));
   std::vector<std::thread> pool;
   std::atomic<int> next{0};
@@ -370,7 +376,7 @@ int Scene::build_host(std::string* err) {
     for (int i = next++; i < nm; i = next++) {
       const float* P = h.positions.data() + 3 * (size_t)h.mesh_vertex_offset[i];
       const int* T = h.tris.data() + 3 * (size_t)h.mesh_tri_offset[i];
-      build_cached(P, h.mesh_num_vertices[i], T, h.mesh_num_tris[i], &bvhs[i]);
+      build_cached(P, h.mesh_num_vertices[i], T, h.mesh_num_tris[i], &bvhs[i], device);
     }
   };
   for (int t = 1; t < nthreads; ++t) pool.emplace_back(work);

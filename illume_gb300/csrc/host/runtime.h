@@ -36,6 +36,7 @@ struct Context {
   std::atomic<size_t> used{0};
   int sm_count = 0;
   int l2_bytes = 0;
+  int bvh_builder = 0;               // illume_bvh_builder of the scenes made on this context
   std::atomic<long long> launches{0};
   // illume_render_noalloc's set-up on this context: the device address of its fixed
   // scratch array, the driver context it was looked up in, and grid sizes per kernel

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define ILLUME_ABI_VERSION 3
+#define ILLUME_ABI_VERSION 4
 
 enum illume_status {
   ILLUME_OK = 0,
@@ -233,6 +233,16 @@ int illume_abi_version(void);
 /* ---- context ---- */
 int illume_context_create(int device, size_t hbm_budget_bytes, illume_context** out);
 int illume_context_destroy(illume_context* ctx);
+/* Where the BVHs of the scenes later made on this context are built (no counterpart in
+ * the reference, whose tree is built on one host thread, src/accel/bvh.cpp:65-439):
+ * HOST (the default) = binned SAH on the host cores; DEVICE = locally-ordered clustering
+ * on the context's GPU (Morton order, then merges of mutual nearest neighbours within 16
+ * positions), the leaves and node layouts made on the host from its tree. The two give
+ * different trees and the same closest hits. A device build that fails or whose tree is
+ * too deep for the traversal stacks is replaced by the host build
+ * (illume_scene_build_info). Host-only scenes (no context) are always built on the host. */
+enum illume_bvh_builder { ILLUME_BVH_BUILD_HOST = 0, ILLUME_BVH_BUILD_DEVICE = 1 };
+int illume_context_set_bvh_builder(illume_context* ctx, int builder);
 /* the context's CUDA stream (a cudaStream_t) */
 void* illume_context_stream(illume_context* ctx);
 
@@ -260,6 +270,9 @@ int illume_scene_upload(illume_scene* scene, size_t* bytes);
  * boxes inside their parent's, quantised boxes containing the exact boxes) and writes a
  * one-line summary per mesh (node counts, depths) into report. */
 int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t report_len);
+/* Meshes of the scene whose BVHs came from the device build, and the wall time of the
+ * scene's BVH construction (all meshes, cache hits included) in milliseconds. */
+int illume_scene_build_info(const illume_scene* scene, int* device_meshes, double* build_ms);
 /* Test hook: 64-bit FNV-1a digests of mesh `mesh`'s built layouts, in the order binary
  * nodes, 4-wide nodes, triangle records of both, 8-wide nodes with their triangle
  * records. Equal digests = bit-identical trees (the build's thread count, set by the

@@ -27,7 +27,7 @@ def test_every_declared_symbol_is_exported(native_lib):
 
 
 def test_abi_version(native_lib):
-    assert native_lib.illume_abi_version() == 3
+    assert native_lib.illume_abi_version() == 4
 
 
 def load_host(path, base=SCENES):
