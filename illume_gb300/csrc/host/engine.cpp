@@ -398,7 +398,7 @@ int Engine::run_profiled(int depth, bool count_visits, std::vector<cudaEvent_t>&
     launch_raygen(w, grid_raygen, st);
   }
   ILLUME_CUDA_TRY(event());
-  nl += 2;
+  nl += regen ? 3 : 2;   // plan, then the first batch's slots and camera rays, or every camera ray
   for (int b = 0;; ++b) {
     if (!regen && b >= depth) break;
     launch_trace(w, knobs, regen ? -1 : b, grid_trace, st, count_visits);
