@@ -296,7 +296,9 @@ std::vector<BNode> tree_from_clusters(const ClusterTree& ct, int max_leaf, std::
 
 }  // namespace
 
-void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, MeshBvh* out, Context* device) {
+void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, MeshBvh* out, Context* device,
+                    int layouts) {
+  if (!(layouts & kLayoutBinary4)) device = nullptr;   // the device tree serves the binary and 4-wide layouts
   // padded triangle boxes
   double mlo[3] = {INFINITY, INFINITY, INFINITY}, mhi[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (int i = 0; i < T; ++i)
@@ -616,17 +618,26 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
       out->stats.wide_depth = max_depth;
     }
   };
-  // the two layouts are independent: build them concurrently
-  std::thread wide_thread(build_wide_layout);
-  build_binary_layout();
-  wide_thread.join();
+  // the two trees are independent: build them concurrently when both are asked for
+  if (layouts & kLayoutWide) {
+    if (layouts & kLayoutBinary4) {
+      std::thread wide_thread(build_wide_layout);
+      build_binary_layout();
+      wide_thread.join();
+    } else {
+      build_wide_layout();
+    }
+    out->has_wide = true;
+  } else {
+    build_binary_layout();
+  }
   if (use_ct) {
     if (out->stats.bvh2_depth > 60 || 3 * out->stats.bvh4_depth > 60) {
       // deeper than the traversal stacks take (scene upload rejects it): the host's tree
       const std::string why = "device tree too deep (binary depth " + std::to_string(out->stats.bvh2_depth) +
                               ", 4-wide depth " + std::to_string(out->stats.bvh4_depth) + ")";
       *out = MeshBvh{};
-      build_mesh_bvh(P, num_vertices, tris, T, out, nullptr);
+      build_mesh_bvh(P, num_vertices, tris, T, out, nullptr, layouts);
       out->stats.device_fallback = why;
       return;
     }
@@ -745,7 +756,7 @@ bool check_mesh_bvh(const float* P, const int* tris, int T, const MeshBvh& b, st
       if (seen[p] != 1) { *msg = "4-wide: triangle " + std::to_string(p) + " not referenced exactly once"; return false; }
   }
   // ---- wide ----
-  {
+  if (b.has_wide) {
     std::vector<int> seen(T, 0);
     std::vector<std::pair<uint32_t, DBox>> st;
     DBox all{{-INFINITY, -INFINITY, -INFINITY}, {INFINITY, INFINITY, INFINITY}};

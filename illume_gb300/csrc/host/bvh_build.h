@@ -39,9 +39,14 @@ struct MeshBvh {
   std::vector<WideNode> wide;
   std::vector<float4> wide_tris;
   bool root_leaf = false;
+  bool has_wide = false;           // the 8-wide layout is built (on first need, Scene::ensure_wide)
   float lo[3], hi[3];              // padded object-space bounds of the mesh
   BuildStats stats;
 };
+
+// Layouts of build_mesh_bvh: the binary and 4-wide layouts (one tree, shared triangle
+// records), the 8-wide quantised layout (its own tree, leaves of up to 3 triangles).
+enum BuildLayouts { kLayoutBinary4 = 1, kLayoutWide = 2, kLayoutAll = 3 };
 
 // Host threads of a BVH build: ILLUME_BUILD_THREADS if set (>= 1), else the cores (at
 // most 16). The result does not depend on it.
@@ -53,12 +58,15 @@ struct Context;
 // tree is built on that context's GPU by locally-ordered clustering (bvh_device.h) and
 // turned into leaves here; a device build that fails, or whose tree is deeper than the
 // traversal stacks allow, is replaced by the host build (stats.device_fallback says why).
+// `layouts` (BuildLayouts) selects what is built; a call for kLayoutWide alone fills only
+// the 8-wide arrays and statistics of `out` (host build).
 void build_mesh_bvh(const float* positions, int num_vertices, const int* tris, int num_tris, MeshBvh* out,
-                    Context* device = nullptr);
+                    Context* device = nullptr, int layouts = kLayoutAll);
 
-// Invariants of both layouts: every triangle referenced exactly once, every triangle
-// inside its leaf box, every inner child box inside its parent's box, quantised boxes
-// (decoded exactly) containing their contents. Returns false with a message on failure.
+// Invariants of the built layouts (the 8-wide one when has_wide): every triangle
+// referenced exactly once, every triangle inside its leaf box, every inner child box
+// inside its parent's box, quantised boxes (decoded exactly) containing their contents.
+// Returns false with a message on failure.
 bool check_mesh_bvh(const float* positions, const int* tris, int num_tris, const MeshBvh& b, std::string* msg);
 
 }  // namespace illume

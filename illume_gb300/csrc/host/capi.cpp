@@ -164,6 +164,11 @@ int illume_scene_build_info(const illume_scene* scene, int* device_meshes, doubl
 
 int illume_scene_check_bvh(const illume_scene* scene, char* report, size_t report_len) {
   CHECK_ARG(scene, "null scene");
+  {   // every layout is checked, so the 8-wide one is built if it is not yet
+    std::string err;
+    const int st = const_cast<illume_scene*>(scene)->s.ensure_wide(&err);
+    if (st != ILLUME_OK) { set_error(err.empty() ? std::string(last_error()) : err); return st; }
+  }
   const SceneHost& h = scene->s.host;
   std::string rep;
   for (int i = 0; i < h.num_meshes(); ++i) {
@@ -206,6 +211,11 @@ static uint64_t fnv1a(uint64_t h, const void* data, size_t bytes) {
 int illume_scene_bvh_digest(const illume_scene* scene, int mesh, uint64_t out[4]) {
   CHECK_ARG(scene && out, "null argument");
   CHECK_ARG(mesh >= 0 && mesh < (int)scene->s.bvhs.size(), "mesh index out of range");
+  {   // the digest covers every layout, so the 8-wide one is built if it is not yet
+    std::string err;
+    const int st = const_cast<illume_scene*>(scene)->s.ensure_wide(&err);
+    if (st != ILLUME_OK) { set_error(err.empty() ? std::string(last_error()) : err); return st; }
+  }
   const MeshBvh& b = scene->s.bvhs[mesh];
   const uint64_t h0 = 0xcbf29ce484222325ULL;
   out[0] = fnv1a(h0, b.bvh2.data(), b.bvh2.size() * sizeof(Bvh2Node));
@@ -385,6 +395,11 @@ int illume_trace_closest_device(illume_context* ctx, illume_scene* scene, const 
   CHECK_ARG(((uintptr_t)d_rays & 15) == 0, "rays must be 16-byte aligned");
   CHECK_ARG(scene->s.ctx == &ctx->c, "scene was not uploaded with this context");
   cudaSetDevice(ctx->c.device);
+  if (bvh_kind == ILLUME_BVH_WIDE8 || bvh_kind == ILLUME_BVH_WIDE8_PERSISTENT) {
+    std::string err;
+    const int st = scene->s.ensure_wide(&err);
+    if (st != ILLUME_OK) { set_error(err.empty() ? std::string(last_error()) : err); return st; }
+  }
   launch_trace_hook(scene->s.view, scene->s.view_dev, d_rays, n, intersector, bvh_kind, d_hits, ctx->c.stream);
   ILLUME_CUDA_TRY(cudaGetLastError());
   ctx->c.launches += n > 0 ? 1 : 0;

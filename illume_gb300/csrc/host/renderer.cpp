@@ -31,7 +31,7 @@ CameraView make_camera(const SceneHost& h, int W, int H) {
   return camera_view(h.camera_transform, h.camera_fov, h.camera_dof, h.camera_aperture, W, H);
 }
 
-int check_render_params(const illume_render_params& p, const Scene& scene, std::string* err) {
+int check_render_params(const illume_render_params& p, Scene& scene, std::string* err) {
   if (p.width <= 0 || p.height <= 0 || p.spp < 0 || p.max_depth < 0) { *err = "invalid render size, spp or depth"; return ILLUME_ERR_INVALID; }
   if ((long long)p.width * p.height > (1LL << 28)) { *err = "image too large"; return ILLUME_ERR_INVALID; }
   if (p.intersector != ISECT_MT && p.intersector != ISECT_WATERTIGHT) { *err = "unknown intersector"; return ILLUME_ERR_INVALID; }
@@ -52,10 +52,13 @@ int check_render_params(const illume_render_params& p, const Scene& scene, std::
   if ((int)scene.t_mediums.size() > kMaxMediums) { *err = "too many mediums"; return ILLUME_ERR_UNSUPPORTED; }
   // the 8-wide kernels push up to two stack entries per level (a triangle group and a
   // node group); upload bounds the binary and 4-wide trees the same way
-  if (p.bvh_kind == ILLUME_BVH_WIDE8 || p.bvh_kind == ILLUME_BVH_WIDE8_PERSISTENT)
+  if (!scene.ctx || !scene.view_dev) { *err = "scene has not been uploaded to a device"; return ILLUME_ERR_INVALID; }
+  if (p.bvh_kind == ILLUME_BVH_WIDE8 || p.bvh_kind == ILLUME_BVH_WIDE8_PERSISTENT) {
+    const int st = scene.ensure_wide(err);   // built and uploaded on first use
+    if (st != ILLUME_OK) return st;
     for (const MeshBvh& b : scene.bvhs)
       if (2 * b.stats.wide_depth > 60) { *err = "8-wide BVH deeper than the traversal stack"; return ILLUME_ERR_UNSUPPORTED; }
-  if (!scene.ctx || !scene.view_dev) { *err = "scene has not been uploaded to a device"; return ILLUME_ERR_INVALID; }
+  }
   return ILLUME_OK;
 }
 

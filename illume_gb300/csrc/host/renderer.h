@@ -60,7 +60,9 @@ struct Renderer {
 CameraView make_camera(const SceneHost& h, int width, int height);
 
 // Checks the parts of a render's parameters that every path of this library needs.
-int check_render_params(const illume_render_params& p, const Scene& scene, std::string* err);
+// Checks the parameters against the scene; an 8-wide BVH kind builds and uploads the
+// scene's 8-wide layout first (Scene::ensure_wide).
+int check_render_params(const illume_render_params& p, Scene& scene, std::string* err);
 
 // Job row of a render: scene, camera, Philox key and depth of `p`, no sample range yet.
 JobDesc job_row(const Scene& scene, const illume_render_params& p, const Accumulators& acc);

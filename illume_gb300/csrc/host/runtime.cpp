@@ -328,7 +328,7 @@ void build_cached(const float* P, int nv, const int* T, int nt, MeshBvh* out, Co
     }
     ++g_bvh_misses;
   }
-  build_mesh_bvh(P, nv, T, nt, out, device);
+  build_mesh_bvh(P, nv, T, nt, out, device, kLayoutBinary4);   // the 8-wide layout on first need
   // a device build that fell back to the host tree is not kept under the device key
   if (device && !out->stats.device_built) return;
   const size_t bytes = bvh_bytes(*out);
@@ -581,6 +581,64 @@ int Scene::build_and_upload(std::string* err) {
   ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   upload_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
   pin_upload_sources();
+  return ILLUME_OK;
+}
+
+int Scene::ensure_wide(std::string* err) {
+  std::lock_guard<std::mutex> lk(wide_mu);
+  const SceneHost& h = host;
+  const int nm = h.num_meshes();
+  std::vector<int> todo;
+  for (int i = 0; i < nm && i < (int)bvhs.size(); ++i)
+    if (!bvhs[i].has_wide) todo.push_back(i);
+  if (todo.empty()) return ILLUME_OK;
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int k = next++; k < (int)todo.size(); k = next++) {
+      const int i = todo[k];
+      const float* P = h.positions.data() + 3 * (size_t)h.mesh_vertex_offset[i];
+      const int* T = h.tris.data() + 3 * (size_t)h.mesh_tri_offset[i];
+      build_mesh_bvh(P, h.mesh_num_vertices[i], T, h.mesh_num_tris[i], &bvhs[i], nullptr, kLayoutWide);
+    }
+  };
+  const int nthreads = std::max(1, std::min<int>((int)todo.size(), build_threads()));
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nthreads; ++t) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  trace_bytes[1] = 0;
+  for (const MeshBvh& b : bvhs) trace_bytes[1] += b.wide.size() * sizeof(WideNode) + b.wide_tris.size() * sizeof(float4);
+  if (!ctx) return ILLUME_OK;
+  ILLUME_CUDA_TRY(cudaSetDevice(ctx->device));
+  // resident uploads: a per-render re-upload (upload_again) leaves them alone
+  auto up = [&](const void* src, size_t bytes, void** out) -> int {
+    buffers.emplace_back(new DevBuffer);
+    const int st = buffers.back()->upload(ctx, src, bytes);
+    if (st != ILLUME_OK) return st;
+    *out = buffers.back()->get();
+    uploads.push_back({*out, src, bytes, true});
+    device_bytes += buffers.back()->size();
+    return ILLUME_OK;
+  };
+  for (int i : todo) {
+    const MeshBvh& b = bvhs[i];
+    void* pw = nullptr;
+    void* pt = nullptr;
+    int st = up(b.wide.data(), b.wide.size() * sizeof(WideNode), &pw);
+    if (st == ILLUME_OK) st = up(b.wide_tris.data(), b.wide_tris.size() * sizeof(float4), &pt);
+    if (st != ILLUME_OK) { *err = last_error(); return st; }
+    t_meshes[i].wide = reinterpret_cast<const WideNode*>(pw);
+    t_meshes[i].wide_tris = reinterpret_cast<const float4*>(pt);
+  }
+  // the mesh table: the source the per-render re-uploads copy from, then its device copy
+  for (Upload& u : uploads)
+    if (u.dst == (const void*)view.meshes) {
+      if (u.src != t_meshes.data()) memcpy(const_cast<void*>(u.src), t_meshes.data(), u.bytes);
+      break;
+    }
+  ILLUME_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  ILLUME_CUDA_TRY(cudaMemcpy(const_cast<DevMesh*>(view.meshes), t_meshes.data(), sizeof(DevMesh) * (size_t)nm,
+                             cudaMemcpyHostToDevice));
   return ILLUME_OK;
 }
 

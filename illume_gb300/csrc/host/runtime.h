@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -138,6 +139,11 @@ struct Scene {
   double build_ms = 0.0, upload_ms = 0.0;
   int build_host(std::string* err);        // BVHs only (host-only scenes)
   int build_and_upload(std::string* err);  // BVHs + device tables
+  // The 8-wide layout of every mesh, built on first need (an 8-wide render, trace, check
+  // or digest) on the host cores and, for a scene on a device, uploaded (resident) with
+  // the device mesh table pointed at it. Renders of other layouts never wait for it.
+  int ensure_wide(std::string* err);
+  std::mutex wide_mu;
 };
 
 // Process-wide cache of mesh BVH builds keyed by mesh content (runtime.cpp).

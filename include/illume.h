@@ -60,7 +60,9 @@ enum illume_intersector { ILLUME_ISECT_MT = 0, ILLUME_ISECT_WATERTIGHT = 1 };
  * default of illume_render_params_default). BINARY: 64-byte nodes holding both child
  * boxes. WIDE8: 80-byte 8-wide nodes with 8-bit quantised child boxes. WIDE8_PERSISTENT:
  * the same nodes traversed by a persistent kernel that schedules node and triangle steps
- * per warp. All four give the same closest hits. */
+ * per warp. All four give the same closest hits. The 8-wide layout is built (on the host
+ * cores) and uploaded when a render, trace, check or digest first asks for it, so the
+ * first such call on a scene takes longer and must not be made under stream capture. */
 enum illume_bvh_kind { ILLUME_BVH_BINARY = 0, ILLUME_BVH_WIDE8 = 1, ILLUME_BVH_WIDE8_PERSISTENT = 2, ILLUME_BVH_WIDE4 = 3 };
 enum illume_accum_mode { ILLUME_ACCUM_FP32 = 0, ILLUME_ACCUM_KAHAN = 1, ILLUME_ACCUM_FP64 = 2 };
 /* REFERENCE: paths find light only by BSDF sampling, as src/renderer.cu:183-386 (the
