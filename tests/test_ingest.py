@@ -2,6 +2,7 @@
 the reference's own parse of the same files (tests/golden/ref_*.npz)."""
 import ctypes
 import json
+import re
 import os
 import struct
 
@@ -200,6 +201,99 @@ def test_obj_variants(native_lib, tmp_path):
     sd = host_scene_from_json(json.dumps(sc), str(tmp_path))
     assert sd.meshes[0].normals is not None
     assert np.allclose(np.linalg.norm(sd.meshes[0].normals, axis=1), 1.0)
+
+
+_FLOAT_PREFIX = re.compile(r"^\s*[+-]?(\d+\.?\d*(?:[eE][+-]?\d+)?|\.\d+(?:[eE][+-]?\d+)?)")
+_INT_PREFIX = re.compile(r"^\s*[+-]?\d+")
+
+
+def _strtof(tok):
+    m = _FLOAT_PREFIX.match(tok)
+    return np.float32(float(m.group(0))) if m else np.float32(0.0)
+
+
+def _strtol(tok):
+    m = _INT_PREFIX.match(tok)
+    return int(m.group(0)) if m else 0
+
+
+def _obj_expected(text, face_normals=True, has_texcoords=False):
+    """The loader's rules restated (mesh.cu:159-340 via load_obj_mesh): lines split on
+    newlines with one trailing CR dropped, fields on single spaces with empty ones dropped
+    (a tab stays inside its field), numbers read as strtof / strtol read a field's prefix,
+    the first three corners of a face, corners p, p/t, p//n or p/t/n with empty fields
+    dropped, vertices merged by value (+0 equal to -0) in first-use order, each taking the
+    values of its first corner. Normals in these cases are unit length already."""
+    v, vt, vn, corners = [], [], [], []
+    for line in text.split("\n"):
+        if line.endswith("\r"):
+            line = line[:-1]
+        tok = [t for t in line.split(" ") if t]
+        if not tok:
+            continue
+        fl = lambda k: _strtof(tok[k]) if k < len(tok) else np.float32(0.0)
+        if tok[0] == "v":
+            v.append((fl(1), fl(2), fl(3)))
+        elif tok[0] == "vt":
+            vt.append((fl(1), fl(2)))
+        elif tok[0] == "vn":
+            vn.append((fl(1), fl(2), fl(3)))
+        elif tok[0] == "f":
+            for t in tok[1:4]:
+                parts = [x for x in t.split("/") if x]
+                num = lambda k: _strtol(parts[k]) - 1 if k < len(parts) else -1
+                slashes = t.count("/")
+                c = [-1, -1, -1]
+                if slashes == 0:
+                    c = [num(0), -1, -1]
+                elif slashes == 1:
+                    c = [num(0), num(1), -1]
+                elif slashes == 2:
+                    c = [num(0), -1, num(1)] if "//" in t else [num(0), num(1), num(2)]
+                corners.append(c)
+    ids, pos, nrm, tex, tris = {}, [], [], [], []
+    for p, t, n in corners:
+        key = (v[p], vn[n] if not face_normals else None, vt[t] if has_texcoords else None)
+        if key not in ids:
+            ids[key] = len(ids)
+            pos.append(v[p])
+            if not face_normals:
+                nrm.append(vn[n])
+            if has_texcoords:
+                tex.append(vt[t])
+        tris.append(ids[key])
+    as32 = lambda a, k: np.array(a, np.float32).reshape(-1, k)
+    return as32(pos, 3), np.array(tris, np.int32).reshape(-1, 3), as32(nrm, 3), as32(tex, 2)
+
+
+def test_obj_parser_rules(native_lib, tmp_path):
+    text = ("# a comment\nv 0 0 0\nv -0 0 0\nv 1 0 0\r\nv  0   1  0\nv 0\t1 0\nv 2.5 -0 1e1\n"
+            "vt 0.5 0.25\nvt 0.5 0.25\nvt 1 1\nvn 0 0 1\nvn 0 1 0\nvn 0 0 1\n"
+            "f 2/1/1 3/2/3 4/3/1\nf 1/2/3 3/1/1 6/3/2\nf 5/1/1 6/2/2 4/3/3 2/1/1\n"
+            "f 6//2 1//1 3//3\nf +1/1/1 3/2/1 4/3/1\n")
+    (tmp_path / "r.obj").write_text(text)
+    for opts in ({}, {"face_normals": False}, {"has_texcoords": True}, {"face_normals": False, "has_texcoords": True}):
+        if opts.get("has_texcoords"):    # the "p//n" face has no texcoord: an error, checked below
+            body = text.replace("f 6//2 1//1 3//3\n", "")
+        else:
+            body = text
+        (tmp_path / "s.obj").write_text(body)
+        sc = {"meshes": [dict(file="s.obj", name="m", **opts)],
+              "materials": [{"name": "a", "type": "lambert", "albedo": [1, 1, 1]}],
+              "primitives": [{"type": "mesh_instance", "mesh": "m", "material": "a", "transform": {}}], "camera": CAM}
+        sd = host_scene_from_json(json.dumps(sc), str(tmp_path))
+        m = sd.meshes[0]
+        pos, tris, nrm, tex = _obj_expected(body, opts.get("face_normals", True), opts.get("has_texcoords", False))
+        assert np.array_equal(m.tris, tris), opts
+        assert np.array_equal(m.positions.view(np.uint32), pos.view(np.uint32)), opts   # signs of zeros too
+        if not opts.get("face_normals", True):
+            assert np.array_equal(m.normals, nrm), opts
+        if opts.get("has_texcoords"):
+            assert np.array_equal(m.texcoords, tex), opts
+    sc["meshes"] = [{"file": "r.obj", "name": "m", "has_texcoords": True}]
+    h = ctypes.c_void_p()
+    st = C.lib().illume_scene_load_json_string(None, json.dumps(sc).encode(), str(tmp_path).encode(), ctypes.byref(h))
+    assert st != C.OK and b"texcoord index" in C.lib().illume_last_error()
 
 
 def test_bitmap_texels_and_environment_like_the_reference(native_lib):
