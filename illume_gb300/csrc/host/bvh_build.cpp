@@ -448,8 +448,67 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
       out->bvh4.push_back(n);
       out->stats.bvh4_depth = 1;
     } else {
-      // children of each 4-wide node: start from the binary node's two children and pull
-      // up the largest-area inner child until there are four (or only leaves)
+      // children of each 4-wide node, chosen to minimise the total box area of the
+      // 4-wide nodes (the surface-area cost of the node visits; the leaves are the binary
+      // tree's either way). F[x][j - 1] = the least area of the 4-wide nodes below binary
+      // node x when x may fill up to j child slots of its parent: x itself as a node (its
+      // area plus the best split of its four slots between its children, split4[x]), or
+      // x opened and its slots split between its children (choice[x][j - 1] = the left
+      // child's share). Leaves cost nothing and fill one slot. Ties keep the lower split.
+      const int nbn = (int)bn.size();
+      std::vector<std::array<double, 4>> F(nbn);
+      std::vector<std::array<int8_t, 4>> choice(nbn);
+      std::vector<int8_t> split4(nbn, 0);
+      {
+        std::vector<int> post;
+        post.reserve(nbn);
+        std::vector<std::pair<int, bool>> st{{0, false}};
+        while (!st.empty()) {   // post order: children before their parent
+          const auto [x, seen] = st.back();
+          st.pop_back();
+          if (seen || bn[x].left < 0) { post.push_back(x); continue; }
+          st.push_back({x, true});
+          st.push_back({bn[x].right, false});
+          st.push_back({bn[x].left, false});
+        }
+        for (int x : post) {
+          if (bn[x].left < 0) {
+            F[x] = {0.0, 0.0, 0.0, 0.0};
+            choice[x] = {0, 0, 0, 0};
+            continue;
+          }
+          const int L = bn[x].left, R = bn[x].right;
+          double g = INFINITY;
+          for (int m = 1; m <= 3; ++m) {
+            const double c = F[L][m - 1] + F[R][4 - m - 1];
+            if (c < g) { g = c; split4[x] = (int8_t)m; }
+          }
+          F[x][0] = bn[x].box.area() + g;
+          choice[x][0] = 0;
+          for (int j = 2; j <= 4; ++j) {
+            double best = F[x][0];
+            int8_t ch = 0;
+            for (int m = 1; m < j; ++m) {
+              const double c = F[L][m - 1] + F[R][j - m - 1];
+              if (c < best) { best = c; ch = (int8_t)m; }
+            }
+            F[x][j - 1] = best;
+            choice[x][j - 1] = ch;
+          }
+        }
+      }
+      // the slots of binary node x given up to j of them
+      auto collect = [&](int x0, int j0, std::array<int, 4>& ch, int& nc) {
+        std::vector<std::pair<int, int>> work{{x0, j0}};
+        while (!work.empty()) {
+          const auto [x, j] = work.back();
+          work.pop_back();
+          if (bn[x].left < 0 || choice[x][j - 1] == 0) { ch[nc++] = x; continue; }
+          const int m = choice[x][j - 1];
+          work.push_back({bn[x].right, j - m});
+          work.push_back({bn[x].left, m});
+        }
+      };
       std::vector<std::array<int, 4>> kids;
       std::vector<int> nkids, depth4, map4(bn.size(), -1);
       std::vector<std::pair<int, int>> st4{{0, 1}};
@@ -457,18 +516,10 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
         const int i = st4.back().first, dpt = st4.back().second;
         st4.pop_back();
         map4[i] = (int)kids.size();
-        std::array<int, 4> ch{bn[i].left, bn[i].right, -1, -1};
-        int nc = 2;
-        while (nc < 4) {
-          int best = -1;
-          double ba = -1.0;
-          for (int k = 0; k < nc; ++k)
-            if (bn[ch[k]].left >= 0 && bn[ch[k]].box.area() > ba) { ba = bn[ch[k]].box.area(); best = k; }
-          if (best < 0) break;
-          const int c = ch[best];
-          ch[best] = bn[c].left;
-          ch[nc++] = bn[c].right;
-        }
+        std::array<int, 4> ch{-1, -1, -1, -1};
+        int nc = 0;
+        collect(bn[i].left, split4[i], ch, nc);
+        collect(bn[i].right, 4 - split4[i], ch, nc);
         kids.push_back(ch);
         nkids.push_back(nc);
         depth4.push_back(dpt);

@@ -3,8 +3,9 @@
 // * Binned SAH binary build (16 bins per axis on centroids).
 // * Binary layout (Bvh2Node, 64 B): both child boxes live in the parent node.
 // * 4-wide layout (Bvh4Node, 128 B): the binary tree (leaves of up to 4 triangles)
-//   collapsed by pulling up the largest-area inner child until a node has 4 children;
-//   it shares the binary layout's triangle records.
+//   collapsed into nodes of up to 4 children chosen by a dynamic program that minimises
+//   the summed box area of the 4-wide nodes; it shares the binary layout's triangle
+//   records.
 // * 8-wide layout (WideNode, 80 B): the binary tree collapsed greedily into nodes of up
 //   to 8 children, child slots ordered by ray octant, child boxes quantised to 8 bits per
 //   axis with outward rounding.
