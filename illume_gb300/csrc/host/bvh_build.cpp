@@ -144,6 +144,76 @@ void build_step(const Work& w, const std::vector<Box>& boxes, const std::vector<
   stack.push_back({nd.left, w.first, mid - w.first});
 }
 
+// Collapse of a binary tree into nodes of up to K children that minimises the summed box
+// area of the K-wide nodes (the surface-area cost of their visits; the leaves are the
+// binary tree's either way). F[x][j - 1] = the least area of the K-wide nodes below
+// binary node x when x may fill up to j child slots of its parent: x itself as a node (its
+// area plus the best split of its K slots between its children, split[x]), or x opened and
+// its slots split between its children (choice[x][j - 1] = the left child's share).
+// Leaves cost nothing and fill one slot. Ties keep the lower split.
+template <int K>
+struct WideCollapse {
+  const std::vector<BNode>& bn;
+  std::vector<std::array<double, K>> F;
+  std::vector<std::array<int8_t, K>> choice;
+  std::vector<int8_t> split;
+
+  explicit WideCollapse(const std::vector<BNode>& b) : bn(b), F(b.size()), choice(b.size()), split(b.size(), 0) {
+    std::vector<int> post;
+    post.reserve(bn.size());
+    std::vector<std::pair<int, bool>> st{{0, false}};
+    while (!st.empty()) {   // post order: children before their parent
+      const auto [x, seen] = st.back();
+      st.pop_back();
+      if (seen || bn[x].left < 0) { post.push_back(x); continue; }
+      st.push_back({x, true});
+      st.push_back({bn[x].right, false});
+      st.push_back({bn[x].left, false});
+    }
+    for (int x : post) {
+      if (bn[x].left < 0) {
+        F[x].fill(0.0);
+        choice[x].fill(0);
+        continue;
+      }
+      const int L = bn[x].left, R = bn[x].right;
+      double g = INFINITY;
+      for (int m = 1; m < K; ++m) {
+        const double c = F[L][m - 1] + F[R][K - m - 1];
+        if (c < g) { g = c; split[x] = (int8_t)m; }
+      }
+      F[x][0] = bn[x].box.area() + g;
+      choice[x][0] = 0;
+      for (int j = 2; j <= K; ++j) {
+        double best = F[x][0];
+        int8_t ch = 0;
+        for (int m = 1; m < j; ++m) {
+          const double c = F[L][m - 1] + F[R][j - m - 1];
+          if (c < best) { best = c; ch = (int8_t)m; }
+        }
+        F[x][j - 1] = best;
+        choice[x][j - 1] = ch;
+      }
+    }
+  }
+
+  // The children of the K-wide node made from inner binary node x (binary nodes, left
+  // to right), into out[0..K); returns their count.
+  int children(int x, int* out) const {
+    int nc = 0;
+    std::vector<std::pair<int, int>> work{{bn[x].right, K - split[x]}, {bn[x].left, split[x]}};
+    while (!work.empty()) {
+      const auto [y, j] = work.back();
+      work.pop_back();
+      if (bn[y].left < 0 || choice[y][j - 1] == 0) { out[nc++] = y; continue; }
+      const int m = choice[y][j - 1];
+      work.push_back({bn[y].right, j - m});
+      work.push_back({bn[y].left, m});
+    }
+    return nc;
+  }
+};
+
 // Binned SAH build; returns nodes (root at 0) and fills order. The top of the tree is
 // split on one thread until the pending subtrees are small; those are built on the host
 // cores (each into its own node list, on a disjoint range of `order`) and stitched in
@@ -448,67 +518,8 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
       out->bvh4.push_back(n);
       out->stats.bvh4_depth = 1;
     } else {
-      // children of each 4-wide node, chosen to minimise the total box area of the
-      // 4-wide nodes (the surface-area cost of the node visits; the leaves are the binary
-      // tree's either way). F[x][j - 1] = the least area of the 4-wide nodes below binary
-      // node x when x may fill up to j child slots of its parent: x itself as a node (its
-      // area plus the best split of its four slots between its children, split4[x]), or
-      // x opened and its slots split between its children (choice[x][j - 1] = the left
-      // child's share). Leaves cost nothing and fill one slot. Ties keep the lower split.
-      const int nbn = (int)bn.size();
-      std::vector<std::array<double, 4>> F(nbn);
-      std::vector<std::array<int8_t, 4>> choice(nbn);
-      std::vector<int8_t> split4(nbn, 0);
-      {
-        std::vector<int> post;
-        post.reserve(nbn);
-        std::vector<std::pair<int, bool>> st{{0, false}};
-        while (!st.empty()) {   // post order: children before their parent
-          const auto [x, seen] = st.back();
-          st.pop_back();
-          if (seen || bn[x].left < 0) { post.push_back(x); continue; }
-          st.push_back({x, true});
-          st.push_back({bn[x].right, false});
-          st.push_back({bn[x].left, false});
-        }
-        for (int x : post) {
-          if (bn[x].left < 0) {
-            F[x] = {0.0, 0.0, 0.0, 0.0};
-            choice[x] = {0, 0, 0, 0};
-            continue;
-          }
-          const int L = bn[x].left, R = bn[x].right;
-          double g = INFINITY;
-          for (int m = 1; m <= 3; ++m) {
-            const double c = F[L][m - 1] + F[R][4 - m - 1];
-            if (c < g) { g = c; split4[x] = (int8_t)m; }
-          }
-          F[x][0] = bn[x].box.area() + g;
-          choice[x][0] = 0;
-          for (int j = 2; j <= 4; ++j) {
-            double best = F[x][0];
-            int8_t ch = 0;
-            for (int m = 1; m < j; ++m) {
-              const double c = F[L][m - 1] + F[R][j - m - 1];
-              if (c < best) { best = c; ch = (int8_t)m; }
-            }
-            F[x][j - 1] = best;
-            choice[x][j - 1] = ch;
-          }
-        }
-      }
-      // the slots of binary node x given up to j of them
-      auto collect = [&](int x0, int j0, std::array<int, 4>& ch, int& nc) {
-        std::vector<std::pair<int, int>> work{{x0, j0}};
-        while (!work.empty()) {
-          const auto [x, j] = work.back();
-          work.pop_back();
-          if (bn[x].left < 0 || choice[x][j - 1] == 0) { ch[nc++] = x; continue; }
-          const int m = choice[x][j - 1];
-          work.push_back({bn[x].right, j - m});
-          work.push_back({bn[x].left, m});
-        }
-      };
+      // children of each 4-wide node: the collapse of least summed node area
+      const WideCollapse<4> wc(bn);
       std::vector<std::array<int, 4>> kids;
       std::vector<int> nkids, depth4, map4(bn.size(), -1);
       std::vector<std::pair<int, int>> st4{{0, 1}};
@@ -517,9 +528,7 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
         st4.pop_back();
         map4[i] = (int)kids.size();
         std::array<int, 4> ch{-1, -1, -1, -1};
-        int nc = 0;
-        collect(bn[i].left, split4[i], ch, nc);
-        collect(bn[i].right, 4 - split4[i], ch, nc);
+        const int nc = wc.children(i, ch.data());
         kids.push_back(ch);
         nkids.push_back(nc);
         depth4.push_back(dpt);
@@ -557,6 +566,7 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
     } else {
       // queue of (binary node, wide node index); children of one wide node are allocated
       // consecutively so that a child's index = child_base + rank among inner children
+      const WideCollapse<8> wc8(bn);
       std::vector<std::pair<int, int>> queue;
       out->wide.emplace_back();
       queue.push_back({0, 0});
@@ -568,23 +578,14 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
         const int wi = queue[head].second;
         ++head;
         max_depth = std::max(max_depth, depth_of[wi]);
-        // collapse: expand the largest inner child until 8 children
+        // children: the collapse of least summed node area (a root leaf alone)
         std::vector<int> kids;
         if (bn[b].left < 0) {
-          kids.push_back(b);  // root leaf
+          kids.push_back(b);
         } else {
-          kids = {bn[b].left, bn[b].right};
-          for (;;) {
-            if (kids.size() >= 8) break;
-            int best = -1;
-            double ba = -1;
-            for (size_t k = 0; k < kids.size(); ++k)
-              if (bn[kids[k]].left >= 0 && bn[kids[k]].box.area() > ba) { ba = bn[kids[k]].box.area(); best = (int)k; }
-            if (best < 0) break;
-            const int x = kids[best];
-            kids[best] = bn[x].left;
-            kids.push_back(bn[x].right);
-          }
+          int ch[8];
+          const int nk = wc8.children(b, ch);
+          kids.assign(ch, ch + nk);
         }
         // node box and octant slot assignment
         Box nb;

@@ -6,9 +6,9 @@
 //   collapsed into nodes of up to 4 children chosen by a dynamic program that minimises
 //   the summed box area of the 4-wide nodes; it shares the binary layout's triangle
 //   records.
-// * 8-wide layout (WideNode, 80 B): the binary tree collapsed greedily into nodes of up
-//   to 8 children, child slots ordered by ray octant, child boxes quantised to 8 bits per
-//   axis with outward rounding.
+// * 8-wide layout (WideNode, 80 B): the binary tree (leaves of up to 3 triangles)
+//   collapsed into nodes of up to 8 children by the same dynamic program, child slots
+//   ordered by ray octant, child boxes quantised to 8 bits per axis with outward rounding.
 // Triangle boxes are padded by a small absolute margin before building, so that a box
 // test evaluated in FP32 never rejects a ray whose FP32 triangle test reports a hit
 // (for ray origins within ~100x the mesh extent); quantisation only widens boxes.
