@@ -331,6 +331,12 @@ int build_cluster_tree_device(Context* ctx, const float* boxes6, int n, ClusterT
   ALLOC(d_merge_off, sizeof(int) * ((size_t)n + 1));
   ALLOC(d_keep_off, sizeof(int) * ((size_t)n + 1));
 #undef ALLOC
+  // every return below waits for the stream first, so no launch of this build is still
+  // in flight when its buffers are released (declared after them: destroyed before them)
+  struct Drain {
+    cudaStream_t s;
+    ~Drain() { cudaStreamSynchronize(s); }
+  } drain{st};
   ILLUME_CUDA_TRY(cudaMemcpyAsync(d_box.get(), boxes6, sizeof(float) * 6 * (size_t)n, cudaMemcpyHostToDevice, st));
   const unsigned init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
   ILLUME_CUDA_TRY(cudaMemcpyAsync(d_bounds.get(), init, sizeof(init), cudaMemcpyHostToDevice, st));
