@@ -108,3 +108,50 @@ def test_bvh_digest_rejects_a_bad_mesh_index(native_lib):
     out = (ctypes.c_uint64 * 4)()
     assert C.lib().illume_scene_bvh_digest(h, 1, out) == C.ERR_INVALID
     C.lib().illume_scene_destroy(h)
+
+
+def test_concurrent_scene_builds_match_serial_builds(native_lib):
+    """Host threads building, checking and digesting scenes at the same time (one scene per
+    thread; the BVH cache and the build's own worker threads shared) give the trees a
+    serial build gives: ctypes releases the interpreter lock for every library call, so
+    the calls overlap."""
+    import threading
+    from illume_gb300 import synth
+    L = C.lib()
+    meshes = [synth.displaced_icosphere(f, seed=s) for f, s in ((14, 1), (20, 2), (14, 1), (42, 3), (20, 2), (8, 4))]
+    assert L.illume_bvh_cache_clear() == C.OK
+    serial = []
+    for P, T in meshes:
+        h = _host_scene(P, T)
+        serial.append(_digest(h))
+        L.illume_scene_destroy(h)
+    assert L.illume_bvh_cache_clear() == C.OK
+    results, errors = {}, []
+    barrier = threading.Barrier(len(meshes))
+
+    def work(i):
+        try:
+            P, T = meshes[i]
+            barrier.wait(timeout=60)
+            got = []
+            for _ in range(3):
+                h = _host_scene(P.copy(), T.copy())
+                buf = ctypes.create_string_buffer(1 << 14)
+                assert L.illume_scene_check_bvh(h, buf, len(buf)) == C.OK, buf.value
+                got.append(_digest(h))
+                L.illume_scene_destroy(h)
+            results[i] = got
+        except Exception as e:          # reported by the main thread
+            errors.append((i, repr(e)))
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(len(meshes))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=300)
+    assert not errors, errors
+    for i in range(len(meshes)):
+        assert results[i] == [serial[i]] * 3, i
+    entries = _stats()[0]
+    assert entries == 4                    # four distinct meshes, each cached once
+    assert L.illume_bvh_cache_clear() == C.OK
