@@ -224,9 +224,74 @@ def cpu_baseline(sd, args, seconds):
     return rays / dt / 1e6, threads, desc
 
 
+def reference_integrator_line(args):
+    """The reference arm on the reference's own integrator: its src/ built for the host
+    (OpenMP) from the staged copy of the sources (oracle/build_ref.py), timed on the
+    traversal workload's full frame at 1 spp per step. Returns (line, None), or (None,
+    why) where that cannot run here (then the CPU restatement stands in)."""
+    if args.scene != "traversal" or args.workload != "traversal":
+        return None, "the reference's own integrator is timed on the traversal workload only"
+    from oracle import build_ref
+    if not (build_ref.available() or build_ref.staged_available()):
+        return None, "no copy of the reference sources here (oracle/build_ref.py stage)"
+    try:
+        from illume_gb300 import synth
+        from oracle import pyref
+        from oracle.time_ref_vs_port import write_scene
+        t0 = time.perf_counter()
+        pyref.lib(staged=True)
+        build_s = time.perf_counter() - t0
+        # the reference keeps a BVH file beside each OBJ and reuses it by name: one folder
+        # per mesh size
+        work = os.path.join(build_ref.WORK_DIR, f"bench_{args.tris}")
+        os.makedirs(work, exist_ok=True)
+        name = write_scene(work, args.tris)
+        t0 = time.perf_counter()
+        rs = pyref.RefScene(name, work, staged=True)
+        rs.set_env(synth.environment_map(1, 2048, 1024))
+        load_s = time.perf_counter() - t0
+    except Exception as e:  # a build or load failure: the restatement stands in
+        return None, f"the reference's integrator could not be built or loaded here: {e!r}"[:300]
+    W = H = args.res
+    threads = os.cpu_count() or 1
+
+    def step(k):
+        return rs.render(W, H, 1, args.depth, sample_begin=k, nthreads=threads)[2]
+
+    for k in range(args.warmup):
+        step(k)
+    rays = 0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        rays += step(args.warmup + k)
+    dt = time.perf_counter() - t0
+    rs.close()
+    v = rays / dt / 1e6
+    sample = (f"the {W}x{H} frame at 1 spp per step (depth {args.depth}; {rays} rays over {args.steps} steps), "
+              f"the reference's own integrator (its src/ built for the host with OpenMP, {threads} threads)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "mode": "the reference's own integrator on host cores",
+                   "material": "the reference's rough conductor 'Au' (Beckmann, alpha 0.2) for the GGX gold: "
+                               "the reference has no GGX",
+                   "pixels_per_step": W * H, "spp_per_step": 1, "l2": "n/a (CPU)",
+                   "reference_build_s": round(build_s, 1), "reference_scene_load_s": round(load_s, 1)},
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": threads, "kind": "reference",
+                         "sample": sample},
+        "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line, None
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
+        return
+    line, why = reference_integrator_line(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
         return
     from illume_gb300 import synth  # noqa: F401
     from oracle import pyoracle
@@ -250,8 +315,9 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "mode": "reference integrator on host cores",
-                   "pixels_per_step": int(len(pixels)), "spp_per_step": 1, "l2": "n/a (CPU)"},
+        "config": {"workload": WORKLOAD, "mode": "CPU restatement of the reference integrator on host cores",
+                   "pixels_per_step": int(len(pixels)), "spp_per_step": 1, "l2": "n/a (CPU)",
+                   "reference_integrator": why},
         "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{len(pixels)} paths per step (every 97th pixel, 1 spp, depth {args.depth}), "
                                    f"CPU restatement of the reference integrator (oracle/), OpenMP {threads} threads"},

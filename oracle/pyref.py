@@ -1,8 +1,9 @@
 """Python binding of the reference renderer built for the host (oracle/_ref/libillume_ref.so).
 
 TEST INFRASTRUCTURE: used to pin the oracle and to generate tests/golden/ fixtures in the
-build container, where the reference sources exist. Unavailable elsewhere (available()
-returns False), and never used by the product.
+build container, where the reference sources exist, and by the bench's reference arm
+(built there from the staged copy of the sources, build_ref.stage()). available() is
+False where there is no checkout; the product never uses it.
 """
 from __future__ import annotations
 
@@ -29,21 +30,26 @@ def available() -> bool:
 def quiet():
     """Silence the reference's printf output (fd 1) during a call."""
     sys.stdout.flush()
+    libc = ctypes.CDLL(None)
+    libc.fflush(None)
     saved = os.dup(1)
     devnull = os.open(os.devnull, os.O_WRONLY)
     os.dup2(devnull, 1)
     try:
         yield
     finally:
+        libc.fflush(None)   # the reference's printf output still in the C library's buffer
         os.dup2(saved, 1)
         os.close(saved)
         os.close(devnull)
 
 
-def lib():
+def lib(staged: bool = False):
+    """The loaded library; staged=True lets it be built from the staged copy of the
+    reference sources where there is no checkout (the bench's reference arm)."""
     global _LIB
     if _LIB is None:
-        path = build_ref.build()
+        path = build_ref.build(staged=staged)
         if path is None:
             raise RuntimeError("reference sources are not available here")
         L = ctypes.CDLL(path)
@@ -99,10 +105,11 @@ def _fp(a):
 class RefScene:
     """A scene loaded by the reference's HostScene + SceneRef on the host."""
 
-    def __init__(self, json_name: str, work_dir: str | None = None):
+    def __init__(self, json_name: str, work_dir: str | None = None, staged: bool = False):
         work = work_dir or build_ref.prepare_work_dir()
+        L = lib(staged)
         with quiet():
-            self.handle = lib().ref_scene_load(json_name.encode(), work.encode())
+            self.handle = L.ref_scene_load(json_name.encode(), work.encode())
         if not self.handle:
             raise RuntimeError(f"reference could not load {json_name}")
         w, h, b = c_int(), c_int(), c_float()

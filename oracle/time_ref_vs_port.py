@@ -1,11 +1,12 @@
 """CPU baseline check: the reference's own integrator built for the host (oracle/_ref)
 against the oracle port, timed on the same scene, frame and thread count.
 
-TEST INFRASTRUCTURE, build container only (the reference checkout is needed to build
-oracle/_ref). The bench's CPU baseline and reference arm run the port, because the
-reference's sources do not travel to the GPU machine; this script measures how the
+TEST INFRASTRUCTURE (the reference checkout, or its staged copy, is needed to build
+oracle/_ref). The bench's reference arm runs the reference's own integrator where it
+can be built (bench.py reference_integrator_line) and the port elsewhere; the CPU
+baseline inside the bench's own line runs the port. This script measures how the
 port's speed compares with the reference's own code on the triangle-heavy traversal
-scene, so the ratio can be stated beside the baseline.
+scene, so the ratio can be stated beside either baseline.
 
 The scene: the 100k-triangle displaced icosphere over the checkerboard ground with the
 synthetic 2048x1024 environment, written as reference JSON + OBJ. The reference knows
@@ -77,7 +78,7 @@ def main():
         print("reference sources not available")
         return
     build_ref.build()
-    work = os.path.join(build_ref.WORK_DIR, "timing")
+    work = os.path.join(build_ref.WORK_DIR, f"timing_{args.tris}")   # BVH files are reused by name
     os.makedirs(work, exist_ok=True)
     name = write_scene(work, args.tris)
     env = synth.environment_map(1, 2048, 1024)
