@@ -22,6 +22,28 @@ int build_threads() {
 
 namespace {
 
+// fn(t, begin, end) on contiguous chunks of [0, n), chunk t on thread t (the caller runs
+// chunk 0), with at most build_threads() chunks of at least min_chunk items each. Every
+// use combines the chunks' results in chunk order or by min / max / integer sums, so the
+// result does not depend on the number of threads.
+template <class Fn>
+void parallel_chunks(size_t n, size_t min_chunk, Fn&& fn) {
+  const size_t want = std::max<size_t>(1, n / std::max<size_t>(1, min_chunk));
+  const int threads = (int)std::min<size_t>((size_t)build_threads(), want);
+  if (threads <= 1) {
+    fn(0, (size_t)0, n);
+    return;
+  }
+  const size_t step = (n + threads - 1) / threads;
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) {
+    const size_t b = std::min(n, t * step), e = std::min(n, b + step);
+    pool.emplace_back([&fn, t, b, e] { fn(t, b, e); });
+  }
+  fn(0, (size_t)0, std::min(n, step));
+  for (auto& th : pool) th.join();
+}
+
 struct Box {
   double lo[3], hi[3];
   void reset() {
@@ -59,18 +81,42 @@ float up(double d) {
 
 struct Work { int node, first, count; };
 
-// One step of the top-down binned SAH build (16 bins per axis on centroids): the node
-// of `w` becomes a leaf, or is split and its two children are pushed.
-void build_step(const Work& w, const std::vector<Box>& boxes, const std::vector<double>& ctr, std::vector<int>& order,
-                int max_leaf, std::vector<BNode>& nodes, std::vector<Work>& stack) {
-  const int kBins = 16;
-  BNode nd;
+// The split of node w in the top-down binned SAH build (16 bins per axis on centroids):
+// nd gets the node's box and range; returns the first position of the right child in
+// `order` (the range partitioned), or -1 when the node is a leaf. With threads_free, the
+// bounds and the bins of a large node are gathered on the host threads (minima, maxima
+// and counts: the same values on any number of threads); the partition is sequential.
+int split_node(const Work& w, const std::vector<Box>& boxes, const std::vector<double>& ctr, std::vector<int>& order,
+               int max_leaf, bool threads_free, BNode& nd) {
+  constexpr int kBins = 16;
+  constexpr int kParallelNode = 1 << 16;   // nodes of at least this many primitives
+  constexpr size_t kChunk = 1 << 14;
+  const bool par = threads_free && w.count >= kParallelNode;
+  auto over = [&](auto&& body) {   // body(part, begin, end) over the node's range
+    if (par) parallel_chunks((size_t)w.count, kChunk, body);
+    else body(0, (size_t)0, (size_t)w.count);
+  };
+  const int nparts = par ? build_threads() : 1;
+  nd = BNode();
   nd.box.reset();
   Box cb;
   cb.reset();
-  for (int i = w.first; i < w.first + w.count; ++i) {
-    nd.box.grow(boxes[order[i]]);
-    cb.grow_pt(&ctr[3 * (size_t)order[i]]);
+  {
+    std::array<Box, 2> one;   // small nodes: no heap work per node
+    std::vector<std::array<Box, 2>> many(par ? nparts : 0);
+    std::array<Box, 2>* part = par ? many.data() : &one;
+    for (int t = 0; t < nparts; ++t) { part[t][0].reset(); part[t][1].reset(); }
+    over([&](int t, size_t b, size_t e) {
+      Box bx = part[t][0], cx = part[t][1];
+      for (size_t i = b; i < e; ++i) {
+        const int p = order[w.first + i];
+        bx.grow(boxes[p]);
+        cx.grow_pt(&ctr[3 * (size_t)p]);
+      }
+      part[t][0] = bx;
+      part[t][1] = cx;
+    });
+    for (int t = 0; t < nparts; ++t) { nd.box.grow(part[t][0]); cb.grow(part[t][1]); }
   }
   nd.first = w.first;
   nd.count = w.count;
@@ -79,20 +125,44 @@ void build_step(const Work& w, const std::vector<Box>& boxes, const std::vector<
   double best_cost = INFINITY;
   int best_axis = -1, best_bin = -1;
   if (w.count > 1) {
+    // the bins of the three axes in one sweep over the node's primitives
+    bool live[3];
+    double k[3];
     for (int a = 0; a < 3; ++a) {
       const double ext = cb.hi[a] - cb.lo[a];
-      if (!(ext > 0)) continue;
-      Box bb[kBins];
-      int bc[kBins] = {0};
-      for (int b = 0; b < kBins; ++b) bb[b].reset();
-      const double k = kBins / ext;
-      for (int i = w.first; i < w.first + w.count; ++i) {
-        const int p = order[i];
-        int b = (int)((ctr[3 * (size_t)p + a] - cb.lo[a]) * k);
-        b = std::min(std::max(b, 0), kBins - 1);
-        bb[b].grow(boxes[p]);
-        bc[b]++;
+      live[a] = ext > 0;
+      k[a] = live[a] ? kBins / ext : 0.0;
+    }
+    struct Bins { Box bb[3][kBins]; int bc[3][kBins]; };
+    Bins one;
+    std::vector<Bins> many(par ? nparts : 0);
+    Bins* part = par ? many.data() : &one;
+    for (int t = 0; t < nparts; ++t)
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < kBins; ++b) { part[t].bb[a][b].reset(); part[t].bc[a][b] = 0; }
+    over([&](int t, size_t b0, size_t e0) {
+      Bins& q = part[t];
+      for (size_t i = b0; i < e0; ++i) {
+        const int p = order[w.first + i];
+        for (int a = 0; a < 3; ++a) {
+          if (!live[a]) continue;
+          int b = (int)((ctr[3 * (size_t)p + a] - cb.lo[a]) * k[a]);
+          b = std::min(std::max(b, 0), kBins - 1);
+          q.bb[a][b].grow(boxes[p]);
+          q.bc[a][b]++;
+        }
       }
+    });
+    for (int t = 1; t < nparts; ++t)
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < kBins; ++b) {
+          part[0].bb[a][b].grow(part[t].bb[a][b]);
+          part[0].bc[a][b] += part[t].bc[a][b];
+        }
+    for (int a = 0; a < 3; ++a) {
+      if (!live[a]) continue;
+      const Box* bb = part[0].bb[a];
+      const int* bc = part[0].bc[a];
       double rarea[kBins];
       int rcount[kBins];
       Box acc;
@@ -116,10 +186,7 @@ void build_step(const Work& w, const std::vector<Box>& boxes, const std::vector<
     }
   }
   const bool make_leaf = w.count == 1 || (w.count <= max_leaf && leaf_cost <= best_cost);
-  if (make_leaf) {
-    nodes[w.node] = nd;
-    return;
-  }
+  if (make_leaf) return -1;
   int mid;
   if (best_axis < 0) {
     // all centroids coincide (or no valid split): object median
@@ -134,6 +201,19 @@ void build_step(const Work& w, const std::vector<Box>& boxes, const std::vector<
     });
     mid = (int)(it - order.begin());
     if (mid == w.first || mid == w.first + w.count) mid = w.first + w.count / 2;
+  }
+  return mid;
+}
+
+// One step of a sequential build: the node of `w` becomes a leaf, or is split and its two
+// children are pushed.
+void build_step(const Work& w, const std::vector<Box>& boxes, const std::vector<double>& ctr, std::vector<int>& order,
+                int max_leaf, std::vector<BNode>& nodes, std::vector<Work>& stack) {
+  BNode nd;
+  const int mid = split_node(w, boxes, ctr, order, max_leaf, false, nd);
+  if (mid < 0) {
+    nodes[w.node] = nd;
+    return;
   }
   nd.left = (int)nodes.size();
   nd.right = nd.left + 1;
@@ -159,18 +239,26 @@ struct WideCollapse {
   std::vector<int8_t> split;
 
   explicit WideCollapse(const std::vector<BNode>& b) : bn(b), F(b.size()), choice(b.size()), split(b.size(), 0) {
+    // children before their parents: both builders number a node's children after the
+    // node, so a sweep by descending index is bottom-up (a post-order walk otherwise)
+    const int n = (int)bn.size();
+    bool ordered = true;
+    for (int x = 0; x < n && ordered; ++x) ordered = bn[x].left < 0 || (bn[x].left > x && bn[x].right > x);
     std::vector<int> post;
-    post.reserve(bn.size());
-    std::vector<std::pair<int, bool>> st{{0, false}};
-    while (!st.empty()) {   // post order: children before their parent
-      const auto [x, seen] = st.back();
-      st.pop_back();
-      if (seen || bn[x].left < 0) { post.push_back(x); continue; }
-      st.push_back({x, true});
-      st.push_back({bn[x].right, false});
-      st.push_back({bn[x].left, false});
+    if (!ordered) {
+      post.reserve(bn.size());
+      std::vector<std::pair<int, bool>> st{{0, false}};
+      while (!st.empty()) {
+        const auto [x, seen] = st.back();
+        st.pop_back();
+        if (seen || bn[x].left < 0) { post.push_back(x); continue; }
+        st.push_back({x, true});
+        st.push_back({bn[x].right, false});
+        st.push_back({bn[x].left, false});
+      }
     }
-    for (int x : post) {
+    for (int q = 0; q < n; ++q) {
+      const int x = ordered ? n - 1 - q : post[q];
       if (bn[x].left < 0) {
         F[x].fill(0.0);
         choice[x].fill(0);
@@ -201,43 +289,112 @@ struct WideCollapse {
   // to right), into out[0..K); returns their count.
   int children(int x, int* out) const {
     int nc = 0;
-    std::vector<std::pair<int, int>> work{{bn[x].right, K - split[x]}, {bn[x].left, split[x]}};
-    while (!work.empty()) {
-      const auto [y, j] = work.back();
-      work.pop_back();
+    // at most K pending entries: each holds at least one of the node's K slots
+    int wy[2 * K], wj[2 * K], sp = 0;
+    wy[sp] = bn[x].right; wj[sp++] = K - split[x];
+    wy[sp] = bn[x].left; wj[sp++] = split[x];
+    while (sp > 0) {
+      --sp;
+      const int y = wy[sp], j = wj[sp];
       if (bn[y].left < 0 || choice[y][j - 1] == 0) { out[nc++] = y; continue; }
       const int m = choice[y][j - 1];
-      work.push_back({bn[y].right, j - m});
-      work.push_back({bn[y].left, m});
+      wy[sp] = bn[y].right; wj[sp++] = j - m;
+      wy[sp] = bn[y].left; wj[sp++] = m;
     }
     return nc;
   }
 };
 
 // Binned SAH build; returns nodes (root at 0) and fills order. The top of the tree is
-// split on one thread until the pending subtrees are small; those are built on the host
+// split level by level until the pending subtrees are small; those are built on the host
 // cores (each into its own node list, on a disjoint range of `order`) and stitched in
-// the order they were set aside. Neither the splits nor the size at which subtrees are
-// set aside depend on the thread count, so the node arrays are identical on any number
-// of cores.
+// the order a depth-first build sets them aside. Neither the splits nor the size at which
+// subtrees are set aside depend on the thread count, so the node arrays are identical on
+// any number of cores.
 std::vector<BNode> build_binary(const std::vector<Box>& boxes, std::vector<int>& order, int max_leaf) {
   const int N = (int)boxes.size();
   order.resize(N);
   for (int i = 0; i < N; ++i) order[i] = i;
   std::vector<double> ctr((size_t)N * 3);
-  for (int i = 0; i < N; ++i)
-    for (int a = 0; a < 3; ++a) ctr[3 * (size_t)i + a] = 0.5 * (boxes[i].lo[a] + boxes[i].hi[a]);
+  parallel_chunks((size_t)N, 1 << 15, [&](int, size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i)
+      for (int a = 0; a < 3; ++a) ctr[3 * i + a] = 0.5 * (boxes[i].lo[a] + boxes[i].hi[a]);
+  });
   std::vector<BNode> nodes;
   nodes.reserve(2 * (size_t)N + 1);
   nodes.emplace_back();
   const int threads = build_threads();
   const int grain = N > 20000 ? std::max(4096, N / 128) : N + 1;
-  std::vector<Work> stack{{0, 0, N}}, deferred;
-  while (!stack.empty()) {
-    const Work w = stack.back();
-    stack.pop_back();
-    if (w.count <= grain && w.count > max_leaf) { deferred.push_back(w); continue; }
-    build_step(w, boxes, ctr, order, max_leaf, nodes, stack);
+  std::vector<Work> deferred;
+  {
+    // The top of the tree, level by level: each node of a level is split on its own
+    // range of `order` (a level of many nodes on the threads node by node, one of few
+    // nodes with each node's bins gathered on all threads); nodes of at most `grain`
+    // primitives (and more than a leaf's) are set aside for the subtree builds. A
+    // depth-first replay then numbers the nodes and lists the set-aside subtrees as a
+    // sequential depth-first build would: the arrays do not depend on the threads.
+    struct Top {
+      Work w;
+      BNode nd;
+      int kid = -1;            // left child in `top` (the right one is kid + 1); -1: a leaf
+      bool deferred = false;
+    };
+    std::vector<Top> top(1);
+    top[0].w = Work{0, 0, N};
+    std::vector<int> level{0}, todo, mids, next_level;
+    while (!level.empty()) {
+      todo.clear();
+      for (int id : level) {
+        const Work& w = top[id].w;
+        if (w.count <= grain && w.count > max_leaf) top[id].deferred = true;
+        else todo.push_back(id);
+      }
+      mids.assign(todo.size(), -1);
+      if ((int)todo.size() < threads) {
+        for (size_t q = 0; q < todo.size(); ++q)
+          mids[q] = split_node(top[todo[q]].w, boxes, ctr, order, max_leaf, true, top[todo[q]].nd);
+      } else {
+        std::atomic<size_t> nx{0};
+        auto lw = [&]() {
+          for (size_t q = nx++; q < todo.size(); q = nx++)
+            mids[q] = split_node(top[todo[q]].w, boxes, ctr, order, max_leaf, false, top[todo[q]].nd);
+        };
+        std::vector<std::thread> lp;
+        for (int t = 1; t < threads; ++t) lp.emplace_back(lw);
+        lw();
+        for (auto& th : lp) th.join();
+      }
+      next_level.clear();
+      for (size_t q = 0; q < todo.size(); ++q) {
+        if (mids[q] < 0) continue;
+        const Work w = top[todo[q]].w;
+        const int kid = (int)top.size();
+        top[todo[q]].kid = kid;
+        top.emplace_back();
+        top.back().w = Work{-1, w.first, mids[q] - w.first};
+        top.emplace_back();
+        top.back().w = Work{-1, mids[q], w.first + w.count - mids[q]};
+        next_level.push_back(kid);
+        next_level.push_back(kid + 1);
+      }
+      level.swap(next_level);
+    }
+    std::vector<std::pair<int, int>> st{{0, 0}};   // (node of `top`, its slot in `nodes`)
+    while (!st.empty()) {
+      const auto [id, slot] = st.back();
+      st.pop_back();
+      const Top& t = top[id];
+      if (t.deferred) { deferred.push_back(Work{slot, t.w.first, t.w.count}); continue; }
+      BNode nd = t.nd;
+      if (t.kid < 0) { nodes[slot] = nd; continue; }
+      nd.left = (int)nodes.size();
+      nd.right = nd.left + 1;
+      nodes.emplace_back();
+      nodes.emplace_back();
+      nodes[slot] = nd;
+      st.push_back({t.kid + 1, nd.right});
+      st.push_back({t.kid, nd.left});
+    }
   }
   if (deferred.empty()) return nodes;
   std::vector<std::vector<BNode>> sub(deferred.size());
@@ -259,34 +416,62 @@ std::vector<BNode> build_binary(const std::vector<Box>& boxes, std::vector<int>&
   for (int t = 1; t < threads; ++t) pool.emplace_back(worker);
   worker();
   for (auto& th : pool) th.join();
-  // stitch: a subtree's root replaces its placeholder, the rest is appended
+  // stitch: a subtree's root replaces its placeholder, the rest is appended in the
+  // order the subtrees were set aside (subtree k's index j >= 1 -> base[k] + j)
+  std::vector<size_t> base(deferred.size());
+  size_t total = nodes.size();
   for (size_t k = 0; k < deferred.size(); ++k) {
-    const std::vector<BNode>& sn = sub[k];
-    const int base = (int)nodes.size() - 1;   // sub index j >= 1 -> base + j
-    auto remap = [&](BNode n) {
-      if (n.left >= 0) { n.left += base; n.right += base; }
-      return n;
-    };
-    nodes[deferred[k].node] = remap(sn[0]);
-    for (size_t j = 1; j < sn.size(); ++j) nodes.push_back(remap(sn[j]));
+    base[k] = total - 1;
+    total += sub[k].size() - 1;
   }
+  nodes.resize(total);
+  std::atomic<size_t> nk{0};
+  auto stitch = [&]() {
+    for (size_t k = nk++; k < deferred.size(); k = nk++) {
+      const std::vector<BNode>& sn = sub[k];
+      const int b = (int)base[k];
+      auto remap = [&](BNode n) {
+        if (n.left >= 0) { n.left += b; n.right += b; }
+        return n;
+      };
+      nodes[deferred[k].node] = remap(sn[0]);
+      for (size_t j = 1; j < sn.size(); ++j) nodes[base[k] + j] = remap(sn[j]);
+    }
+  };
+  std::vector<std::thread> sp;
+  for (int t = 1; t < threads; ++t) sp.emplace_back(stitch);
+  stitch();
+  for (auto& th : sp) th.join();
   return nodes;
 }
 
-void put_tri(std::vector<float4>& out, const float* P, const int* tri, int prim) {
+// A triangle record: three vertices, the primitive index in the first one's w.
+void put_tri(float4* out, const float* P, const int* tri, int prim) {
   const float* a = P + 3 * (size_t)tri[0];
   const float* b = P + 3 * (size_t)tri[1];
   const float* c = P + 3 * (size_t)tri[2];
   float w;
   memcpy(&w, &prim, 4);
-  out.push_back(float4{a[0], a[1], a[2], w});
-  out.push_back(float4{b[0], b[1], b[2], 0.0f});
-  out.push_back(float4{c[0], c[1], c[2], 0.0f});
+  out[0] = float4{a[0], a[1], a[2], w};
+  out[1] = float4{b[0], b[1], b[2], 0.0f};
+  out[2] = float4{c[0], c[1], c[2], 0.0f};
+}
+void put_tri(std::vector<float4>& out, const float* P, const int* tri, int prim) {
+  out.resize(out.size() + 3);
+  put_tri(&out[out.size() - 3], P, tri, prim);
 }
 
-int tree_depth(const std::vector<BNode>& n, int i) {
-  if (n[i].left < 0) return 1;
-  return 1 + std::max(tree_depth(n, n[i].left), tree_depth(n, n[i].right));
+int tree_depth(const std::vector<BNode>& n, int root) {
+  int best = 0;
+  std::vector<std::pair<int, int>> st{{root, 1}};
+  while (!st.empty()) {
+    const auto [i, d] = st.back();
+    st.pop_back();
+    if (n[i].left < 0) { best = std::max(best, d); continue; }
+    st.push_back({n[i].right, d + 1});
+    st.push_back({n[i].left, d + 1});
+  }
+  return best;
 }
 
 }  // namespace
@@ -369,15 +554,27 @@ std::vector<BNode> tree_from_clusters(const ClusterTree& ct, int max_leaf, std::
 void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, MeshBvh* out, Context* device,
                     int layouts) {
   if (!(layouts & kLayoutBinary4)) device = nullptr;   // the device tree serves the binary and 4-wide layouts
-  // padded triangle boxes
+  // padded triangle boxes (the mesh bounds are minima and maxima: any chunking gives them)
   double mlo[3] = {INFINITY, INFINITY, INFINITY}, mhi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (int i = 0; i < T; ++i)
-    for (int k = 0; k < 3; ++k)
+  {
+    std::vector<std::array<double, 6>> part(build_threads(), {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY,
+                                                              -INFINITY});
+    parallel_chunks((size_t)T, 1 << 15, [&](int t, size_t b, size_t e) {
+      std::array<double, 6>& r = part[t];
+      for (size_t i = b; i < e; ++i)
+        for (int k = 0; k < 3; ++k)
+          for (int a = 0; a < 3; ++a) {
+            const double v = P[3 * (size_t)tris[3 * i + k] + a];
+            r[a] = std::min(r[a], v);
+            r[3 + a] = std::max(r[3 + a], v);
+          }
+    });
+    for (const auto& r : part)
       for (int a = 0; a < 3; ++a) {
-        const double v = P[3 * (size_t)tris[3 * i + k] + a];
-        mlo[a] = std::min(mlo[a], v);
-        mhi[a] = std::max(mhi[a], v);
+        mlo[a] = std::min(mlo[a], r[a]);
+        mhi[a] = std::max(mhi[a], r[3 + a]);
       }
+  }
   double ext = 0, mag = 0;
   for (int a = 0; a < 3; ++a) {
     if (T > 0) {
@@ -387,18 +584,20 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
   }
   const double pad = ldexp(ext + mag, -16) + 1e-30;
   std::vector<Box> boxes(T);
-  for (int i = 0; i < T; ++i) {
-    boxes[i].reset();
-    for (int k = 0; k < 3; ++k) {
-      double p[3];
-      for (int a = 0; a < 3; ++a) p[a] = P[3 * (size_t)tris[3 * i + k] + a];
-      boxes[i].grow_pt(p);
+  parallel_chunks((size_t)T, 1 << 15, [&](int, size_t b, size_t e) {
+    for (size_t i = b; i < e; ++i) {
+      boxes[i].reset();
+      for (int k = 0; k < 3; ++k) {
+        double p[3];
+        for (int a = 0; a < 3; ++a) p[a] = P[3 * (size_t)tris[3 * i + k] + a];
+        boxes[i].grow_pt(p);
+      }
+      for (int a = 0; a < 3; ++a) {
+        boxes[i].lo[a] = (double)down(boxes[i].lo[a] - pad);
+        boxes[i].hi[a] = (double)up(boxes[i].hi[a] + pad);
+      }
     }
-    for (int a = 0; a < 3; ++a) {
-      boxes[i].lo[a] = (double)down(boxes[i].lo[a] - pad);
-      boxes[i].hi[a] = (double)up(boxes[i].hi[a] + pad);
-    }
-  }
+  });
   for (int a = 0; a < 3; ++a) {
     out->lo[a] = T ? down(mlo[a] - pad) : 0.0f;
     out->hi[a] = T ? up(mhi[a] + pad) : 0.0f;
@@ -426,9 +625,10 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
     std::vector<int> order;
     std::vector<BNode> bn = T ? binary(4, order) : std::vector<BNode>();
     out->bvh2.clear();
-    out->bvh2_tris.clear();
-    out->bvh2_tris.reserve((size_t)T * 3);
-    for (int i = 0; i < T; ++i) put_tri(out->bvh2_tris, P, tris + 3 * (size_t)order[i], order[i]);
+    out->bvh2_tris.resize((size_t)T * 3);
+    parallel_chunks((size_t)T, 1 << 15, [&](int, size_t b, size_t e) {
+      for (size_t i = b; i < e; ++i) put_tri(&out->bvh2_tris[3 * i], P, tris + 3 * (size_t)order[i], order[i]);
+    });
     auto encode_box = [](Bvh2Node& n, int slot, const Box& b) {
       float lo[3], hi[3];
       for (int a = 0; a < 3; ++a) { lo[a] = (float)b.lo[a]; hi[a] = (float)b.hi[a]; }
@@ -471,20 +671,24 @@ void build_mesh_bvh(const float* P, int num_vertices, const int* tris, int T, Me
           if (bn[bn[i].left].left >= 0) st.push_back(bn[i].left);
         }
         out->bvh2.resize(inner.size());
-        for (size_t k = 0; k < inner.size(); ++k) {
-          const BNode& b = bn[inner[k]];
-          Bvh2Node n{};
-          const BNode& L = bn[b.left];
-          const BNode& R = bn[b.right];
-          encode_box(n, 0, L.box);
-          encode_box(n, 1, R.box);
-          n.d.x = L.left >= 0 ? idx[b.left] : ~((L.first << 3) | L.count);
-          n.d.y = R.left >= 0 ? idx[b.right] : ~((R.first << 3) | R.count);
-          n.d.z = L.left >= 0 ? 0 : L.count;
-          n.d.w = R.left >= 0 ? 0 : R.count;
-          out->bvh2[k] = n;
-          out->stats.bvh2_leaves += (L.left < 0) + (R.left < 0);
-        }
+        std::vector<int> leaves(build_threads(), 0);
+        parallel_chunks(inner.size(), 1 << 15, [&](int t, size_t b0, size_t e0) {
+          for (size_t k = b0; k < e0; ++k) {
+            const BNode& b = bn[inner[k]];
+            Bvh2Node n{};
+            const BNode& L = bn[b.left];
+            const BNode& R = bn[b.right];
+            encode_box(n, 0, L.box);
+            encode_box(n, 1, R.box);
+            n.d.x = L.left >= 0 ? idx[b.left] : ~((L.first << 3) | L.count);
+            n.d.y = R.left >= 0 ? idx[b.right] : ~((R.first << 3) | R.count);
+            n.d.z = L.left >= 0 ? 0 : L.count;
+            n.d.w = R.left >= 0 ? 0 : R.count;
+            out->bvh2[k] = n;
+            leaves[t] += (L.left < 0) + (R.left < 0);
+          }
+        });
+        for (int c : leaves) out->stats.bvh2_leaves += c;
       }
       out->stats.bvh2_nodes = (int)out->bvh2.size();
       out->stats.bvh2_depth = tree_depth(bn, 0);
