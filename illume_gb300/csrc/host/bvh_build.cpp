@@ -14,10 +14,26 @@
 
 namespace illume {
 
-int build_threads() {
+static thread_local int t_thread_share = 0;   // 0: no share set on this thread
+
+static int all_build_threads() {
   const char* e = getenv("ILLUME_BUILD_THREADS");
   if (e && atoi(e) > 0) return std::min(256, atoi(e));
   return std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+}
+
+int build_threads() { return t_thread_share > 0 ? t_thread_share : all_build_threads(); }
+
+BuildThreadShare::BuildThreadShare(int share) : saved_(t_thread_share) { t_thread_share = std::max(1, share); }
+BuildThreadShare::~BuildThreadShare() { t_thread_share = saved_; }
+
+int build_thread_share(const int* sizes, int count, int builders) {
+  constexpr int kLarge = 1 << 15;   // meshes below this build on one thread anyway
+  int large = 0;
+  for (int i = 0; i < count; ++i) large += sizes[i] >= kLarge;
+  const int all = build_threads();
+  if (large <= 1) return all;
+  return std::max(1, all / std::max(1, std::min(large, builders)));
 }
 
 namespace {

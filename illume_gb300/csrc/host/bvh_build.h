@@ -50,8 +50,28 @@ struct MeshBvh {
 enum BuildLayouts { kLayoutBinary4 = 1, kLayoutWide = 2, kLayoutAll = 3 };
 
 // Host threads of a BVH build: ILLUME_BUILD_THREADS if set (>= 1), else the cores (at
-// most 16). The result does not depend on it.
+// most 16), unless the calling thread holds a share set by BuildThreadShare. The result
+// does not depend on it.
 int build_threads();
+
+// While alive, build_threads() on this thread returns `share` (>= 1): for builds that
+// run beside other builds on the same cores (one mesh per thread), so that their own
+// parallel passes do not oversubscribe the cores.
+class BuildThreadShare {
+ public:
+  explicit BuildThreadShare(int share);
+  ~BuildThreadShare();
+  BuildThreadShare(const BuildThreadShare&) = delete;
+  BuildThreadShare& operator=(const BuildThreadShare&) = delete;
+
+ private:
+  int saved_;
+};
+
+// The share of each of the builds that run together on `builders` threads: all cores
+// when at most one of `sizes` (triangles per mesh) is large enough to use more than one
+// thread, else the cores divided among the builders.
+int build_thread_share(const int* sizes, int count, int builders);
 
 struct Context;
 

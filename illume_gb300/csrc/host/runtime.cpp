@@ -370,9 +370,11 @@ int Scene::build_host(std::string* err) {
   bvhs.assign(nm, MeshBvh{});
   Context* device = ctx && ctx->bvh_builder == ILLUME_BVH_BUILD_DEVICE ? ctx : nullptr;
   const int nthreads = std::max(1, std::min<int>(nm, build_threads()));
+  const int share = build_thread_share(h.mesh_num_tris.data(), nm, nthreads);
   std::vector<std::thread> pool;
   std::atomic<int> next{0};
   auto work = [&]() {
+    const BuildThreadShare scope(share);
     for (int i = next++; i < nm; i = next++) {
       const float* P = h.positions.data() + 3 * (size_t)h.mesh_vertex_offset[i];
       const int* T = h.tris.data() + 3 * (size_t)h.mesh_tri_offset[i];
@@ -593,7 +595,12 @@ int Scene::ensure_wide(std::string* err) {
     if (!bvhs[i].has_wide) todo.push_back(i);
   if (todo.empty()) return ILLUME_OK;
   std::atomic<int> next{0};
+  std::vector<int> sizes;
+  for (int i : todo) sizes.push_back(h.mesh_num_tris[i]);
+  const int nthreads = std::max(1, std::min<int>((int)todo.size(), build_threads()));
+  const int share = build_thread_share(sizes.data(), (int)sizes.size(), nthreads);
   auto work = [&]() {
+    const BuildThreadShare scope(share);
     for (int k = next++; k < (int)todo.size(); k = next++) {
       const int i = todo[k];
       const float* P = h.positions.data() + 3 * (size_t)h.mesh_vertex_offset[i];
@@ -601,7 +608,6 @@ int Scene::ensure_wide(std::string* err) {
       build_mesh_bvh(P, h.mesh_num_vertices[i], T, h.mesh_num_tris[i], &bvhs[i], nullptr, kLayoutWide);
     }
   };
-  const int nthreads = std::max(1, std::min<int>((int)todo.size(), build_threads()));
   std::vector<std::thread> pool;
   for (int t = 1; t < nthreads; ++t) pool.emplace_back(work);
   work();
