@@ -298,8 +298,12 @@ __global__ void __launch_bounds__(128, MINB) k_shade(WaveBuffers w, int bounce_a
       const float4 qo = w.q_orig[parity][i];
       const float4 qd = w.q_dir[parity][i];
       const float4 qt = w.q_thr[parity][i];
-      const float4 hv = w.hit[i];
-      const int geom = w.hit_geom[i];
+      // The hit record is not gathered for escaped rays, whose record is what every trace
+      // kernel writes for no hit (FLT_MAX, 0, 0, prim -1, instance -1), nor for scatter
+      // events in a medium, which do not read it.
+      const bool no_hit = cls == EV_MISS || cls == EV_MEDIUM;
+      const float4 hv = no_hit ? make_float4(FLT_MAX, 0.0f, 0.0f, __int_as_float(-1)) : w.hit[i];
+      const int geom = no_hit ? -1 : w.hit_geom[i];
       const int g = __float_as_int(qo.w);
       const int packed = __float_as_int(qd.w);
       const int job = packed >> kMediumBits;
