@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["kernels/trace_kernels.cu", "kernels/integrator.cu", "kernels/noalloc.cu", "kernels/bvh_device.cu"]
 CPP_SOURCES = ["host/json.cpp", "host/mesh_io.cpp", "host/xform.cpp", "host/bvh_build.cpp", "host/runtime.cpp",
-               "host/scene_json.cpp", "host/image_io.cpp", "host/png_decode.cpp", "host/engine.cpp", "host/lights.cpp", "host/renderer.cpp", "host/server.cpp",
+               "host/scene_json.cpp", "host/image_io.cpp", "host/deflate_encode.cpp", "host/png_decode.cpp", "host/engine.cpp", "host/lights.cpp", "host/renderer.cpp", "host/server.cpp",
                "host/capi.cpp"]
 
 

@@ -1,12 +1,17 @@
 #include "image_io.h"
+
+#include "deflate_encode.h"
 #include "png_decode.h"
 
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+#include <atomic>
 #include <fstream>
 #include <sstream>
+#include <thread>
 
 namespace illume {
 
@@ -144,19 +149,72 @@ bool load_hdr(const std::vector<uint8_t>& d, Image* out, std::string* err) {
   return true;
 }
 
-uint32_t crc_table[256];
-bool crc_init = false;
-uint32_t crc32(const uint8_t* p, size_t n, uint32_t c = 0xffffffffu) {
-  if (!crc_init) {
+struct CrcTable {
+  uint32_t t[256];
+  CrcTable() {
     for (uint32_t i = 0; i < 256; ++i) {
       uint32_t v = i;
       for (int k = 0; k < 8; ++k) v = (v & 1) ? 0xedb88320u ^ (v >> 1) : v >> 1;
-      crc_table[i] = v;
+      t[i] = v;
     }
-    crc_init = true;
   }
-  for (size_t i = 0; i < n; ++i) c = crc_table[(c ^ p[i]) & 0xff] ^ (c >> 8);
+};
+uint32_t crc32(const uint8_t* p, size_t n, uint32_t c = 0xffffffffu) {
+  static const CrcTable table;   // built once, thread-safe
+  for (size_t i = 0; i < n; ++i) c = table.t[(c ^ p[i]) & 0xff] ^ (c >> 8);
   return c;
+}
+
+// The scanlines of an 8-bit RGB image, each behind the filter byte of the filter (none,
+// sub, up, average, Paeth; ISO 15948 9.2) whose output has the least sum of absolute
+// values read as signed bytes, the usual choice of PNG writers.
+std::vector<uint8_t> filtered_scanlines(const uint8_t* rgb, int w, int h) {
+  const size_t stride = (size_t)w * 3;
+  std::vector<uint8_t> raw((size_t)h * (stride + 1));
+  std::vector<uint8_t> zero(stride, 0);
+  auto mag = [](int v) { const uint8_t u = (uint8_t)v; return u < 128 ? (int)u : 256 - (int)u; };
+  auto paeth = [](int a, int b, int c) {
+    const int p = a + b - c, pa = p > a ? p - a : a - p, pb = p > b ? p - b : b - p, pc = p > c ? p - c : c - p;
+    return (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+  };
+  auto row = [&](int y) {
+    const uint8_t* cur = rgb + (size_t)y * stride;
+    const uint8_t* up = y > 0 ? rgb + (size_t)(y - 1) * stride : zero.data();
+    long s0 = 0, s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+    for (size_t i = 0; i < stride; ++i) {
+      const int x = cur[i], a = i >= 3 ? cur[i - 3] : 0, b = up[i], c = i >= 3 ? up[i - 3] : 0;
+      s0 += mag(x);
+      s1 += mag(x - a);
+      s2 += mag(x - b);
+      s3 += mag(x - ((a + b) >> 1));
+      s4 += mag(x - paeth(a, b, c));
+    }
+    const long sums[5] = {s0, s1, s2, s3, s4};
+    int f = 0;
+    for (int k = 1; k < 5; ++k)
+      if (sums[k] < sums[f]) f = k;
+    uint8_t* o = raw.data() + (size_t)y * (stride + 1);
+    o[0] = (uint8_t)f;
+    ++o;
+    for (size_t i = 0; i < stride; ++i) {
+      const int a = i >= 3 ? cur[i - 3] : 0, b = up[i], c = i >= 3 ? up[i - 3] : 0;
+      const int pred = f == 0 ? 0 : f == 1 ? a : f == 2 ? b : f == 3 ? (a + b) >> 1 : paeth(a, b, c);
+      o[i] = (uint8_t)(cur[i] - pred);
+    }
+  };
+  // rows filter independently (each reads the image, not its neighbours' output): bands
+  // of rows on the host threads
+  const int threads = (int)std::max(1u, std::min({16u, std::thread::hardware_concurrency(), (unsigned)(h / 64 + 1)}));
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int y0 = next.fetch_add(64); y0 < h; y0 = next.fetch_add(64))
+      for (int y = y0; y < std::min(h, y0 + 64); ++y) row(y);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < threads; ++t) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  return raw;
 }
 
 void be32(std::vector<uint8_t>& v, uint32_t x) {
@@ -186,28 +244,8 @@ bool load_image(const std::string& path, Image* out, std::string* err) {
 }
 
 bool save_png_rgb8(const std::string& path, const uint8_t* rgb, int w, int h, std::string* err) {
-  // raw scanlines, filter byte 0
-  std::vector<uint8_t> raw;
-  raw.reserve((size_t)h * (3 * w + 1));
-  for (int y = 0; y < h; ++y) {
-    raw.push_back(0);
-    raw.insert(raw.end(), rgb + (size_t)y * w * 3, rgb + (size_t)(y + 1) * w * 3);
-  }
-  // zlib stream of stored deflate blocks
-  std::vector<uint8_t> z{0x78, 0x01};
-  size_t pos = 0;
-  uint32_t a = 1, b = 0;
-  for (uint8_t c : raw) { a = (a + c) % 65521; b = (b + a) % 65521; }
-  do {
-    const size_t n = std::min<size_t>(65535, raw.size() - pos);
-    const bool last = pos + n == raw.size();
-    z.push_back(last ? 1 : 0);
-    z.push_back(n & 0xff); z.push_back(n >> 8);
-    z.push_back(~n & 0xff); z.push_back((~n >> 8) & 0xff);
-    z.insert(z.end(), raw.begin() + pos, raw.begin() + pos + n);
-    pos += n;
-  } while (pos < raw.size());
-  be32(z, (b << 16) | a);
+  const std::vector<uint8_t> raw = filtered_scanlines(rgb, w, h);
+  const std::vector<uint8_t> z = zlib_compress(raw.data(), raw.size());
   std::vector<uint8_t> png{0x89, 'P', 'N', 'G', 0x0d, 0x0a, 0x1a, 0x0a};
   std::vector<uint8_t> ihdr;
   be32(ihdr, (uint32_t)w);
