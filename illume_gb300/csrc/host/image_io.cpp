@@ -66,6 +66,211 @@ bool load_pfm(const std::vector<uint8_t>& d, Image* out, std::string* err) {
   return true;
 }
 
+uint32_t le16(const std::vector<uint8_t>& d, size_t p) { return d[p] | (uint32_t)d[p + 1] << 8; }
+uint32_t le32(const std::vector<uint8_t>& d, size_t p) {
+  return d[p] | (uint32_t)d[p + 1] << 8 | (uint32_t)d[p + 2] << 16 | (uint32_t)d[p + 3] << 24;
+}
+
+// Windows bitmap: uncompressed (BI_RGB) 4 and 8 bits per pixel through the palette, 24
+// (B, G, R) and 32 bits (B, G, R, A; or BI_BITFIELDS with byte-aligned masks); rows padded
+// to 4 bytes, bottom-up unless the height is negative. As stb_image 2.14 reads it (the
+// reference's loader, texture.cu:36-65): 8-bit texels, alpha 255 where there is none;
+// 1-bit files, which it refuses, are refused too (the texture becomes black in both).
+bool load_bmp(const std::vector<uint8_t>& d, Image* out, std::string* err) {
+  if (d.size() < 26 || d[0] != 'B' || d[1] != 'M') { *err = "not a BMP file"; return false; }
+  const size_t offset = le32(d, 10), hsz = le32(d, 14);
+  if (hsz != 12 && hsz != 40 && hsz != 56 && hsz != 108 && hsz != 124) { *err = "unsupported BMP header"; return false; }
+  long w, h;
+  int bpp, comp = 0, ncolors = 0;
+  if (hsz == 12) {
+    w = (int16_t)le16(d, 18);
+    h = (int16_t)le16(d, 20);
+    bpp = (int)le16(d, 24);
+  } else {
+    if (d.size() < 14 + hsz) { *err = "truncated BMP file"; return false; }
+    w = (int32_t)le32(d, 18);
+    h = (int32_t)le32(d, 22);
+    bpp = (int)le16(d, 28);
+    comp = (int)le32(d, 30);
+    ncolors = (int)le32(d, 46);
+  }
+  const bool top_down = h < 0;
+  if (h < 0) h = -h;
+  if (w <= 0 || h <= 0 || w > (1 << 16) || h > (1 << 16)) { *err = "bad BMP size"; return false; }
+  uint32_t mask[4] = {0x00ff0000u, 0x0000ff00u, 0x000000ffu, 0xff000000u};
+  if (comp == 3) {
+    if (bpp != 32) { *err = "unsupported BMP bit fields"; return false; }
+    const size_t mp = 54;   // the masks follow a 40-byte header, or sit at the same place inside a longer one
+    if (d.size() < mp + 12) { *err = "truncated BMP file"; return false; }
+    mask[0] = le32(d, mp);
+    mask[1] = le32(d, mp + 4);
+    mask[2] = le32(d, mp + 8);
+    mask[3] = hsz >= 56 && d.size() >= mp + 16 ? le32(d, mp + 12) : 0;
+    for (int c = 0; c < 3; ++c) {
+      uint32_t m = mask[c];
+      int sh = 0;
+      while (m && !(m & 1)) { m >>= 1; ++sh; }
+      if (m != 0xff || sh % 8) { *err = "unsupported BMP bit fields"; return false; }
+    }
+  } else if (comp != 0) {
+    *err = "unsupported BMP compression";
+    return false;
+  }
+  if (bpp != 4 && bpp != 8 && bpp != 24 && bpp != 32) { *err = "unsupported BMP bit depth"; return false; }
+  uint8_t pal[256][3] = {};
+  if (bpp <= 8) {
+    const int entry = hsz == 12 ? 3 : 4;
+    const int n = ncolors > 0 && ncolors <= 256 ? ncolors : 1 << bpp;
+    const size_t pp = 14 + hsz;
+    if (d.size() < pp + (size_t)n * entry) { *err = "truncated BMP palette"; return false; }
+    for (int i = 0; i < n; ++i)
+      for (int c = 0; c < 3; ++c) pal[i][c] = d[pp + (size_t)i * entry + 2 - c];   // stored B, G, R
+  }
+  const size_t stride = (((size_t)w * bpp + 31) / 32) * 4;
+  if (offset + stride * h > d.size()) { *err = "truncated BMP file"; return false; }
+  out->width = (int)w;
+  out->height = (int)h;
+  out->hdr = false;
+  out->rgba.assign((size_t)w * h * 4, 255.0f);
+  auto shift_of = [](uint32_t m) { int s = 0; while (m && !(m & 1)) { m >>= 1; ++s; } return s; };
+  const int sh[4] = {shift_of(mask[0]), shift_of(mask[1]), shift_of(mask[2]), shift_of(mask[3])};
+  for (long y = 0; y < h; ++y) {
+    const uint8_t* row = d.data() + offset + stride * (size_t)(top_down ? y : h - 1 - y);
+    float* o = &out->rgba[(size_t)y * w * 4];
+    for (long x = 0; x < w; ++x, o += 4) {
+      if (bpp <= 8) {
+        const int per = 8 / bpp;
+        const int idx = (row[x / per] >> (8 - bpp * (x % per + 1))) & ((1 << bpp) - 1);
+        for (int c = 0; c < 3; ++c) o[c] = pal[idx][c];
+      } else if (bpp == 24) {
+        for (int c = 0; c < 3; ++c) o[c] = row[3 * x + 2 - c];
+      } else {
+        const uint32_t v = row[4 * x] | (uint32_t)row[4 * x + 1] << 8 | (uint32_t)row[4 * x + 2] << 16 |
+                           (uint32_t)row[4 * x + 3] << 24;
+        for (int c = 0; c < 3; ++c) o[c] = (float)((v & mask[c]) >> sh[c]);
+        if (mask[3]) o[3] = (float)((v & mask[3]) >> sh[3]);
+      }
+    }
+  }
+  return true;
+}
+
+// Truevision TGA: colour-mapped (1), true-colour (2) and grey (3) images, run-length coded
+// or not (9, 10, 11), 8, 15/16 (5 bits a channel, scaled by 255 / 31 as integers), 24
+// and 32 bits per pixel (B, G, R[, A]); bottom-up unless the descriptor's bit 5 is set.
+// As stb_image 2.14 reads it (the reference's loader): 8-bit texels, grey replicated. One
+// deviation: a colour map whose first entry index is not 0 is read as the format defines
+// it (pixel index minus first entry); stb_image 2.14 skips that many bytes instead.
+bool load_tga(const std::vector<uint8_t>& d, Image* out, std::string* err) {
+  if (d.size() < 18) { *err = "not a TGA file"; return false; }
+  const int idlen = d[0], cmtype = d[1], type = d[2];
+  const int cm_first = (int)le16(d, 3), cm_len = (int)le16(d, 5), cm_bits = d[7];
+  const int w = (int)le16(d, 12), h = (int)le16(d, 14), bpp = d[16], desc = d[17];
+  const int base = type & 7;
+  const bool rle = type & 8;
+  if ((base != 1 && base != 2 && base != 3) || (type & ~11) || w <= 0 || h <= 0) { *err = "unsupported TGA type"; return false; }
+  if ((base == 1 && (cmtype != 1 || bpp != 8)) || (base == 3 && bpp != 8) ||
+      (base == 2 && bpp != 15 && bpp != 16 && bpp != 24 && bpp != 32)) {
+    *err = "unsupported TGA bit depth";
+    return false;
+  }
+  size_t pos = 18 + (size_t)idlen;
+  // one pixel of `bits` at p as R, G, B, A
+  auto decode = [](const uint8_t* p, int bits, uint8_t* rgba) {
+    if (bits == 8) {
+      rgba[0] = rgba[1] = rgba[2] = p[0];
+      rgba[3] = 255;
+    } else if (bits == 15 || bits == 16) {
+      const uint32_t v = p[0] | (uint32_t)p[1] << 8;
+      rgba[0] = (uint8_t)(((v >> 10) & 31) * 255 / 31);
+      rgba[1] = (uint8_t)(((v >> 5) & 31) * 255 / 31);
+      rgba[2] = (uint8_t)((v & 31) * 255 / 31);
+      rgba[3] = 255;
+    } else {
+      rgba[0] = p[2];
+      rgba[1] = p[1];
+      rgba[2] = p[0];
+      rgba[3] = bits == 32 ? p[3] : 255;
+    }
+  };
+  std::vector<uint8_t> pal;
+  if (cmtype == 1) {
+    const int eb = (cm_bits + 7) / 8;
+    if (pos + (size_t)cm_len * eb > d.size()) { *err = "truncated TGA palette"; return false; }
+    if (base == 1) {
+      if (cm_bits != 15 && cm_bits != 16 && cm_bits != 24 && cm_bits != 32) { *err = "unsupported TGA palette"; return false; }
+      pal.resize((size_t)cm_len * 4);
+      for (int i = 0; i < cm_len; ++i) decode(d.data() + pos + (size_t)i * eb, cm_bits, &pal[4 * (size_t)i]);
+    }
+    pos += (size_t)cm_len * eb;
+  }
+  const int pb = (bpp + 7) / 8;
+  const size_t npx = (size_t)w * h;
+  std::vector<uint8_t> px(npx * 4);
+  auto put = [&](size_t k, const uint8_t* p) {
+    if (base == 1) {
+      const int idx = p[0] - cm_first;
+      for (int c = 0; c < 4; ++c) px[4 * k + c] = idx >= 0 && idx < cm_len ? pal[4 * (size_t)idx + c] : 0;
+    } else {
+      decode(p, bpp, &px[4 * k]);
+    }
+  };
+  for (size_t k = 0; k < npx;) {
+    if (!rle) {
+      if (pos + pb > d.size()) { *err = "truncated TGA file"; return false; }
+      put(k++, d.data() + pos);
+      pos += pb;
+      continue;
+    }
+    if (pos >= d.size()) { *err = "truncated TGA file"; return false; }
+    const int head = d[pos++], n = (head & 127) + 1;
+    if (head & 128) {
+      if (pos + pb > d.size()) { *err = "truncated TGA file"; return false; }
+      for (int r = 0; r < n && k < npx; ++r) put(k++, d.data() + pos);
+      pos += pb;
+    } else {
+      for (int r = 0; r < n && k < npx; ++r) {
+        if (pos + pb > d.size()) { *err = "truncated TGA file"; return false; }
+        put(k++, d.data() + pos);
+        pos += pb;
+      }
+    }
+  }
+  const bool top_down = (desc & 0x20) != 0;
+  out->width = w;
+  out->height = h;
+  out->hdr = false;
+  out->rgba.resize(npx * 4);
+  for (int y = 0; y < h; ++y) {
+    const size_t src = (size_t)(top_down ? y : h - 1 - y) * w;
+    for (int x = 0; x < w; ++x)
+      for (int c = 0; c < 4; ++c) out->rgba[4 * ((size_t)y * w + x) + c] = px[4 * (src + x) + c];
+  }
+  return true;
+}
+
+// binary PGM (P5, maxval <= 255): grey replicated to R, G, B
+bool load_pgm(const std::vector<uint8_t>& d, Image* out, std::string* err) {
+  size_t pos = 0;
+  std::string tok[4];
+  int fields = 0;
+  while (pos < d.size() && fields < 4) {
+    while (pos < d.size() && isspace(d[pos])) ++pos;
+    if (pos < d.size() && d[pos] == '#') { while (pos < d.size() && d[pos] != '\n') ++pos; continue; }
+    while (pos < d.size() && !isspace(d[pos])) tok[fields] += (char)d[pos++];
+    ++fields;
+  }
+  ++pos;
+  if (fields < 4 || tok[0] != "P5") { *err = "not a binary PGM file"; return false; }
+  const int w = atoi(tok[1].c_str()), h = atoi(tok[2].c_str()), mx = atoi(tok[3].c_str());
+  if (w <= 0 || h <= 0 || mx <= 0 || mx > 255 || d.size() < pos + (size_t)w * h) { *err = "truncated PGM file"; return false; }
+  out->width = w; out->height = h; out->hdr = false;
+  out->rgba.assign((size_t)w * h * 4, 255.0f);
+  for (size_t i = 0; i < (size_t)w * h; ++i)
+    for (int c = 0; c < 3; ++c) out->rgba[4 * i + c] = (float)d[pos + i];
+  return true;
+}
+
 // binary PPM (P6, maxval <= 255)
 bool load_ppm(const std::vector<uint8_t>& d, Image* out, std::string* err) {
   size_t pos = 0;
@@ -237,6 +442,9 @@ bool load_image(const std::string& path, Image* out, std::string* err) {
   const std::string e = lower_ext(path);
   if (e == "pfm") return load_pfm(d, out, err);
   if (e == "ppm") return load_ppm(d, out, err);
+  if (e == "pgm") return load_pgm(d, out, err);
+  if (e == "bmp") return load_bmp(d, out, err);
+  if (e == "tga") return load_tga(d, out, err);
   if (e == "hdr") return load_hdr(d, out, err);
   if (e == "png") return decode_png(d, out, err);
   *err = "unsupported image format ." + e + " (" + path + ")";

@@ -1,6 +1,6 @@
-// Image files: texture input (Radiance .hdr, .pfm, binary .ppm, .png) and render output
-// (8-bit RGB .png and .ppm, float .pfm). The PNG writer stores deflate blocks without
-// compression, so it needs no zlib.
+// Image files: texture input (Radiance .hdr, .pfm, binary .ppm / .pgm, .png, .bmp, .tga)
+// and render output (8-bit RGB .png and .ppm, float .pfm). The PNG writer compresses with
+// the library's own deflate encoder (deflate_encode.h), so it needs no zlib.
 #pragma once
 
 #include <stdint.h>

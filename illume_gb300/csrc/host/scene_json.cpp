@@ -13,7 +13,7 @@
 // warning: ior 1.5, the identity transform, ray_bias 0. Numbers written as integers are
 // accepted wherever the reference reads a float. Extensions: "eta"/"k" arrays on
 // conductors, "distribution": "ggx" | "beckmann" on rough materials, and bitmap
-// textures in the .pfm / .hdr / .ppm / .png formats.
+// textures in the .pfm / .hdr / .ppm / .pgm / .png / .bmp / .tga formats.
 #include <math.h>
 #include <stdio.h>
 #include <string.h>

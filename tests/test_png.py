@@ -172,3 +172,27 @@ def test_corrupt_png_becomes_black(native_lib, tmp_path):
     (tmp_path / "bad.png").write_bytes(bytes(data))
     t = load(tmp_path, "bad.png")
     assert t.type == C.TEX_CONSTANT
+
+
+def _format_cases():
+    from conftest import golden
+    z = golden("ref_image_formats.npz")
+    return z, sorted(k[len("file_"):] for k in z.files if k.startswith("file_"))
+
+
+@pytest.mark.parametrize("key", _format_cases()[1])
+def test_bmp_tga_pgm_decode_like_the_reference(native_lib, tmp_path, key):
+    """BMP (1/4/8/24/32 bits, core / info / V4 headers, bit fields, both row orders), TGA
+    (colour-mapped, true-colour and grey, raw and run-length, 8/16/24/32 bits, both row
+    orders) and PGM files: the texels equal the ones the reference's own loader gives
+    (tests/golden/make_image_formats.py); a file it cannot read is black for both."""
+    z, _ = _format_cases()
+    name = str(z["name_" + key])
+    (tmp_path / name).write_bytes(z["file_" + key].tobytes())
+    want = z["texels_" + key]
+    tex = load(tmp_path, name)
+    if tex.type == C.TEX_CONSTANT:     # the loader refused the file: a black constant
+        assert not want.any(), name
+        return
+    got = np.asarray(tex.texels, np.float32).reshape(want.shape[0], want.shape[1], 4)[..., :3] / np.float32(255)
+    assert np.array_equal(got, want), (name, np.argwhere(got != want)[:5])
