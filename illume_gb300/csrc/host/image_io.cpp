@@ -96,7 +96,10 @@ bool load_bmp(const std::vector<uint8_t>& d, Image* out, std::string* err) {
   }
   const bool top_down = h < 0;
   if (h < 0) h = -h;
-  if (w <= 0 || h <= 0 || w > (1 << 16) || h > (1 << 16)) { *err = "bad BMP size"; return false; }
+  if (w <= 0 || h <= 0 || w > (1 << 16) || h > (1 << 16) || (long long)w * h > (1LL << 28)) {
+    *err = "bad BMP size";
+    return false;
+  }
   uint32_t mask[4] = {0x00ff0000u, 0x0000ff00u, 0x000000ffu, 0xff000000u};
   if (comp == 3) {
     if (bpp != 32) { *err = "unsupported BMP bit fields"; return false; }
@@ -169,6 +172,7 @@ bool load_tga(const std::vector<uint8_t>& d, Image* out, std::string* err) {
   const int base = type & 7;
   const bool rle = type & 8;
   if ((base != 1 && base != 2 && base != 3) || (type & ~11) || w <= 0 || h <= 0) { *err = "unsupported TGA type"; return false; }
+  if ((long long)w * h > (1LL << 28)) { *err = "bad TGA size"; return false; }
   if ((base == 1 && (cmtype != 1 || bpp != 8)) || (base == 3 && bpp != 8) ||
       (base == 2 && bpp != 15 && bpp != 16 && bpp != 24 && bpp != 32)) {
     *err = "unsupported TGA bit depth";
@@ -206,6 +210,11 @@ bool load_tga(const std::vector<uint8_t>& d, Image* out, std::string* err) {
   }
   const int pb = (bpp + 7) / 8;
   const size_t npx = (size_t)w * h;
+  // no allocation beyond what the file can hold: raw pixels, or 128 per run-length packet
+  if ((!rle && pos + npx * pb > d.size()) || (rle && npx > 128 * (d.size() - std::min(pos, d.size())))) {
+    *err = "truncated TGA file";
+    return false;
+  }
   std::vector<uint8_t> px(npx * 4);
   auto put = [&](size_t k, const uint8_t* p) {
     if (base == 1) {

@@ -196,3 +196,26 @@ def test_bmp_tga_pgm_decode_like_the_reference(native_lib, tmp_path, key):
         return
     got = np.asarray(tex.texels, np.float32).reshape(want.shape[0], want.shape[1], 4)[..., :3] / np.float32(255)
     assert np.array_equal(got, want), (name, np.argwhere(got != want)[:5])
+
+
+def test_mutated_bmp_tga_pgm_files_load_or_turn_black(native_lib, tmp_path):
+    """Byte flips, overwritten words and truncations of the format fixtures: every file
+    loads as some texture or is refused (a black constant); none crashes the loader."""
+    z, keys = _format_cases()
+    rng = np.random.default_rng(0)
+    for key in keys:
+        name = str(z["name_" + key])
+        data = bytearray(z["file_" + key].tobytes())
+        for trial in range(40):
+            d = bytearray(data)
+            if trial % 3 == 0:
+                for _ in range(int(rng.integers(1, 6))):
+                    d[int(rng.integers(0, len(d)))] = int(rng.integers(0, 256))
+            elif trial % 3 == 1:
+                d = d[:int(rng.integers(0, len(d)))]
+            else:
+                i = int(rng.integers(0, max(1, len(d) - 4)))
+                d[i:i + 4] = bytes(int(v) for v in rng.integers(0, 256, 4))
+            (tmp_path / name).write_bytes(bytes(d))
+            tex = load(tmp_path, name)
+            assert tex.type in (C.TEX_CONSTANT, C.TEX_BITMAP)
